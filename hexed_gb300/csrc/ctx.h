@@ -1,0 +1,82 @@
+// ctx.h -- device context behind the opaque hexed_gpu_ctx handle.
+#pragma once
+#include <cuda_runtime.h>
+#include "../../include/hexed_gpu.h"
+
+namespace hx {
+
+struct HostTables {
+  const double* node; const double* weight; const double* diff; const double* bound;
+  const double* filter; const double* prolong; const double* restrict_; const double* ortho;
+  double max_cfl, min_eig_diffusion, step_ratio;
+};
+
+struct Ctx;
+
+// Per-kernel CUDA-event timing, the device analogue of the reference's per-kernel
+// Stopwatch_tree hooks (include/kernel_factory.hpp:32-45). Off unless enabled.
+struct Profiler {
+  static constexpr int max_events = 8192;
+  static constexpr int max_names = 64;
+  bool enabled = false;
+  cudaEvent_t events[max_events];
+  int event_name[max_events/2];
+  int n_pairs = 0;
+  bool created = false;
+  const char* names[max_names];
+  int n_names = 0;
+  int launches[max_names];
+  double total_ms[max_names];
+};
+
+// Launch sequences of one (n_dim, row_size, precision); all enqueue on Ctx::stream.
+struct OpsTable {
+  void (*compute_euler)(Ctx&, int stage, int compute_residual, int use_filter, bool fuse_bc);
+  void (*compute_navier_stokes)(Ctx&, int stage, int compute_residual, int use_filter,
+                                const hexed_transport& visc, const hexed_transport& cond, bool fuse_bc);
+  void (*max_dt)(Ctx&, double msc, double msd, int local_time, int viscous, const hexed_transport& visc,
+                 const hexed_transport& cond, double max_time_step, double cheby);
+  void (*refine)(Ctx&, bool prolong, bool scale, bool offset);
+  void (*write_face)(Ctx&);
+  void (*bc_state)(Ctx&);
+  void (*bc_flux)(Ctx&);
+  void (*residual_norm)(Ctx&, double* d_out);
+};
+
+struct Ctx {
+  int nd, rs, precision, device;
+  int n_car, n_def, n_slot, n_car_con, n_def_con, n_bc_con, n_ref, n_bc_spec;
+  size_t nq, nfq, nv;
+  cudaStream_t stream;
+  HostTables tables;
+  const OpsTable* ops;
+  // device arena
+  double* elem; double* rcache; double* face;
+  double* nom_size; double* vert_tss; double* jac; double* face_nrml;
+  int* car_con; int* def_con; double* def_con_nrml;
+  int* bc_con; double* bc_nrml; double* bc_cache; int* ref_face; hexed_bc_spec* bc_spec;
+  // scratch
+  double* scalars;       // SC_* slots
+  double* partials;      // reduction partials, max_partials doubles
+  int max_partials;
+  int* status;
+  double* d_norm;        // residual norm output [3]
+  double* h_pinned;      // pinned host staging for scalars [8]
+  Profiler* prof;
+};
+
+// Bracket one launch with timing events when profiling is enabled.
+struct ProfScope {
+  Ctx& c; int pair;
+  ProfScope(Ctx& ctx, const char* name);
+  ~ProfScope();
+};
+
+const OpsTable* ops_2_2(int); const OpsTable* ops_2_3(int); const OpsTable* ops_2_4(int);
+const OpsTable* ops_2_5(int); const OpsTable* ops_2_6(int); const OpsTable* ops_2_7(int);
+const OpsTable* ops_2_8(int);
+const OpsTable* ops_3_2(int); const OpsTable* ops_3_3(int); const OpsTable* ops_3_4(int);
+const OpsTable* ops_3_5(int); const OpsTable* ops_3_6(int); const OpsTable* ops_3_7(int);
+const OpsTable* ops_3_8(int);
+
+} // namespace hx

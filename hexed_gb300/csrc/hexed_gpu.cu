@@ -1,0 +1,516 @@
+// hexed_gpu.cu -- C ABI (include/hexed_gpu.h): context, arena upload, entry points.
+//
+// Every entry point validates its arguments on the host before anything reaches the
+// device: all connection, boundary and refined-face indices of the arena are range
+// checked at creation, so no kernel can be handed an out-of-range slot.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <cstdarg>
+#include <string>
+#include <vector>
+#include "ctx.h"
+#include "kernels.cuh"
+#include "basis_tables.h"
+
+using hx::Ctx;
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int status, const char* fmt, ...)
+{
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_error = buf;
+  return status;
+}
+
+#define HX_CUDA(call) do { cudaError_t err_ = (call); if (err_ != cudaSuccess) \
+  return fail(err_ == cudaErrorMemoryAllocation ? HEXED_ERR_ALLOC : HEXED_ERR_CUDA, "%s: %s (%s:%d)", #call, \
+              cudaGetErrorString(err_), __FILE__, __LINE__); } while (0)
+
+#define HX_LAUNCHED() do { cudaError_t err_ = cudaGetLastError(); if (err_ != cudaSuccess) \
+  return fail(HEXED_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(err_)); } while (0)
+
+hx::HostTables host_tables(int rs)
+{
+  using namespace hexed_tables;
+  switch (rs) {
+#define HX_T(n) case n: return {node##n, weight##n, diff_mat##n, boundary##n, filter##n, prolong##n, restrict_##n, orthogonal##n, max_cfl##n, min_eig_diffusion##n, step_ratio};
+    HX_T(2) HX_T(3) HX_T(4) HX_T(5) HX_T(6) HX_T(7) HX_T(8)
+#undef HX_T
+  }
+  return {};
+}
+
+const hx::OpsTable* lookup_ops(int nd, int rs, int precision)
+{
+  switch (nd*16 + rs) {
+    case 2*16 + 2: return hx::ops_2_2(precision);
+    case 2*16 + 3: return hx::ops_2_3(precision);
+    case 2*16 + 4: return hx::ops_2_4(precision);
+    case 2*16 + 5: return hx::ops_2_5(precision);
+    case 2*16 + 6: return hx::ops_2_6(precision);
+    case 2*16 + 7: return hx::ops_2_7(precision);
+    case 2*16 + 8: return hx::ops_2_8(precision);
+    case 3*16 + 2: return hx::ops_3_2(precision);
+    case 3*16 + 3: return hx::ops_3_3(precision);
+    case 3*16 + 4: return hx::ops_3_4(precision);
+    case 3*16 + 5: return hx::ops_3_5(precision);
+    case 3*16 + 6: return hx::ops_3_6(precision);
+    case 3*16 + 7: return hx::ops_3_7(precision);
+    case 3*16 + 8: return hx::ops_3_8(precision);
+  }
+  return nullptr;
+}
+
+// chebyshev_step (src/math.cpp:104-107)
+double chebyshev_step(int n_steps, int i_step)
+{
+  return 1/(1 - std::cos((n_steps - i_step - 0.5)*M_PI/n_steps));
+}
+
+template <typename T>
+int upload_array(T** dst, const T* src, size_t count, const char* name)
+{
+  *dst = nullptr;
+  if (count == 0) return HEXED_OK;
+  if (!src) return fail(HEXED_ERR_INVALID, "arena array `%s` is null but %zu entries are required", name, count);
+  HX_CUDA(cudaMalloc((void**)dst, count*sizeof(T)));
+  HX_CUDA(cudaMemcpy(*dst, src, count*sizeof(T), cudaMemcpyHostToDevice));
+  return HEXED_OK;
+}
+
+int validate(const hexed_mesh_desc* d)
+{
+  if (!d) return fail(HEXED_ERR_INVALID, "null mesh descriptor");
+  if (d->n_dim < 2 || d->n_dim > 3 || d->row_size < HEXED_MIN_ROW_SIZE || d->row_size > HEXED_MAX_ROW_SIZE)
+    return fail(HEXED_ERR_INVALID, "demand for invalid kernel: n_dim %d row_size %d (supported: n_dim 2-3, row_size %d-%d)",
+                d->n_dim, d->row_size, HEXED_MIN_ROW_SIZE, HEXED_MAX_ROW_SIZE);
+  if (d->n_car_elem < 0 || d->n_def_elem < 0 || d->n_car_con < 0 || d->n_def_con < 0 || d->n_bc_con < 0 ||
+      d->n_ref_face < 0 || d->n_bc_spec < 0)
+    return fail(HEXED_ERR_INVALID, "negative count in mesh descriptor");
+  const long n_elem = (long)d->n_car_elem + d->n_def_elem;
+  if (n_elem == 0) return fail(HEXED_ERR_INVALID, "mesh has no elements");
+  if (d->n_slot < n_elem*2*d->n_dim) return fail(HEXED_ERR_INVALID, "n_slot %d < 2*n_dim*n_elem", d->n_slot);
+  auto slot_ok = [&](int s) { return s >= 0 && s < d->n_slot; };
+  for (int i = 0; i < d->n_car_con; ++i) {
+    const int* c = d->car_con + 3*i;
+    if (!slot_ok(c[0]) || !slot_ok(c[1]) || c[2] < 0 || c[2] >= d->n_dim)
+      return fail(HEXED_ERR_INVALID, "Cartesian connection %d out of range", i);
+  }
+  for (int i = 0; i < d->n_def_con; ++i) {
+    const int* c = d->def_con + 3*i;
+    if (!slot_ok(c[0]) || !slot_ok(c[1]) || (c[2] & 3) >= d->n_dim || ((c[2] >> 2) & 3) >= d->n_dim || (c[2] >> 6))
+      return fail(HEXED_ERR_INVALID, "deformed connection %d out of range", i);
+  }
+  for (int i = 0; i < d->n_bc_con; ++i) {
+    const int* c = d->bc_con + 4*i;
+    if (!slot_ok(c[0]) || !slot_ok(c[1]) || (c[2] & 3) >= d->n_dim || (c[2] >> 3) || c[3] < 0 || c[3] >= d->n_bc_spec)
+      return fail(HEXED_ERR_INVALID, "boundary connection %d out of range", i);
+  }
+  for (int i = 0; i < d->n_bc_spec; ++i)
+    if (d->bc_spec[i].kind < 0 || d->bc_spec[i].kind > HEXED_BC_NO_SLIP)
+      return fail(HEXED_ERR_INVALID, "boundary condition %d has unknown kind %d", i, d->bc_spec[i].kind);
+  for (int i = 0; i < d->n_ref_face; ++i) {
+    const int* r = d->ref_face + 7*i;
+    int nf = 1 << (d->n_dim - 1);
+    for (int k = 0; k < d->n_dim - 1; ++k) nf /= 1 + (r[5 + k] != 0);
+    if (!slot_ok(r[0])) return fail(HEXED_ERR_INVALID, "refined face %d: coarse slot out of range", i);
+    for (int k = 0; k < nf; ++k)
+      if (!slot_ok(r[1 + k])) return fail(HEXED_ERR_INVALID, "refined face %d: fine slot %d out of range", i, k);
+  }
+  return HEXED_OK;
+}
+
+size_t array_count(const Ctx* c, int which)
+{
+  const size_t n_elem = c->n_car + c->n_def;
+  switch (which) {
+    case HEXED_ARRAY_ELEM: return n_elem*(c->nv + 3)*c->nq;
+    case HEXED_ARRAY_RCACHE: return n_elem*c->nv*c->nq;
+    case HEXED_ARRAY_FACE: return (size_t)c->n_slot*2*c->nv*c->nfq;
+    case HEXED_ARRAY_BC_CACHE: return (size_t)c->n_bc_con*2*c->nv*c->nfq;
+  }
+  return 0;
+}
+
+double* array_ptr(Ctx* c, int which)
+{
+  switch (which) {
+    case HEXED_ARRAY_ELEM: return c->elem;
+    case HEXED_ARRAY_RCACHE: return c->rcache;
+    case HEXED_ARRAY_FACE: return c->face;
+    case HEXED_ARRAY_BC_CACHE: return c->bc_cache;
+  }
+  return nullptr;
+}
+
+int check_ctx(hexed_gpu_ctx* ctx) { return ctx ? HEXED_OK : fail(HEXED_ERR_INVALID, "null context"); }
+
+int set_dt(Ctx* c, double dt)
+{
+  hx::k_set_scalar<<<1, 1, 0, c->stream>>>(c->scalars, hx::SC_DT, dt);
+  HX_LAUNCHED();
+  return HEXED_OK;
+}
+
+hexed_transport inviscid() { return {0., 0., 1., 1., 0}; }
+
+} // namespace
+
+struct hexed_gpu_ctx : Ctx {};
+
+namespace hx {
+
+ProfScope::ProfScope(Ctx& ctx, const char* name) : c{ctx}, pair{-1}
+{
+  Profiler* p = c.prof;
+  if (!p || !p->enabled || p->n_pairs >= Profiler::max_events/2) return;
+  int idx = -1;
+  for (int i = 0; i < p->n_names; ++i) if (std::strcmp(p->names[i], name) == 0) { idx = i; break; }
+  if (idx < 0) {
+    if (p->n_names >= Profiler::max_names) return;
+    idx = p->n_names++;
+    p->names[idx] = name;
+    p->launches[idx] = 0;
+    p->total_ms[idx] = 0.;
+  }
+  pair = p->n_pairs++;
+  p->event_name[pair] = idx;
+  cudaEventRecord(p->events[2*pair], c.stream);
+}
+
+ProfScope::~ProfScope()
+{
+  if (pair >= 0) cudaEventRecord(c.prof->events[2*pair + 1], c.stream);
+}
+
+} // namespace hx
+
+extern "C" {
+
+const char* hexed_gpu_last_error(void) { return g_error.c_str(); }
+
+const char* hexed_gpu_version(void)
+{
+  static char v[64];
+  snprintf(v, sizeof(v), "hexed_gb300 sm_103a n_dim 2-3 row_size %d-%d", HEXED_MIN_ROW_SIZE, HEXED_MAX_ROW_SIZE);
+  return v;
+}
+
+int hexed_gpu_create(const hexed_mesh_desc* d, int precision, hexed_gpu_ctx** out)
+{
+  if (!out) return fail(HEXED_ERR_INVALID, "null output handle");
+  *out = nullptr;
+  if (int st = validate(d)) return st;
+  if (precision != HEXED_FP64 && precision != HEXED_MIXED) return fail(HEXED_ERR_INVALID, "unknown precision %d", precision);
+  int n_dev = 0;
+  if (cudaGetDeviceCount(&n_dev) != cudaSuccess || n_dev == 0) {
+    cudaGetLastError();
+    return fail(HEXED_ERR_NO_DEVICE, "no CUDA device visible");
+  }
+  hexed_gpu_ctx* c = new hexed_gpu_ctx();
+  std::memset(static_cast<Ctx*>(c), 0, sizeof(Ctx));
+  c->nd = d->n_dim; c->rs = d->row_size; c->precision = precision;
+  HX_CUDA(cudaGetDevice(&c->device));
+  c->n_car = d->n_car_elem; c->n_def = d->n_def_elem; c->n_slot = d->n_slot;
+  c->n_car_con = d->n_car_con; c->n_def_con = d->n_def_con; c->n_bc_con = d->n_bc_con;
+  c->n_ref = d->n_ref_face; c->n_bc_spec = d->n_bc_spec;
+  int nq = 1; for (int i = 0; i < c->nd; ++i) nq *= c->rs;
+  c->nq = nq; c->nfq = nq/c->rs; c->nv = c->nd + 2;
+  c->tables = host_tables(c->rs);
+  c->ops = lookup_ops(c->nd, c->rs, precision);
+  if (!c->ops) { delete c; return fail(HEXED_ERR_INVALID, "no kernels for n_dim %d row_size %d", d->n_dim, d->row_size); }
+  const size_t n_elem = c->n_car + c->n_def;
+  const size_t nd = c->nd, nvert = size_t(1) << nd;
+  int st = HEXED_OK;
+  auto up = [&](auto** dst, const auto* src, size_t n, const char* name) {
+    if (st == HEXED_OK) st = upload_array(dst, src, n, name);
+  };
+  HX_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  up(&c->elem, d->elem, n_elem*(c->nv + 3)*c->nq, "elem");
+  up(&c->rcache, d->rcache, n_elem*c->nv*c->nq, "rcache");
+  up(&c->face, d->face, (size_t)c->n_slot*2*c->nv*c->nfq, "face");
+  up(&c->nom_size, d->nom_size, n_elem, "nom_size");
+  up(&c->vert_tss, d->vert_tss, n_elem*nvert, "vert_tss");
+  up(&c->jac, d->jac, (size_t)c->n_def*(nd*nd + 1)*c->nq, "jac");
+  up(&c->face_nrml, d->face_nrml, (size_t)c->n_def*2*nd*nd*c->nfq, "face_nrml");
+  up(&c->car_con, d->car_con, (size_t)c->n_car_con*3, "car_con");
+  up(&c->def_con, d->def_con, (size_t)c->n_def_con*3, "def_con");
+  up(&c->def_con_nrml, d->def_con_nrml, (size_t)c->n_def_con*nd*c->nfq, "def_con_nrml");
+  up(&c->bc_con, d->bc_con, (size_t)c->n_bc_con*4, "bc_con");
+  up(&c->bc_nrml, d->bc_nrml, (size_t)c->n_bc_con*nd*c->nfq, "bc_nrml");
+  up(&c->bc_cache, d->bc_cache, (size_t)c->n_bc_con*2*c->nv*c->nfq, "bc_cache");
+  up(&c->ref_face, d->ref_face, (size_t)c->n_ref*7, "ref_face");
+  up(&c->bc_spec, d->bc_spec, (size_t)c->n_bc_spec, "bc_spec");
+  if (st != HEXED_OK) { hexed_gpu_destroy(c); return st; }
+  c->max_partials = 152*16*8;
+  if (cudaMalloc((void**)&c->partials, c->max_partials*sizeof(double)) != cudaSuccess ||
+      cudaMalloc((void**)&c->scalars, hx::SC_N*sizeof(double)) != cudaSuccess ||
+      cudaMalloc((void**)&c->status, 4*sizeof(int)) != cudaSuccess ||
+      cudaMalloc((void**)&c->d_norm, 4*sizeof(double)) != cudaSuccess ||
+      cudaMallocHost((void**)&c->h_pinned, 8*sizeof(double)) != cudaSuccess) {
+    hexed_gpu_destroy(c);
+    return fail(HEXED_ERR_ALLOC, "scratch allocation failed");
+  }
+  cudaMemset(c->scalars, 0, hx::SC_N*sizeof(double));
+  cudaMemset(c->status, 0, 4*sizeof(int));
+  HX_CUDA(cudaDeviceSynchronize());
+  *out = c;
+  return HEXED_OK;
+}
+
+int hexed_gpu_destroy(hexed_gpu_ctx* c)
+{
+  if (!c) return HEXED_OK;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  void* ptrs[] = {c->elem, c->rcache, c->face, c->nom_size, c->vert_tss, c->jac, c->face_nrml, c->car_con,
+                  c->def_con, c->def_con_nrml, c->bc_con, c->bc_nrml, c->bc_cache, c->ref_face, c->bc_spec,
+                  c->scalars, c->partials, c->status, c->d_norm};
+  for (void* p : ptrs) if (p) cudaFree(p);
+  if (c->h_pinned) cudaFreeHost(c->h_pinned);
+  if (c->prof) {
+    if (c->prof->created) for (auto& e : c->prof->events) cudaEventDestroy(e);
+    delete c->prof;
+  }
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return HEXED_OK;
+}
+
+int hexed_gpu_upload(hexed_gpu_ctx* c, int which, const double* host)
+{
+  if (int st = check_ctx(c)) return st;
+  double* dst = array_ptr(c, which);
+  size_t n = array_count(c, which);
+  if (n == 0) return HEXED_OK;
+  if (!dst || !host) return fail(HEXED_ERR_INVALID, "bad array %d or null host pointer", which);
+  HX_CUDA(cudaMemcpyAsync(dst, host, n*sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  HX_CUDA(cudaStreamSynchronize(c->stream));
+  return HEXED_OK;
+}
+
+int hexed_gpu_download(hexed_gpu_ctx* c, int which, double* host)
+{
+  if (int st = check_ctx(c)) return st;
+  double* src = array_ptr(c, which);
+  size_t n = array_count(c, which);
+  if (n == 0) return HEXED_OK;
+  if (!src || !host) return fail(HEXED_ERR_INVALID, "bad array %d or null host pointer", which);
+  HX_CUDA(cudaMemcpyAsync(host, src, n*sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  HX_CUDA(cudaStreamSynchronize(c->stream));
+  return HEXED_OK;
+}
+
+int hexed_gpu_synchronize(hexed_gpu_ctx* c)
+{
+  if (int st = check_ctx(c)) return st;
+  HX_CUDA(cudaStreamSynchronize(c->stream));
+  return HEXED_OK;
+}
+
+int hexed_gpu_compute_euler(hexed_gpu_ctx* c, double dt, int i_stage, int compute_residual, int use_filter)
+{
+  if (int st = check_ctx(c)) return st;
+  if (i_stage && compute_residual)
+    return fail(HEXED_ERR_PRECONDITION, "residual calculation is a single-stage operation");
+  if (int st = set_dt(c, dt)) return st;
+  c->ops->compute_euler(*c, i_stage ? 1 : 0, compute_residual, use_filter, false);
+  HX_LAUNCHED();
+  return HEXED_OK;
+}
+
+int hexed_gpu_compute_navier_stokes(hexed_gpu_ctx* c, double dt, int i_stage, int compute_residual, int use_filter,
+                                    const hexed_transport* visc, const hexed_transport* cond)
+{
+  if (int st = check_ctx(c)) return st;
+  if (!visc || !cond) return fail(HEXED_ERR_INVALID, "null transport model");
+  if (i_stage) return fail(HEXED_ERR_PRECONDITION, "two-stage stabilization is not applicable to diffusion equations");
+  if (int st = set_dt(c, dt)) return st;
+  c->ops->compute_navier_stokes(*c, 0, compute_residual, use_filter, *visc, *cond, false);
+  HX_LAUNCHED();
+  return HEXED_OK;
+}
+
+int hexed_gpu_max_dt(hexed_gpu_ctx* c, double msc, double msd, int local_time, int use_filter, int viscous,
+                     const hexed_transport* visc, const hexed_transport* cond, double* out_dt)
+{
+  (void)use_filter;
+  if (int st = check_ctx(c)) return st;
+  hexed_transport inv = inviscid();
+  c->ops->max_dt(*c, msc, msd, local_time, viscous, visc ? *visc : inv, cond ? *cond : inv,
+                 1.7976931348623157e308, 1.);
+  HX_LAUNCHED();
+  if (out_dt) {
+    HX_CUDA(cudaMemcpyAsync(c->h_pinned, c->scalars + hx::SC_MAXDT, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    HX_CUDA(cudaStreamSynchronize(c->stream));
+    *out_dt = c->h_pinned[0];
+  }
+  return HEXED_OK;
+}
+
+int hexed_gpu_compute_prolong(hexed_gpu_ctx* c, int scale, int offset)
+{
+  if (int st = check_ctx(c)) return st;
+  c->ops->refine(*c, true, scale, offset);
+  HX_LAUNCHED();
+  return HEXED_OK;
+}
+
+int hexed_gpu_compute_restrict(hexed_gpu_ctx* c, int scale, int offset)
+{
+  if (int st = check_ctx(c)) return st;
+  c->ops->refine(*c, false, scale, offset);
+  HX_LAUNCHED();
+  return HEXED_OK;
+}
+
+int hexed_gpu_compute_write_face(hexed_gpu_ctx* c)
+{
+  if (int st = check_ctx(c)) return st;
+  c->ops->write_face(*c);
+  HX_LAUNCHED();
+  return HEXED_OK;
+}
+
+int hexed_gpu_apply_state_bcs(hexed_gpu_ctx* c)
+{
+  if (int st = check_ctx(c)) return st;
+  c->ops->bc_state(*c);
+  HX_LAUNCHED();
+  return HEXED_OK;
+}
+
+int hexed_gpu_apply_flux_bcs(hexed_gpu_ctx* c)
+{
+  if (int st = check_ctx(c)) return st;
+  c->ops->bc_flux(*c);
+  HX_LAUNCHED();
+  return HEXED_OK;
+}
+
+int hexed_gpu_update(hexed_gpu_ctx* c, const hexed_update_params* p, double* out_dt)
+{
+  if (int st = check_ctx(c)) return st;
+  if (!p || p->n_cheby_flow < 1 || p->flow_iters < 0) return fail(HEXED_ERR_INVALID, "bad update parameters");
+  const double max_cheby = chebyshev_step(p->n_cheby_flow, p->n_cheby_flow - 1);
+  for (int i_flow = 0; i_flow < p->flow_iters; ++i_flow) {
+    for (int i_cheby = 0; i_cheby < p->n_cheby_flow; ++i_cheby) {
+      c->ops->max_dt(*c, p->max_safety/max_cheby, p->max_safety, p->local_time, p->use_ldg, p->visc, p->cond,
+                     p->max_time_step, chebyshev_step(p->n_cheby_flow, i_cheby));
+      for (int i = 0; i < 2; ++i) {
+        if (p->use_ldg && !i) c->ops->compute_navier_stokes(*c, 0, 0, p->use_filter, p->visc, p->cond, true);
+        else c->ops->compute_euler(*c, i, 0, p->use_filter, true);
+      }
+    }
+  }
+  HX_LAUNCHED();
+  if (out_dt) {
+    HX_CUDA(cudaMemcpyAsync(c->h_pinned, c->scalars + hx::SC_DT, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    HX_CUDA(cudaStreamSynchronize(c->stream));
+    *out_dt = c->h_pinned[0];
+  }
+  return HEXED_OK;
+}
+
+int hexed_gpu_compute_residual(hexed_gpu_ctx* c, const hexed_update_params* p)
+{
+  if (int st = check_ctx(c)) return st;
+  if (!p) return fail(HEXED_ERR_INVALID, "null parameters");
+  if (int st = set_dt(c, 1.)) return st;
+  if (p->use_ldg) c->ops->compute_navier_stokes(*c, 0, 1, p->use_filter, p->visc, p->cond, true);
+  else c->ops->compute_euler(*c, 0, 1, p->use_filter, true);
+  HX_LAUNCHED();
+  return HEXED_OK;
+}
+
+int hexed_gpu_residual_norm(hexed_gpu_ctx* c, double out[3])
+{
+  if (int st = check_ctx(c)) return st;
+  if (!out) return fail(HEXED_ERR_INVALID, "null output");
+  c->ops->residual_norm(*c, c->d_norm);
+  HX_LAUNCHED();
+  HX_CUDA(cudaMemcpyAsync(c->h_pinned, c->d_norm, 3*sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  HX_CUDA(cudaStreamSynchronize(c->stream));
+  for (int i = 0; i < 3; ++i) out[i] = c->h_pinned[i];
+  return HEXED_OK;
+}
+
+void* hexed_gpu_stream(hexed_gpu_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int hexed_gpu_fp64_peak(double* tflops)
+{
+  if (!tflops) return fail(HEXED_ERR_INVALID, "null output");
+  int dev = 0, n_sm = 0;
+  HX_CUDA(cudaGetDevice(&dev));
+  HX_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+  double* out = nullptr;
+  const int block = 256, blocks = n_sm*8, iters = 4096;
+  HX_CUDA(cudaMalloc((void**)&out, (size_t)blocks*block*sizeof(double)));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  hx::k_fp64_fma<<<blocks, block>>>(out, iters, 1.0000001);   // warm-up
+  cudaEventRecord(e0);
+  hx::k_fp64_fma<<<blocks, block>>>(out, iters, 1.0000001);
+  cudaEventRecord(e1);
+  cudaError_t err = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (err != cudaSuccess) return fail(HEXED_ERR_CUDA, "fp64 probe: %s", cudaGetErrorString(err));
+  *tflops = 2.*hx::fp64_fma_chains*double(iters)*blocks*block/(ms*1e-3)/1e12;
+  return HEXED_OK;
+}
+
+int hexed_gpu_profile_enable(hexed_gpu_ctx* c, int enable)
+{
+  if (int st = check_ctx(c)) return st;
+  if (!c->prof) c->prof = new hx::Profiler();
+  hx::Profiler* p = c->prof;
+  if (!p->created) {
+    for (auto& e : p->events) HX_CUDA(cudaEventCreate(&e));
+    p->created = true;
+  }
+  HX_CUDA(cudaStreamSynchronize(c->stream));
+  p->enabled = enable != 0;
+  p->n_pairs = 0;
+  p->n_names = 0;
+  return HEXED_OK;
+}
+
+int hexed_gpu_profile_read(hexed_gpu_ctx* c, hexed_kernel_time* out, int capacity, int* n_out)
+{
+  if (int st = check_ctx(c)) return st;
+  if (n_out) *n_out = 0;
+  hx::Profiler* p = c->prof;
+  if (!p) return HEXED_OK;
+  HX_CUDA(cudaStreamSynchronize(c->stream));
+  for (int i = 0; i < p->n_names; ++i) { p->launches[i] = 0; p->total_ms[i] = 0.; }
+  for (int k = 0; k < p->n_pairs; ++k) {
+    float ms = 0.f;
+    HX_CUDA(cudaEventElapsedTime(&ms, p->events[2*k], p->events[2*k + 1]));
+    p->launches[p->event_name[k]] += 1;
+    p->total_ms[p->event_name[k]] += ms;
+  }
+  int n = 0;
+  for (int i = 0; i < p->n_names && n < capacity; ++i, ++n) {
+    std::snprintf(out[n].name, sizeof(out[n].name), "%s", p->names[i]);
+    out[n].launches = p->launches[i];
+    out[n].total_ms = p->total_ms[i];
+  }
+  if (n_out) *n_out = n;
+  p->n_pairs = 0;
+  p->n_names = 0;
+  return HEXED_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,1361 @@
+// kernels.cuh -- sm_103a device code of the DG spatial operator and stage update.
+//
+// One CUDA thread per quadrature point (volume kernels) or per face quadrature point
+// (face kernels). A CTA holds EPB whole elements; their state, fluxes and per-row
+// boundary corrections are staged in shared memory so that the tensor-product line
+// contractions of Derivative (include/Derivative.hpp:50-60) read each row from shared
+// memory. The contractions are rs x rs with rs <= 8, far too thin for tcgen05 tensor
+// cores, so they run on the FP64 (plain form) or FP32 (mixed form) pipes.
+//
+// Arithmetic follows the reference operation by operation (sums in ascending index
+// order, same association) so that the FP64 form agrees with the CPU oracle to
+// roundoff; nvcc contracts a*b + c into FMAs, which is the only systematic difference.
+//
+// Template parameters: ND (2, 3), RS (row size), R (compute type: double, or float in
+// the mixed form), DEF (deformed elements / connections), VISC (LDG viscous path).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "../../include/hexed_gpu.h"
+
+namespace hx {
+
+constexpr int ipow(int b, int e) { int r = 1; for (int i = 0; i < e; ++i) r *= b; return r; }
+constexpr double heat_rat = 1.4;                 // include/pde.hpp:51
+constexpr double specific_gas_air = 287.05287;   // include/constants.hpp:44
+
+// Basis tables of one row size (generated by hexed_gb300/basis.py), passed by value as a
+// kernel parameter and copied to shared memory by each CTA.
+template <int RS>
+struct Tab {
+  double diff[RS*RS];      // diff[i*RS + j] = L_j'(x_i)
+  double bound[2*RS];      // bound[s*RS + j] = L_j(s)
+  double lift[RS*2];       // lift[i*2 + s] (include/Derivative.hpp:22-28)
+  double filter[RS*RS];
+  double node[RS];
+  double weight[RS];
+  double prolong[2*RS*RS];
+  double restrict_[2*RS*RS];
+  double max_cfl, min_eig_diffusion, step_ratio;
+};
+
+// Device view of the arena (include/hexed_gpu.h). `face` is stored as FaceT.
+template <typename FaceT>
+struct Dev {
+  int n_car, n_def, n_elem, n_slot, n_car_con, n_def_con, n_bc_con, n_ref;
+  double* elem;
+  double* rcache;
+  FaceT* face;
+  const double* nom_size;
+  const double* vert_tss;
+  const double* jac;
+  const double* face_nrml;
+  const int* car_con;
+  const int* def_con;
+  const double* def_con_nrml;
+  const int* bc_con;
+  const double* bc_nrml;
+  double* bc_cache;
+  const int* ref_face;
+  const hexed_bc_spec* bc_spec;
+  double* scalars;       // [0] dt of the current stage, [1] raw max_dt, ...
+  double* partials;      // per-block reduction scratch
+  int* status;           // device-side error flags
+};
+
+enum { SC_DT = 0, SC_MAXDT = 1, SC_FLOWTIME = 2, SC_N = 8 };
+
+template <int ND, int RS>
+struct Shape {
+  static constexpr int nq = ipow(RS, ND);
+  static constexpr int nfq = nq/RS;
+  static constexpr int nv = ND + 2;
+  static constexpr int nvert = 1 << ND;
+  static constexpr int epb = nq >= 256 ? 1 : 256/nq;     // elements per CTA
+  static constexpr int threads_raw = epb*nq;
+  static constexpr int threads = (threads_raw + 31)/32*32;
+  static constexpr int slot_dof = 2*nv*nfq;
+  static __host__ __device__ constexpr int stride(int d) { return ipow(RS, ND - 1 - d); }
+};
+
+template <typename T> __device__ __forceinline__ T load(const T* p) { return __ldg(p); }
+
+// ------------------------------------------------------------------- PDE pieces
+// Navier_stokes<visc>::Pde::Computation (include/pde.hpp:72-175), one qpoint.
+template <int ND, typename R>
+struct Conv {
+  R mass, kin_ener, pressure;
+  __device__ __forceinline__ explicit Conv(const R* s)
+  {
+    mass = s[ND];
+    kin_ener = 0;
+    #pragma unroll
+    for (int d = 0; d < ND; ++d) kin_ener += s[d]*s[d];
+    kin_ener *= R(.5)/mass;
+    pressure = R(heat_rat - 1.)*(s[ND + 1] - kin_ener);
+  }
+  // compute_flux_conv for one flux direction n (pde.hpp:108-122)
+  __device__ __forceinline__ void flux(const R* s, const R* n, R* f) const
+  {
+    R fm = 0;
+    #pragma unroll
+    for (int j = 0; j < ND; ++j) fm += s[j]*n[j];
+    f[ND] = fm;
+    R vol_flux = fm/mass;
+    f[ND + 1] = (s[ND + 1] + pressure)*vol_flux;
+    #pragma unroll
+    for (int j = 0; j < ND; ++j) f[j] = s[j]*vol_flux + pressure*n[j];
+  }
+};
+
+template <int ND, typename R>
+__device__ __forceinline__ R char_speed(const R* s) // pde.hpp:161-166
+{
+  R sound_speed = sqrt(R(heat_rat*(heat_rat - 1))*s[ND + 1]/s[ND]);
+  R sq = 0;
+  #pragma unroll
+  for (int d = 0; d < ND; ++d) sq += s[d]*s[d];
+  return sound_speed + sqrt(sq)/s[ND];
+}
+
+template <typename R>
+__device__ __forceinline__ R transport_coef(const hexed_transport& t, R sqrt_temp) // Transport_model.hpp:35-38
+{
+  R r = sqrt_temp/R(sqrt(t.ref_temp));
+  R p3 = r*r*r;
+  return R(t.const_val) + R(t.ref_val)*p3*R(t.ref_temp + t.temp_offset)/(sqrt_temp*sqrt_temp + R(t.temp_offset));
+}
+
+template <int ND, typename R>
+struct DiffScalars { // compute_scalars_diff (pde.hpp:130-138)
+  R bulk_av, laplacian_av, mu, energy_cond;
+  __device__ __forceinline__ DiffScalars(const R* s, const Conv<ND, R>& c, R bulk, R lap,
+                                         const hexed_transport& visc, const hexed_transport& cond)
+  {
+    bulk_av = fabs(bulk);
+    laplacian_av = fabs(lap);
+    R sqrt_temp = sqrt(fmax((s[ND + 1] - c.kin_ener)/c.mass, R(0))*R(heat_rat - 1)/R(specific_gas_air));
+    mu = transport_coef(visc, sqrt_temp);
+    R k = transport_coef(cond, sqrt_temp);
+    energy_cond = k*R(heat_rat - 1)/R(specific_gas_air);
+  }
+};
+
+// compute_flux_diff (pde.hpp:142-158): g[v][j] gradient, nrm[j][i] (physical j, reference i)
+template <int ND, typename R, bool IDENT>
+__device__ __forceinline__ void flux_diff(const R* s, const Conv<ND, R>& c, const DiffScalars<ND, R>& df,
+                                          const R (&g)[ND + 2][ND], const R (&nrm)[ND][ND], R (&out)[ND + 2][ND])
+{
+  const R mass = c.mass;
+  R veloc[ND];
+  #pragma unroll
+  for (int i = 0; i < ND; ++i) veloc[i] = s[i]/mass;
+  R vg[ND][ND];
+  #pragma unroll
+  for (int i = 0; i < ND; ++i)
+    #pragma unroll
+    for (int j = 0; j < ND; ++j) vg[i][j] = (g[i][j] - veloc[i]*g[ND][j])/mass;
+  R trace = 0;
+  #pragma unroll
+  for (int i = 0; i < ND; ++i) trace += vg[i][i];
+  const R bulk_term = (df.bulk_av*mass - R(2./3.)*df.mu)*trace;
+  R stress[ND][ND];
+  #pragma unroll
+  for (int i = 0; i < ND; ++i)
+    #pragma unroll
+    for (int j = 0; j < ND; ++j) stress[i][j] = df.mu*(vg[i][j] + vg[j][i]) + (i == j ? bulk_term : R(0));
+  R fd[ND + 2][ND];
+  #pragma unroll
+  for (int v = 0; v < ND + 2; ++v)
+    #pragma unroll
+    for (int j = 0; j < ND; ++j) fd[v][j] = -df.laplacian_av*g[v][j];
+  #pragma unroll
+  for (int i = 0; i < ND; ++i)
+    #pragma unroll
+    for (int j = 0; j < ND; ++j) fd[i][j] -= stress[i][j];
+  const R coef = -s[ND + 1]/mass/mass;
+  #pragma unroll
+  for (int j = 0; j < ND; ++j) {
+    R vvg = 0;
+    #pragma unroll
+    for (int i = 0; i < ND; ++i) vvg += veloc[i]*vg[i][j];
+    R ieg = coef*g[ND][j] + g[ND + 1][j]/mass - vvg;
+    R vs = 0;
+    #pragma unroll
+    for (int i = 0; i < ND; ++i) vs += veloc[i]*stress[i][j];
+    fd[ND + 1][j] -= vs + df.energy_cond*ieg;
+  }
+  #pragma unroll
+  for (int v = 0; v < ND + 2; ++v) {
+    #pragma unroll
+    for (int i = 0; i < ND; ++i) {
+      if (IDENT) { out[v][i] = fd[v][i]; continue; }
+      R acc = 0;
+      #pragma unroll
+      for (int j = 0; j < ND; ++j) acc += fd[v][j]*nrm[j][i];
+      out[v][i] = acc;
+    }
+  }
+}
+
+// Face-1 index that lands at face-0 qpoint q after Face_permutation::match_faces
+// (transpose then flip; include/Spatial.hpp:85-129, include/Kernel_connection.hpp:55-85).
+template <int ND, int RS>
+__device__ __forceinline__ int perm_index(int dir, int q)
+{
+  const int i_dim0 = dir & 3, i_dim1 = (dir >> 2) & 3;
+  const bool s0 = (dir >> 4) & 1, s1 = (dir >> 5) & 1;
+  const bool flip_n0 = !s0, flip_n1 = s1;
+  const bool flip_tan = (i_dim0 != i_dim1) && (flip_n0 == flip_n1);
+  const bool transpose = ((i_dim0 == 0) && (i_dim1 == 2)) || ((i_dim0 == 2) && (i_dim1 == 0));
+  if constexpr (ND == 3) {
+    int r = q%RS, c = q/RS;
+    if (flip_tan) {
+      const bool colwise = (i_dim0 > 3 - i_dim0 - i_dim1) != transpose;
+      if (colwise) r = RS - 1 - r; else c = RS - 1 - c;
+    }
+    int idx = r + c*RS;
+    if (transpose) idx = (idx%RS)*RS + idx/RS;
+    return idx;
+  } else {
+    return flip_tan ? RS - 1 - q : q;
+  }
+}
+
+__device__ __forceinline__ int bc_dir(int packed) // {{d,d},{ifs,!ifs}} (include/connection.hpp:378)
+{
+  int d = packed & 3, ifs = (packed >> 2) & 1;
+  return d | (d << 2) | (ifs << 4) | ((!ifs) << 5);
+}
+
+// Per-CTA shared copy of the 1-D operators in the compute type.
+template <int RS, typename R>
+struct STab {
+  R diff[RS*RS];
+  R bound[2*RS];
+  R lift[2*RS];
+  R filter[RS*RS];
+  __device__ __forceinline__ void load(const Tab<RS>& t)
+  {
+    for (int i = threadIdx.x; i < RS*RS; i += blockDim.x) { diff[i] = R(t.diff[i]); filter[i] = R(t.filter[i]); }
+    for (int i = threadIdx.x; i < 2*RS; i += blockDim.x) { bound[i] = R(t.bound[i]); lift[i] = R(t.lift[i]); }
+  }
+};
+
+// ------------------------------------------------------------------- Write_face helper
+// Extrapolate an element's state (shared memory, [nv][nq]) to its 2nd face slots
+// (Spatial::Write_face, include/Spatial.hpp:41-57). Called by all threads of the CTA.
+template <int ND, int RS, typename R, typename FaceT>
+__device__ __forceinline__ void write_faces_from_smem(const Dev<FaceT>& m, const STab<RS, R>& st,
+                                                      const R* s_u, int e0, int e_end)
+{
+  using S = Shape<ND, RS>;
+  constexpr int nq = S::nq, nfq = S::nfq, nv = S::nv;
+  constexpr int n_task = S::epb*ND*nv*nfq;
+  for (int task = threadIdx.x; task < n_task; task += blockDim.x) {
+    int r = task%nfq;
+    int rest = task/nfq;
+    int v = rest%nv; rest /= nv;
+    int d = rest%ND;
+    int le = rest/ND;
+    int e = e0 + le;
+    if (e >= e_end) continue;
+    const int stride = S::stride(d);
+    const int base = (r/stride)*stride*RS + r%stride;
+    const R* row = s_u + (le*nv + v)*nq + base;
+    R a0 = 0, a1 = 0;
+    #pragma unroll
+    for (int i = 0; i < RS; ++i) {
+      R x = row[i*stride];
+      a0 += st.bound[i]*x;
+      a1 += st.bound[RS + i]*x;
+    }
+    FaceT* f0 = m.face + (size_t)(e*2*ND + 2*d)*S::slot_dof + v*nfq + r;
+    f0[0] = FaceT(a0);
+    f0[S::slot_dof] = FaceT(a1);   // slot of face 2d + 1
+  }
+}
+
+// ------------------------------------------------------------------- Local
+// Spatial::Local (include/Spatial.hpp:326-509) fused with the stage update and Write_face.
+template <int ND, int RS, typename R, bool DEF, bool VISC>
+struct LocalSmem {
+  using S = Shape<ND, RS>;
+  static constexpr int per_elem = S::nv*S::nq            // s_u
+                                + ND*S::nv*S::nq         // s_f
+                                + (VISC ? ND*S::nv*S::nq : 0)   // s_g
+                                + ND*2*S::nv*S::nfq;     // s_bf
+  static constexpr size_t bytes = sizeof(STab<RS, R>) + sizeof(R)*(size_t)per_elem*S::epb + 16;
+};
+
+template <int ND, int RS, typename R, bool DEF, bool VISC, typename FaceT>
+__global__ void __launch_bounds__(Shape<ND, RS>::threads)
+k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int compute_residual, int use_filter,
+        hexed_transport visc, hexed_transport cond)
+{
+  using S = Shape<ND, RS>;
+  constexpr int nq = S::nq, nfq = S::nfq, nv = S::nv, EPB = S::epb;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  STab<RS, R>& st = *reinterpret_cast<STab<RS, R>*>(smem_raw);
+  R* s_u = reinterpret_cast<R*>(smem_raw + (sizeof(STab<RS, R>) + 15)/16*16);
+  R* s_f = s_u + EPB*nv*nq;
+  R* s_g = s_f + EPB*ND*nv*nq;
+  R* s_bf = s_g + (VISC ? EPB*ND*nv*nq : 0);
+  st.load(tab);
+
+  const int le = threadIdx.x/nq;
+  const int q = threadIdx.x%nq;
+  const int e0 = e_begin + blockIdx.x*EPB;
+  const int e = e0 + le;
+  const bool active = threadIdx.x < EPB*nq && e < e_end;
+  const int ed = e - m.n_car;
+  const double d_pos = active ? m.nom_size[e] : 1.;
+  const double* state_g = m.elem + (size_t)e*(nv + 3)*nq;
+
+  R u[nv + 2];   // state + bulk AV + Laplacian AV (include/pde.hpp:79-84)
+  R nrm[ND][ND]; // nrm[j][i] = comp.normal(j, i)
+  #pragma unroll
+  for (int i = 0; i < ND; ++i)
+    #pragma unroll
+    for (int j = 0; j < ND; ++j) nrm[j][i] = (i == j) ? R(1) : R(0);
+  if (active) {
+    #pragma unroll
+    for (int v = 0; v < nv; ++v) u[v] = R(state_g[v*nq + q]);
+    u[nv] = R(state_g[(nv + 1)*nq + q]);
+    u[nv + 1] = R(state_g[(nv + 2)*nq + q]);
+    if constexpr (DEF) {
+      const double* nr = m.jac + (size_t)ed*(ND*ND + 1)*nq;
+      #pragma unroll
+      for (int i = 0; i < ND; ++i)
+        #pragma unroll
+        for (int j = 0; j < ND; ++j) nrm[j][i] = R(nr[(i*ND + j)*nq + q]);
+    }
+  } else {
+    #pragma unroll
+    for (int v = 0; v < nv + 2; ++v) u[v] = R(1);
+  }
+  R* my_u = s_u + le*nv*nq;
+  R* my_f = s_f + le*ND*nv*nq;
+  R* my_g = s_g + le*ND*nv*nq;
+  R* my_bf = s_bf + le*ND*2*nv*nfq;
+  // position of this qpoint in its row along each dimension
+  int node_of[ND], base_of[ND], row_of[ND];
+  #pragma unroll
+  for (int d = 0; d < ND; ++d) {
+    const int stride = S::stride(d);
+    node_of[d] = (q/stride)%RS;
+    base_of[d] = q - node_of[d]*stride;
+    row_of[d] = (q/(stride*RS))*stride + q%stride;
+  }
+
+  R grad[nv][ND];
+  if constexpr (VISC) {
+    // ---- gradient times Jacobian determinant (Spatial.hpp:371-402)
+    #pragma unroll
+    for (int v = 0; v < nv; ++v)
+      #pragma unroll
+      for (int j = 0; j < ND; ++j) grad[v][j] = 0;
+    if constexpr (!DEF) {
+      if (threadIdx.x < EPB*nq) {
+        #pragma unroll
+        for (int v = 0; v < nv; ++v) my_u[v*nq + q] = u[v];
+      }
+      __syncthreads();
+      // per-row boundary corrections: bf_s = face_state_s - B_s . row
+      constexpr int n_task = EPB*ND*nv*nfq;
+      for (int task = threadIdx.x; task < n_task; task += blockDim.x) {
+        int r = task%nfq, rest = task/nfq;
+        int v = rest%nv; rest /= nv;
+        int d = rest%ND; int l = rest/ND;
+        int ee = e0 + l;
+        if (ee >= e_end) continue;
+        const int stride = S::stride(d);
+        const R* row = s_u + (l*nv + v)*nq + (r/stride)*stride*RS + r%stride;
+        R a0 = 0, a1 = 0;
+        #pragma unroll
+        for (int i = 0; i < RS; ++i) { R x = row[i*stride]; a0 += st.bound[i]*x; a1 += st.bound[RS + i]*x; }
+        const FaceT* fl = m.face + (size_t)(ee*2*ND + 2*d)*S::slot_dof + nv*nfq + v*nfq + r;
+        R* bf = s_bf + ((l*ND + d)*2*nv)*nfq;
+        bf[v*nfq + r] = R(fl[0]) - a0;
+        bf[(nv + v)*nfq + r] = R(fl[S::slot_dof]) - a1;
+      }
+      __syncthreads();
+      if (active) {
+        #pragma unroll
+        for (int d = 0; d < ND; ++d) {
+          const int stride = S::stride(d);
+          const int i = node_of[d];
+          const R* bf = my_bf + d*2*nv*nfq;
+          #pragma unroll
+          for (int v = 0; v < nv; ++v) {
+            const R* row = my_u + v*nq + base_of[d];
+            R acc = 0;
+            #pragma unroll
+            for (int j = 0; j < RS; ++j) acc += st.diff[i*RS + j]*row[j*stride];
+            R l = 0;
+            l += st.lift[i*2]*bf[v*nfq + row_of[d]];
+            l += st.lift[i*2 + 1]*bf[(nv + v)*nfq + row_of[d]];
+            grad[v][d] = (acc + l)/R(d_pos);
+          }
+        }
+      }
+    } else {
+      const double* nr = m.jac + (size_t)ed*(ND*ND + 1)*nq;
+      const double* fn = m.face_nrml + (size_t)ed*2*ND*ND*nfq;
+      #pragma unroll 1
+      for (int d = 0; d < ND; ++d) {
+        __syncthreads(); // previous use of s_f / s_bf finished
+        if (active) {
+          #pragma unroll
+          for (int j = 0; j < ND; ++j) {
+            R nd_ = R(nr[(d*ND + j)*nq + q]);
+            #pragma unroll
+            for (int v = 0; v < nv; ++v) my_f[(j*nv + v)*nq + q] = nd_*u[v];
+          }
+        }
+        __syncthreads();
+        constexpr int n_task = EPB*ND*nv*nfq;
+        const int stride = S::stride(d);
+        for (int task = threadIdx.x; task < n_task; task += blockDim.x) {
+          int r = task%nfq, rest = task/nfq;
+          int v = rest%nv; rest /= nv;
+          int j = rest%ND; int l = rest/ND;
+          int ee = e0 + l;
+          if (ee >= e_end) continue;
+          const int eed = ee - m.n_car;
+          const R* row = s_f + ((l*ND + j)*nv + v)*nq + (r/stride)*stride*RS + r%stride;
+          R a0 = 0, a1 = 0;
+          #pragma unroll
+          for (int i = 0; i < RS; ++i) { R x = row[i*stride]; a0 += st.bound[i]*x; a1 += st.bound[RS + i]*x; }
+          const FaceT* fl = m.face + (size_t)(ee*2*ND + 2*d)*S::slot_dof + nv*nfq + v*nfq + r;
+          const double* fnr = m.face_nrml + ((size_t)eed*2*ND + 2*d)*ND*nfq + j*nfq + r;
+          R b0 = R(fnr[0])*R(fl[0]);
+          R b1 = R(fnr[ND*nfq])*R(fl[S::slot_dof]);
+          R* bf = s_bf + ((l*ND + j)*2*nv)*nfq;
+          bf[v*nfq + r] = b0 - a0;
+          bf[(nv + v)*nfq + r] = b1 - a1;
+        }
+        __syncthreads();
+        if (active) {
+          const int i = node_of[d];
+          #pragma unroll
+          for (int j = 0; j < ND; ++j) {
+            const R* bf = my_bf + j*2*nv*nfq;
+            #pragma unroll
+            for (int v = 0; v < nv; ++v) {
+              const R* row = my_f + (j*nv + v)*nq + base_of[d];
+              R acc = 0;
+              #pragma unroll
+              for (int jj = 0; jj < RS; ++jj) acc += st.diff[i*RS + jj]*row[jj*stride];
+              R l = 0;
+              l += st.lift[i*2]*bf[v*nfq + row_of[d]];
+              l += st.lift[i*2 + 1]*bf[(nv + v)*nfq + row_of[d]];
+              grad[v][j] = grad[v][j] + (acc + l)/R(d_pos);
+            }
+          }
+        }
+      }
+      (void)fn;
+    }
+    __syncthreads(); // s_f / s_bf are reused below
+  }
+
+  // ---- fluxes (Spatial.hpp:405-442)
+  if (active) {
+    Conv<ND, R> c(u);
+    #pragma unroll
+    for (int i = 0; i < ND; ++i) {
+      R col[ND], f[nv];
+      #pragma unroll
+      for (int j = 0; j < ND; ++j) col[j] = nrm[j][i];
+      c.flux(u, col, f);
+      #pragma unroll
+      for (int v = 0; v < nv; ++v) my_f[(i*nv + v)*nq + q] = f[v];
+    }
+    if constexpr (VISC) {
+      R g[nv][ND];
+      const R det = DEF ? R(m.jac[((size_t)ed*(ND*ND + 1) + ND*ND)*nq + q]) : R(1);
+      #pragma unroll
+      for (int v = 0; v < nv; ++v)
+        #pragma unroll
+        for (int j = 0; j < ND; ++j) g[v][j] = DEF ? grad[v][j]/det : grad[v][j];
+      DiffScalars<ND, R> df(u, c, u[nv], u[nv + 1], visc, cond);
+      R fd[nv][ND];
+      flux_diff<ND, R, !DEF>(u, c, df, g, nrm, fd);
+      #pragma unroll
+      for (int i = 0; i < ND; ++i)
+        #pragma unroll
+        for (int v = 0; v < nv; ++v) my_g[(i*nv + v)*nq + q] = fd[v][i];
+    }
+  }
+  __syncthreads();
+
+  // ---- per-row boundary corrections of the convective flux; viscous flux to LDG faces
+  {
+    constexpr int n_task = EPB*ND*nv*nfq;
+    for (int task = threadIdx.x; task < n_task; task += blockDim.x) {
+      int r = task%nfq, rest = task/nfq;
+      int v = rest%nv; rest /= nv;
+      int d = rest%ND; int l = rest/ND;
+      int ee = e0 + l;
+      if (ee >= e_end) continue;
+      const int stride = S::stride(d);
+      const int off = (r/stride)*stride*RS + r%stride;
+      const R* row = s_f + ((l*ND + d)*nv + v)*nq + off;
+      R a0 = 0, a1 = 0;
+      #pragma unroll
+      for (int i = 0; i < RS; ++i) { R x = row[i*stride]; a0 += st.bound[i]*x; a1 += st.bound[RS + i]*x; }
+      FaceT* fl = m.face + (size_t)(ee*2*ND + 2*d)*S::slot_dof + v*nfq + r;
+      R* bf = s_bf + ((l*ND + d)*2*nv)*nfq;
+      bf[v*nfq + r] = R(fl[0]) - a0;
+      bf[(nv + v)*nfq + r] = R(fl[S::slot_dof]) - a1;
+      if constexpr (VISC) {
+        const R* rg = s_g + ((l*ND + d)*nv + v)*nq + off;
+        R g0 = 0, g1 = 0;
+        #pragma unroll
+        for (int i = 0; i < RS; ++i) { R x = rg[i*stride]; g0 += st.bound[i]*x; g1 += st.bound[RS + i]*x; }
+        fl[nv*nfq] = FaceT(g0);
+        fl[S::slot_dof + nv*nfq] = FaceT(g1);
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- residual (Spatial.hpp:445-470)
+  R rate[nv], vrate[nv];
+  #pragma unroll
+  for (int v = 0; v < nv; ++v) { rate[v] = 0; vrate[v] = 0; }
+  if (active) {
+    #pragma unroll
+    for (int d = 0; d < ND; ++d) {
+      const int stride = S::stride(d);
+      const int i = node_of[d];
+      const R* bf = my_bf + d*2*nv*nfq;
+      #pragma unroll
+      for (int v = 0; v < nv; ++v) {
+        const R* row = my_f + (d*nv + v)*nq + base_of[d];
+        R acc = 0;
+        #pragma unroll
+        for (int j = 0; j < RS; ++j) acc += st.diff[i*RS + j]*row[j*stride];
+        R l = 0;
+        l += st.lift[i*2]*bf[v*nfq + row_of[d]];
+        l += st.lift[i*2 + 1]*bf[(nv + v)*nfq + row_of[d]];
+        rate[v] = rate[v] + -(acc + l);
+        if constexpr (VISC) {
+          const R* rg = my_g + (d*nv + v)*nq + base_of[d];
+          R ag = 0;
+          #pragma unroll
+          for (int j = 0; j < RS; ++j) ag += st.diff[i*RS + j]*rg[j*stride];
+          vrate[v] = vrate[v] + -ag;
+        }
+      }
+    }
+  }
+
+  // ---- modal filter (Spatial.hpp:473-481), one dimension at a time through shared memory
+  if (use_filter) {
+    #pragma unroll 1
+    for (int d = 0; d < ND; ++d) {
+      __syncthreads();
+      if (active) {
+        #pragma unroll
+        for (int v = 0; v < nv; ++v) { my_f[v*nq + q] = rate[v]; my_f[(nv + v)*nq + q] = vrate[v]; }
+      }
+      __syncthreads();
+      if (active) {
+        const int stride = S::stride(d);
+        const int i = node_of[d];
+        #pragma unroll
+        for (int v = 0; v < 2*nv; ++v) {
+          const R* row = my_f + v*nq + base_of[d];
+          R acc = 0;
+          #pragma unroll
+          for (int j = 0; j < RS; ++j) acc += st.filter[i*RS + j]*row[j*stride];
+          if (v < nv) rate[v] = acc; else vrate[v - nv] = acc;
+        }
+      }
+    }
+  }
+
+  // ---- stage update (Spatial.hpp:484-503), in double
+  if (active) {
+    const double dt = m.scalars[SC_DT];
+    const double update_coef = stage ? dt*tab.step_ratio : dt;
+    double* st_w = m.elem + (size_t)e*(nv + 3)*nq;
+    double* rc = m.rcache + (size_t)e*nv*nq;
+    double mult = update_coef*st_w[nv*nq + q]/d_pos;
+    if constexpr (DEF) mult /= m.jac[((size_t)ed*(ND*ND + 1) + ND*ND)*nq + q];
+    #pragma unroll
+    for (int v = 0; v < nv; ++v) {
+      double uu = double(rate[v]);
+      if (stage) {
+        uu -= rc[v*nq + q];
+      } else {
+        rc[v*nq + q] = uu;
+        if constexpr (VISC) uu += double(vrate[v]);
+      }
+      uu *= mult;
+      if (compute_residual) rc[v*nq + q] = uu;
+      else {
+        double nu = st_w[v*nq + q] + uu;
+        st_w[v*nq + q] = nu;
+        u[v] = R(nu);
+      }
+    }
+  }
+  // ---- Write_face of the new state (Spatial.hpp:507); the viscous path defers it
+  if constexpr (!VISC) {
+    __syncthreads();
+    if (active) {
+      #pragma unroll
+      for (int v = 0; v < nv; ++v) my_u[v*nq + q] = u[v];
+    }
+    __syncthreads();
+    write_faces_from_smem<ND, RS, R, FaceT>(m, st, s_u, e0, e_end);
+  }
+}
+
+// ------------------------------------------------------------------- Reconcile_ldg_flux
+// include/Spatial.hpp:543-594, fused with Write_face.
+template <int ND, int RS, typename R, bool DEF>
+struct ReconcileSmem {
+  using S = Shape<ND, RS>;
+  static constexpr size_t bytes = sizeof(STab<RS, R>) + sizeof(R)*(size_t)(S::epb*2*S::nv*S::nq) + 16;
+};
+
+template <int ND, int RS, typename R, bool DEF, typename FaceT>
+__global__ void __launch_bounds__(Shape<ND, RS>::threads)
+k_reconcile_ldg(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int compute_residual, int use_filter)
+{
+  using S = Shape<ND, RS>;
+  constexpr int nq = S::nq, nfq = S::nfq, nv = S::nv, EPB = S::epb;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  STab<RS, R>& st = *reinterpret_cast<STab<RS, R>*>(smem_raw);
+  R* s_u = reinterpret_cast<R*>(smem_raw + (sizeof(STab<RS, R>) + 15)/16*16);
+  R* s_t = s_u + EPB*nv*nq;
+  st.load(tab);
+  __syncthreads();
+  const int le = threadIdx.x/nq, q = threadIdx.x%nq;
+  const int e0 = e_begin + blockIdx.x*EPB, e = e0 + le;
+  const bool active = threadIdx.x < EPB*nq && e < e_end;
+  R tr[nv];
+  #pragma unroll
+  for (int v = 0; v < nv; ++v) tr[v] = 0;
+  int node_of[ND], base_of[ND];
+  #pragma unroll
+  for (int d = 0; d < ND; ++d) {
+    const int stride = S::stride(d);
+    node_of[d] = (q/stride)%RS;
+    base_of[d] = q - node_of[d]*stride;
+  }
+  if (active) {
+    #pragma unroll
+    for (int d = 0; d < ND; ++d) {
+      const int stride = S::stride(d);
+      const int i = node_of[d];
+      const int r = (q/(stride*RS))*stride + q%stride;
+      const FaceT* fl = m.face + (size_t)(e*2*ND + 2*d)*S::slot_dof + nv*nfq + r;
+      #pragma unroll
+      for (int v = 0; v < nv; ++v) {
+        R b0 = R(fl[v*nfq]), b1 = R(fl[S::slot_dof + v*nfq]);
+        R l = 0;
+        l += st.lift[i*2]*b0;
+        l += st.lift[i*2 + 1]*b1;
+        tr[v] = tr[v] + -l;
+      }
+    }
+  }
+  if (use_filter) {
+    R* my_t = s_t + le*nv*nq;
+    #pragma unroll 1
+    for (int d = 0; d < ND; ++d) {
+      __syncthreads();
+      if (active) {
+        #pragma unroll
+        for (int v = 0; v < nv; ++v) my_t[v*nq + q] = tr[v];
+      }
+      __syncthreads();
+      if (active) {
+        const int stride = S::stride(d);
+        const int i = node_of[d];
+        #pragma unroll
+        for (int v = 0; v < nv; ++v) {
+          const R* row = my_t + v*nq + base_of[d];
+          R acc = 0;
+          #pragma unroll
+          for (int j = 0; j < RS; ++j) acc += st.filter[i*RS + j]*row[j*stride];
+          tr[v] = acc;
+        }
+      }
+    }
+  }
+  R* my_u = s_u + le*nv*nq;
+  if (active) {
+    const double dt = m.scalars[SC_DT];
+    double* st_w = m.elem + (size_t)e*(nv + 3)*nq;
+    double mult = dt*st_w[nv*nq + q]/m.nom_size[e];
+    if constexpr (DEF) mult /= m.jac[((size_t)(e - m.n_car)*(ND*ND + 1) + ND*ND)*nq + q];
+    double* to_update = compute_residual ? m.rcache + (size_t)e*nv*nq : st_w;
+    const int ld = compute_residual ? nq : nq;
+    #pragma unroll
+    for (int v = 0; v < nv; ++v) to_update[v*ld + q] += double(tr[v])*mult;
+    #pragma unroll
+    for (int v = 0; v < nv; ++v) my_u[v*nq + q] = R(st_w[v*nq + q]);
+  }
+  __syncthreads();
+  write_faces_from_smem<ND, RS, R, FaceT>(m, st, s_u, e0, e_end);
+}
+
+// ------------------------------------------------------------------- Neighbor
+// Spatial::Neighbor (include/Spatial.hpp:613-705): local Lax-Friedrichs flux written back
+// to both faces with sign; LDG face average for the viscous path. One thread per face qpoint.
+template <int ND, int RS, typename R, typename FaceT>
+__device__ __forceinline__ void neighbor_point(const Dev<FaceT>& m, int slot0, int slot1, int dir, int q,
+                                               const double* nrml, bool viscous, const R* ghost_override)
+{
+  using S = Shape<ND, RS>;
+  constexpr int nfq = S::nfq, nv = S::nv;
+  const bool deformed = nrml != nullptr;
+  int sign0 = 1, sign1 = 1;
+  if (deformed) {
+    sign0 = 1 - 2*(((dir >> 4) & 1) == 0);
+    sign1 = 1 - 2*(((dir >> 5) & 1) == 1);
+  }
+  const int q1 = deformed ? perm_index<ND, RS>(dir, q) : q;
+  FaceT* f0 = m.face + (size_t)slot0*S::slot_dof;
+  FaceT* f1 = m.face + (size_t)slot1*S::slot_dof;
+  R u0[nv], u1[nv];
+  #pragma unroll
+  for (int v = 0; v < nv; ++v) {
+    u0[v] = R(f0[v*nfq + q]);
+    u1[v] = ghost_override ? ghost_override[v] : R(f1[v*nfq + q1]);
+  }
+  if (viscous) {
+    #pragma unroll
+    for (int v = 0; v < nv; ++v) {
+      R avg = R(.5)*(u0[v] + u1[v]);
+      f0[nv*nfq + v*nfq + q] = FaceT(avg);
+      f1[nv*nfq + v*nfq + q1] = FaceT(avg);
+    }
+  }
+  R n[ND];
+  const int i_dim0 = dir & 3;
+  #pragma unroll
+  for (int d = 0; d < ND; ++d) n[d] = deformed ? R(sign0)*R(nrml[d*nfq + q]) : (d == i_dim0 ? R(1) : R(0));
+  R fl0[nv], fl1[nv];
+  Conv<ND, R> c0(u0), c1(u1);
+  c0.flux(u0, n, fl0);
+  c1.flux(u1, n, fl1);
+  const R cs0 = char_speed<ND, R>(u0), cs1 = char_speed<ND, R>(u1);
+  R nn = 0;
+  #pragma unroll
+  for (int d = 0; d < ND; ++d) nn += n[d]*n[d];
+  const R mult = fmax(cs0, cs1)*sqrt(nn);
+  #pragma unroll
+  for (int v = 0; v < nv; ++v) {
+    R flux = R(.5)*(fl0[v] + fl1[v] + mult*(u0[v] - u1[v]));
+    f0[v*nfq + q] = FaceT(R(sign0)*flux);
+    f1[v*nfq + q1] = FaceT(R(sign1)*flux);
+  }
+}
+
+template <int ND, int RS, typename R, bool DEF, bool VISC, typename FaceT>
+__global__ void k_neighbor(Dev<FaceT> m)
+{
+  using S = Shape<ND, RS>;
+  constexpr int nfq = S::nfq;
+  const int n_con = DEF ? m.n_def_con : m.n_car_con;
+  const long total = (long)n_con*nfq;
+  for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
+    const int i = int(t/nfq), q = int(t%nfq);
+    if constexpr (DEF) {
+      const int* c = m.def_con + 3*i;
+      neighbor_point<ND, RS, R, FaceT>(m, c[0], c[1], c[2], q, m.def_con_nrml + (size_t)i*ND*nfq, VISC, nullptr);
+    } else {
+      const int* c = m.car_con + 3*i;
+      neighbor_point<ND, RS, R, FaceT>(m, c[0], c[1], c[2] | (c[2] << 2) | (1 << 4), q, nullptr, VISC, nullptr);
+    }
+  }
+}
+
+// ------------------------------------------------------------------- boundary conditions
+// Characteristics (include/pde.hpp:182-256) solved with partially pivoted LU; apply_char
+// (src/Boundary_condition.cpp:82-95).
+template <int ND>
+struct Characteristics {
+  double vals[3], vecs[3][3], dir[ND], mass, veloc[ND];
+  double lu[3][3]; int piv[3];
+  __device__ double nrml(const double* v) const { double r = 0.; for (int d = 0; d < ND; ++d) r += dir[d]*v[d]; return r; }
+  __device__ void tang(const double* v, double* out) const { double n = nrml(v); for (int d = 0; d < ND; ++d) out[d] = v[d] - dir[d]*n; }
+  __device__ Characteristics(const double* state, const double* direction)
+  {
+    double nsq = 0.;
+    for (int d = 0; d < ND; ++d) nsq += direction[d]*direction[d];
+    double norm = sqrt(nsq);
+    for (int d = 0; d < ND; ++d) dir[d] = direction[d]/norm;
+    mass = state[ND];
+    for (int d = 0; d < ND; ++d) veloc[d] = state[d]/mass;
+    double vsq = 0.;
+    for (int d = 0; d < ND; ++d) vsq += veloc[d]*veloc[d];
+    double pres = .4*(state[ND + 1] - .5*mass*vsq);
+    double sound_speed = sqrt(1.4*fmax(pres, 0.)/mass);
+    vals[2] = nrml(veloc);
+    vals[0] = vals[2] - sound_speed;
+    vals[1] = vals[2] + sound_speed;
+    for (int sign = 0; sign < 2; ++sign) {
+      double d_veloc = (2*sign - 1)*sound_speed/mass*1.;
+      double d_pres = 1.4*pres/mass*1.;
+      vecs[0][sign] = 1.*vals[2] + mass*d_veloc;
+      vecs[1][sign] = 1.;
+      vecs[2][sign] = d_pres/.4 + .5*1.*vsq + mass*vals[2]*d_veloc;
+    }
+    vecs[0][2] = 1.*vals[2];
+    vecs[1][2] = 1.;
+    vecs[2][2] = .5*1.*vsq;
+    for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) lu[i][j] = vecs[i][j];
+    for (int i = 0; i < 3; ++i) piv[i] = i;
+    for (int k = 0; k < 3; ++k) {
+      int p = k;
+      for (int i = k + 1; i < 3; ++i) if (fabs(lu[i][k]) > fabs(lu[p][k])) p = i;
+      if (p != k) {
+        for (int j = 0; j < 3; ++j) { double t = lu[k][j]; lu[k][j] = lu[p][j]; lu[p][j] = t; }
+        int t = piv[k]; piv[k] = piv[p]; piv[p] = t;
+      }
+      for (int i = k + 1; i < 3; ++i) {
+        double f = lu[k][k] != 0. ? lu[i][k]/lu[k][k] : 0.;
+        lu[i][k] = f;
+        for (int j = k + 1; j < 3; ++j) lu[i][j] -= f*lu[k][j];
+      }
+    }
+  }
+  __device__ void solve(const double* b, double* x) const
+  {
+    double y[3];
+    for (int i = 0; i < 3; ++i) {
+      double acc = b[piv[i]];
+      for (int j = 0; j < i; ++j) acc -= lu[i][j]*y[j];
+      y[i] = acc;
+    }
+    for (int i = 2; i >= 0; --i) {
+      double acc = y[i];
+      for (int j = i + 1; j < 3; ++j) acc -= lu[i][j]*x[j];
+      x[i] = lu[i][i] != 0. ? acc/lu[i][i] : 0.;
+    }
+  }
+  __device__ void decomp(const double* state, double (*d)[3]) const
+  {
+    double mmtm[ND], tm[ND], tv[ND], corr[ND];
+    for (int i = 0; i < ND; ++i) mmtm[i] = state[i];
+    tang(mmtm, tm);
+    tang(veloc, tv);
+    for (int i = 0; i < ND; ++i) corr[i] = tm[i] - state[ND]*tv[i];
+    double vc = 0.;
+    for (int i = 0; i < ND; ++i) vc += veloc[i]*corr[i];
+    double s1d[3] = {nrml(mmtm), state[ND], state[ND + 1] - vc};
+    double eb[3];
+    solve(s1d, eb);
+    double ed[3][3];
+    for (int r = 0; r < 3; ++r) for (int c = 0; c < 3; ++c) ed[r][c] = vecs[r][c]*eb[c];
+    for (int c = 0; c < 3; ++c) {
+      d[ND][c] = ed[1][c];
+      d[ND + 1][c] = ed[2][c];
+      for (int i = 0; i < ND; ++i) d[i][c] = dir[i]*ed[0][c] + tv[i]*eb[c];
+    }
+    for (int i = 0; i < ND; ++i) d[i][2] += corr[i];
+    d[ND + 1][2] += vc;
+  }
+};
+
+template <int ND>
+__device__ void apply_char(const double* state, const double* normal, int sign, const double* inside,
+                           const double* outside, double* out)
+{
+  constexpr int nv = ND + 2;
+  Characteristics<ND> ch(state, normal);
+  double di[nv][3], fo[nv][3];
+  ch.decomp(inside, di);
+  ch.decomp(outside, fo);
+  for (int i = 0; i < 3; ++i) if (sign*ch.vals[i] > 0) for (int r = 0; r < nv; ++r) di[r][i] = fo[r][i];
+  for (int r = 0; r < nv; ++r) { double acc = 0.; for (int c = 0; c < 3; ++c) acc += di[r][c]; out[r] = acc; }
+}
+
+__device__ __forceinline__ double ipow_d(double x, int e) { double r = 1; for (int i = 0; i < e; ++i) r *= x; return r; }
+
+template <int ND>
+__device__ double ghost_heat_flux(const hexed_bc_spec& b, const double* s, double heat_flux)
+{
+  constexpr int nv = ND + 2;
+  if (b.thermal_kind == HEXED_THERMAL_ENERGY) return heat_flux;
+  if (b.thermal_kind == HEXED_THERMAL_HEAT_FLUX) return b.thermal_value;
+  double temp = s[nv - 1]*.4/s[nv - 2]/specific_gas_air;
+  const double sb = 2*ipow_d(3.14159265358979323846, 5)*ipow_d(1.380649e-23, 4)/(15*ipow_d(299792458., 2)*ipow_d(6.62607015e-34, 3));
+  return b.emissivity*sb*ipow_d(temp, 4) + b.heat_transfer_coef*(temp - b.temperature);
+}
+
+// Flow_bc::apply_state for one face qpoint (src/Boundary_condition.cpp). Writes the ghost
+// state into `gh` (registers) and the slot, and the state cache where the BC primes it.
+template <int ND, int RS, typename FaceT>
+__device__ void bc_state_point(const Dev<FaceT>& m, int i_bc, int q, double* gh)
+{
+  using S = Shape<ND, RS>;
+  constexpr int nfq = S::nfq, nv = S::nv;
+  const int* c = m.bc_con + 4*i_bc;
+  const hexed_bc_spec& b = m.bc_spec[c[3]];
+  const int ifs = (c[2] >> 2) & 1;
+  FaceT* in = m.face + (size_t)c[0]*S::slot_dof;
+  FaceT* gf = m.face + (size_t)c[1]*S::slot_dof;
+  const double* nrml = m.bc_nrml + (size_t)i_bc*ND*nfq;
+  double* sc = m.bc_cache + (size_t)i_bc*2*nv*nfq;
+  double inside[nv], n[ND];
+  for (int v = 0; v < nv; ++v) inside[v] = double(in[v*nfq + q]);
+  for (int d = 0; d < ND; ++d) n[d] = nrml[d*nfq + q];
+  switch (b.kind) {
+    case HEXED_BC_FREESTREAM:
+      for (int v = 0; v < nv; ++v) gh[v] = b.freestream[v];
+      break;
+    case HEXED_BC_RIEMANN_INVARIANTS: {
+      double st[nv];
+      apply_char<ND>(inside, n, 1 - 2*ifs, inside, b.freestream, st);
+      st[ND] = fmax(st[ND], inside[ND]/2);
+      double sq = 0., isq = 0.;
+      for (int d = 0; d < ND; ++d) { sq += st[d]*st[d]; isq += inside[d]*inside[d]; }
+      double kin = .5*sq/st[ND];
+      double ikin = .5*isq/inside[ND];
+      st[ND + 1] = fmax(kin + fmax(st[ND + 1] - kin, (inside[ND + 1] - ikin)/2), 0.);
+      for (int v = 0; v < nv; ++v) { gh[v] = st[v]; sc[v*nfq + q] = inside[v]; }
+      break;
+    }
+    case HEXED_BC_NONPENETRATION: {
+      double dot = 0., norm_sq = 0.;
+      for (int d = 0; d < ND; ++d) { dot += inside[d]*n[d]; norm_sq += n[d]*n[d]; }
+      for (int v = 0; v < nv; ++v) gh[v] = inside[v];
+      for (int d = 0; d < ND; ++d) gh[d] -= 2*dot*n[d]/norm_sq;
+      break;
+    }
+    case HEXED_BC_COPY:
+    case HEXED_BC_OUTFLOW:
+      for (int v = 0; v < nv; ++v) { gh[v] = inside[v]; gf[nv*nfq + v*nfq + q] = in[nv*nfq + v*nfq + q]; }
+      break;
+    case HEXED_BC_PRESSURE_OUTFLOW: {
+      const int sign = 2*ifs - 1;
+      double dot = 0., nsq = 0., msq = 0.;
+      for (int d = 0; d < ND; ++d) { dot += inside[d]*n[d]; nsq += n[d]*n[d]; msq += inside[d]*inside[d]; }
+      double nrml_veloc = dot/inside[ND]/sqrt(nsq);
+      double kin = .5*msq/inside[ND];
+      double pres = fmax(.4*(inside[ND + 1] - kin), 0.);
+      double sound = sqrt(1.4*pres/inside[ND]);
+      for (int v = 0; v < nv; ++v) gh[v] = inside[v];
+      if (nrml_veloc*sign < sound) gh[ND + 1] = b.pressure/.4 + kin;
+      break;
+    }
+    case HEXED_BC_NO_SLIP: {
+      for (int d = 0; d < ND; ++d) gh[d] = -inside[d];
+      gh[ND] = inside[ND];
+      double ge = (b.thermal_kind == HEXED_THERMAL_ENERGY) ? b.thermal_value*inside[ND] : inside[ND + 1];
+      gh[ND + 1] = ge*ge/inside[nv - 1];
+      for (int v = 0; v < nv; ++v) sc[v*nfq + q] = (gh[v] + inside[v])/2;
+      break;
+    }
+    default:
+      for (int v = 0; v < nv; ++v) gh[v] = inside[v];
+      break;
+  }
+  for (int v = 0; v < nv; ++v) gf[v*nfq + q] = FaceT(gh[v]);
+}
+
+template <int ND, int RS, typename FaceT>
+__global__ void k_bc_state(Dev<FaceT> m)
+{
+  constexpr int nfq = Shape<ND, RS>::nfq;
+  const long total = (long)m.n_bc_con*nfq;
+  for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
+    double gh[ND + 2];
+    bc_state_point<ND, RS, FaceT>(m, int(t/nfq), int(t%nfq), gh);
+  }
+}
+
+// Neighbor over boundary connections; with FUSE the state BC is applied first in the same
+// thread (Solver::apply_state_bcs followed by the boundary part of Neighbor).
+template <int ND, int RS, typename R, bool VISC, bool FUSE, typename FaceT>
+__global__ void k_bc_neighbor(Dev<FaceT> m)
+{
+  constexpr int nfq = Shape<ND, RS>::nfq;
+  const long total = (long)m.n_bc_con*nfq;
+  for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
+    const int i = int(t/nfq), q = int(t%nfq);
+    const int* c = m.bc_con + 4*i;
+    R gr[ND + 2];
+    const R* ov = nullptr;
+    if (FUSE) {
+      double gh[ND + 2];
+      bc_state_point<ND, RS, FaceT>(m, i, q, gh);
+      for (int v = 0; v < ND + 2; ++v) gr[v] = R(gh[v]);
+      ov = gr;
+    }
+    neighbor_point<ND, RS, R, FaceT>(m, c[0], c[1], bc_dir(c[2]), q, m.bc_nrml + (size_t)i*ND*nfq, VISC, ov);
+  }
+}
+
+// Solver::apply_flux_bcs (src/Solver.cpp:69-81) + Flow_bc::apply_flux.
+template <int ND, int RS, typename FaceT>
+__device__ void bc_flux_point(const Dev<FaceT>& m, int i_bc, int q)
+{
+  using S = Shape<ND, RS>;
+  constexpr int nfq = S::nfq, nv = S::nv;
+  const int* c = m.bc_con + 4*i_bc;
+  const hexed_bc_spec& b = m.bc_spec[c[3]];
+  const int ifs = (c[2] >> 2) & 1;
+  FaceT* in_l = m.face + (size_t)c[0]*S::slot_dof + nv*nfq;
+  FaceT* gh_l = m.face + (size_t)c[1]*S::slot_dof + nv*nfq;
+  const double* nrml = m.bc_nrml + (size_t)i_bc*ND*nfq;
+  double* sc = m.bc_cache + (size_t)i_bc*2*nv*nfq;
+  double* fc = sc + nv*nfq;
+  double in[nv], n[ND];
+  for (int v = 0; v < nv; ++v) { in[v] = double(in_l[v*nfq + q]); fc[v*nfq + q] = in[v]; }
+  for (int d = 0; d < ND; ++d) n[d] = nrml[d*nfq + q];
+  double out[nv];
+  switch (b.kind) {
+    case HEXED_BC_FREESTREAM:
+    case HEXED_BC_COPY: {
+      FaceT* in_s = m.face + (size_t)c[0]*S::slot_dof;
+      FaceT* gh_s = m.face + (size_t)c[1]*S::slot_dof;
+      for (int v = 0; v < nv; ++v) gh_s[v*nfq + q] = in_s[v*nfq + q];
+      for (int v = 0; v < nv; ++v) out[v] = in[v];
+      break;
+    }
+    case HEXED_BC_RIEMANN_INVARIANTS: {
+      double cache[nv], zero[nv];
+      for (int v = 0; v < nv; ++v) { cache[v] = sc[v*nfq + q]; zero[v] = 0.; }
+      apply_char<ND>(cache, n, 1 - 2*ifs, zero, in, out);
+      break;
+    }
+    case HEXED_BC_NONPENETRATION: {
+      for (int v = 0; v < nv; ++v) out[v] = -in[v];
+      double dot = 0., norm_sq = 0.;
+      for (int d = 0; d < ND; ++d) { dot += out[d]*n[d]; norm_sq += n[d]*n[d]; }
+      for (int d = 0; d < ND; ++d) out[d] -= 2*dot*n[d]/norm_sq;
+      break;
+    }
+    case HEXED_BC_OUTFLOW:
+    case HEXED_BC_PRESSURE_OUTFLOW:
+      for (int v = 0; v < nv; ++v) out[v] = -in[v];
+      break;
+    case HEXED_BC_NO_SLIP: {
+      for (int d = 0; d < ND; ++d) out[d] = in[d];
+      out[ND] = -in[ND];
+      double normal = 0;
+      for (int d = 0; d < ND; ++d) normal += n[d]*n[d];
+      normal = sqrt(normal);
+      const int flux_sign = 2*ifs - 1;
+      double s[nv];
+      for (int v = 0; v < nv; ++v) s[v] = sc[v*nfq + q];
+      const double x = in[ND + 1];
+      out[ND + 1] = b.coercion*(normal*flux_sign*ghost_heat_flux<ND>(b, s, x*flux_sign/normal) - x) + x;
+      break;
+    }
+    default:
+      for (int v = 0; v < nv; ++v) out[v] = in[v];
+  }
+  for (int v = 0; v < nv; ++v) gh_l[v*nfq + q] = FaceT(out[v]);
+}
+
+// Neighbor_reconcile (include/Spatial.hpp:716-759) for one face qpoint.
+template <int ND, int RS, typename R, typename FaceT>
+__device__ __forceinline__ void reconcile_point(const Dev<FaceT>& m, int slot0, int slot1, int dir, int q, bool deformed)
+{
+  using S = Shape<ND, RS>;
+  constexpr int nfq = S::nfq, nv = S::nv;
+  int sign0 = 1, sign1 = 1;
+  if (deformed) {
+    sign0 = 1 - 2*(((dir >> 4) & 1) == 0);
+    sign1 = 1 - 2*(((dir >> 5) & 1) == 1);
+  }
+  const int q1 = deformed ? perm_index<ND, RS>(dir, q) : q;
+  FaceT* l0 = m.face + (size_t)slot0*S::slot_dof + nv*nfq;
+  FaceT* l1 = m.face + (size_t)slot1*S::slot_dof + nv*nfq;
+  #pragma unroll
+  for (int v = 0; v < nv; ++v) {
+    R a = R(l0[v*nfq + q]), b = R(l1[v*nfq + q1]);
+    R avg = 0;
+    avg += R(.5*sign0)*a;
+    avg += R(.5*sign1)*b;
+    l0[v*nfq + q] = FaceT(R(sign0)*avg - a);
+    l1[v*nfq + q1] = FaceT(R(sign1)*avg - b);
+  }
+}
+
+template <int ND, int RS, typename R, int KIND, bool FUSE_BC, typename FaceT>  // KIND 0 car, 1 def, 2 bc
+__global__ void k_neighbor_reconcile(Dev<FaceT> m)
+{
+  constexpr int nfq = Shape<ND, RS>::nfq;
+  const int n_con = KIND == 0 ? m.n_car_con : KIND == 1 ? m.n_def_con : m.n_bc_con;
+  const long total = (long)n_con*nfq;
+  for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
+    const int i = int(t/nfq), q = int(t%nfq);
+    if (KIND == 0) {
+      const int* c = m.car_con + 3*i;
+      reconcile_point<ND, RS, R, FaceT>(m, c[0], c[1], 0, q, false);
+    } else if (KIND == 1) {
+      const int* c = m.def_con + 3*i;
+      reconcile_point<ND, RS, R, FaceT>(m, c[0], c[1], c[2], q, true);
+    } else {
+      const int* c = m.bc_con + 4*i;
+      if (FUSE_BC) bc_flux_point<ND, RS, FaceT>(m, i, q);
+      reconcile_point<ND, RS, R, FaceT>(m, c[0], c[1], bc_dir(c[2]), q, true);
+    }
+  }
+}
+
+template <int ND, int RS, typename FaceT>
+__global__ void k_bc_flux(Dev<FaceT> m)
+{
+  constexpr int nfq = Shape<ND, RS>::nfq;
+  const long total = (long)m.n_bc_con*nfq;
+  for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x)
+    bc_flux_point<ND, RS, FaceT>(m, int(t/nfq), int(t%nfq));
+}
+
+// ------------------------------------------------------------------- hanging faces
+// Prolong_refined / Restrict_refined (include/Spatial.hpp:153-285). One CTA per refined face;
+// thread (fine face, var, qpoint). Row transforms go through shared memory one dimension at a time.
+template <int ND, int RS, bool PROLONG, typename FaceT>
+__global__ void k_refine(Dev<FaceT> m, Tab<RS> tab, int scale, int offset)
+{
+  using S = Shape<ND, RS>;
+  constexpr int nfq = S::nfq, nv = S::nv;
+  constexpr int n_face = 1 << (ND - 1);
+  __shared__ double s_face[n_face*nv*nfq];
+  __shared__ double s_mat[2*RS*RS];
+  for (int i = threadIdx.x; i < 2*RS*RS; i += blockDim.x) s_mat[i] = PROLONG ? tab.prolong[i] : tab.restrict_[i];
+  const int i_ref = blockIdx.x;
+  const int* rf = m.ref_face + 7*i_ref;
+  const bool str[2] = {rf[5] != 0, rf[6] != 0};
+  int nf = n_face;
+  for (int d = 0; d < ND - 1; ++d) nf /= 1 + str[d];
+  FaceT* coarse = m.face + (size_t)rf[0]*S::slot_dof + offset*nv*nfq;
+  const int n_item = nf*nv*nfq;
+  __syncthreads();
+  for (int t = threadIdx.x; t < n_item; t += blockDim.x) {
+    const int i_face = t/(nv*nfq), k = t%(nv*nfq);
+    FaceT* fine = m.face + (size_t)rf[1 + i_face]*S::slot_dof + offset*nv*nfq;
+    s_face[t] = PROLONG ? double(coarse[k]) : double(fine[k]);
+  }
+  #pragma unroll 1
+  for (int d = 0; d < ND - 1; ++d) {
+    __syncthreads();
+    double val[(n_face*nv*nfq + 63)/64 + 1];
+    int cnt = 0;
+    for (int t = threadIdx.x; t < n_item; t += blockDim.x, ++cnt) {
+      const int i_face = t/(nv*nfq), k = t%(nv*nfq);
+      const int qq = k%nfq;
+      double x = s_face[t];
+      if (str[d]) {
+        x = PROLONG ? x*double(1 + scale) : x/double(1 + scale);
+      } else {
+        const int pw = ND - 2 - d;
+        const int face_stride = str[ND - 2] ? 1 : ipow(2, pw);
+        const int qstride = ipow(RS, pw);
+        const int i_half = (i_face/face_stride)%2;
+        const int i = (qq/qstride)%RS;
+        const int base = t - i*qstride;
+        const double* mat = s_mat + i_half*RS*RS;
+        double acc = 0.;
+        #pragma unroll
+        for (int j = 0; j < RS; ++j) acc += mat[i*RS + j]*s_face[base + j*qstride];
+        x = acc;
+      }
+      val[cnt] = x;
+    }
+    __syncthreads();
+    cnt = 0;
+    for (int t = threadIdx.x; t < n_item; t += blockDim.x, ++cnt) s_face[t] = val[cnt];
+  }
+  __syncthreads();
+  if (PROLONG) {
+    for (int t = threadIdx.x; t < n_item; t += blockDim.x) {
+      const int i_face = t/(nv*nfq), k = t%(nv*nfq);
+      FaceT* fine = m.face + (size_t)rf[1 + i_face]*S::slot_dof + offset*nv*nfq;
+      fine[k] = FaceT(s_face[t]);
+    }
+  } else {
+    for (int t = threadIdx.x; t < n_item; t += blockDim.x) {
+      const int i_face = t/(nv*nfq), k = t%(nv*nfq);
+      FaceT* fine = m.face + (size_t)rf[1 + i_face]*S::slot_dof + offset*nv*nfq;
+      fine[k] = FaceT(s_face[t]);
+    }
+    for (int k = threadIdx.x; k < nv*nfq; k += blockDim.x) {
+      double acc = 0.;
+      for (int i_face = 0; i_face < nf; ++i_face) acc += s_face[i_face*nv*nfq + k];
+      coarse[k] = FaceT(acc);
+    }
+  }
+}
+
+// ------------------------------------------------------------------- Write_face (standalone)
+template <int ND, int RS, typename FaceT>
+__global__ void k_write_face(Dev<FaceT> m, Tab<RS> tab)
+{
+  using S = Shape<ND, RS>;
+  constexpr int nq = S::nq, nfq = S::nfq, nv = S::nv;
+  const long total = (long)m.n_elem*ND*nv*nfq;
+  for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
+    int r = int(t%nfq); long rest = t/nfq;
+    int v = int(rest%nv); rest /= nv;
+    int d = int(rest%ND); int e = int(rest/ND);
+    const int stride = S::stride(d);
+    const double* row = m.elem + (size_t)e*(nv + 3)*nq + v*nq + (r/stride)*stride*RS + r%stride;
+    double a0 = 0., a1 = 0.;
+    for (int i = 0; i < RS; ++i) { double x = row[i*stride]; a0 += tab.bound[i]*x; a1 += tab.bound[RS + i]*x; }
+    FaceT* f0 = m.face + (size_t)(e*2*ND + 2*d)*S::slot_dof + v*nfq + r;
+    f0[0] = FaceT(a0);
+    f0[S::slot_dof] = FaceT(a1);
+  }
+}
+
+// ------------------------------------------------------------------- Max_dt
+// Spatial::Max_dt (include/Spatial.hpp:784-828); global minimum through per-CTA partials.
+template <int ND, int RS, bool VISC, typename FaceT>
+__global__ void __launch_bounds__(256)
+k_max_dt(Dev<FaceT> m, Tab<RS> tab, double msc, double msd, int local_time, hexed_transport visc,
+         hexed_transport cond, double* partials)
+{
+  using S = Shape<ND, RS>;
+  constexpr int nq = S::nq, nv = S::nv, nvert = S::nvert;
+  const double max_cfl_c = tab.max_cfl*msc;
+  const double max_cfl_d = -2/tab.min_eig_diffusion*msd;
+  double dt = 1.7976931348623157e308;
+  const long total = (long)m.n_elem*nq;
+  for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
+    const int e = int(t/nq), q = int(t%nq);
+    double* state = m.elem + (size_t)e*(nv + 3)*nq;
+    double vals[nvert];
+    #pragma unroll
+    for (int i = 0; i < nvert; ++i) vals[i] = m.vert_tss[(size_t)e*nvert + i];
+    int stride = nvert;
+    #pragma unroll
+    for (int d = 0; d < ND; ++d) {
+      const double coord = tab.node[(q/ipow(RS, ND - 1 - d))%RS];
+      stride /= 2;
+      #pragma unroll
+      for (int i = 0; i < (nvert >> (d + 1)); ++i) vals[i] += coord*(vals[i + stride] - vals[i]);
+    }
+    const double spacing = vals[0];
+    double s[nv];
+    #pragma unroll
+    for (int v = 0; v < nv; ++v) s[v] = state[v*nq + q];
+    double scale = 0;
+    scale += char_speed<ND, double>(s)/max_cfl_c/spacing;
+    if constexpr (VISC) {
+      Conv<ND, double> c(s);
+      DiffScalars<ND, double> df(s, c, state[(nv + 1)*nq + q], state[(nv + 2)*nq + q], visc, cond);
+      double diffusivity = fabs(df.laplacian_av) + fmax(fabs(df.bulk_av) + df.mu/c.mass, df.energy_cond/c.mass);
+      scale += diffusivity/max_cfl_d/spacing/spacing;
+    }
+    if (local_time) state[nv*nq + q] = 1./scale;
+    else {
+      state[nv*nq + q] = 1.;
+      dt = fmin(dt, 1./scale);
+    }
+  }
+  // CTA minimum
+  __shared__ double s_min[32];
+  for (int o = 16; o > 0; o >>= 1) dt = fmin(dt, __shfl_xor_sync(0xffffffffu, dt, o));
+  if ((threadIdx.x & 31) == 0) s_min[threadIdx.x >> 5] = dt;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double x = threadIdx.x < (blockDim.x + 31)/32 ? s_min[threadIdx.x] : 1.7976931348623157e308;
+    for (int o = 16; o > 0; o >>= 1) x = fmin(x, __shfl_xor_sync(0xffffffffu, x, o));
+    if (threadIdx.x == 0) partials[blockIdx.x] = x;
+  }
+}
+
+// Minimum over the CTA partials -> scalars[SC_MAXDT]; then the stage step
+// dt = min(max_dt, max_time_step)*cheby (src/Solver.cpp:843-846) -> scalars[SC_DT].
+static __global__ void k_finalize_dt(double* scalars, const double* partials, int n_part, int local_time,
+                              double max_time_step, double cheby)
+{
+  double x = 1.7976931348623157e308;
+  for (int i = threadIdx.x; i < n_part; i += blockDim.x) x = fmin(x, partials[i]);
+  __shared__ double s_min[32];
+  for (int o = 16; o > 0; o >>= 1) x = fmin(x, __shfl_xor_sync(0xffffffffu, x, o));
+  if ((threadIdx.x & 31) == 0) s_min[threadIdx.x >> 5] = x;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 1.7976931348623157e308;
+    for (int i = 0; i < (int)(blockDim.x + 31)/32; ++i) r = fmin(r, s_min[i]);
+    if (local_time) r = 1.;
+    scalars[SC_MAXDT] = r;
+    scalars[SC_DT] = fmin(r, max_time_step)*cheby;
+  }
+}
+
+static __global__ void k_set_scalar(double* scalars, int which, double value) { scalars[which] = value; }
+
+// FP64 pipe probe: fp64_fma_chains independent dependent-FMA chains per thread.
+constexpr int fp64_fma_chains = 8;
+static __global__ void k_fp64_fma(double* out, int iters, double a)
+{
+  double x[fp64_fma_chains];
+  #pragma unroll
+  for (int k = 0; k < fp64_fma_chains; ++k) x[k] = threadIdx.x*1e-3 + k;
+  for (int i = 0; i < iters; ++i) {
+    #pragma unroll
+    for (int k = 0; k < fp64_fma_chains; ++k) x[k] = fma(x[k], a, 1e-7);
+  }
+  double s = 0.;
+  #pragma unroll
+  for (int k = 0; k < fp64_fma_chains; ++k) s += x[k];
+  out[blockIdx.x*blockDim.x + threadIdx.x] = s;
+}
+
+// ------------------------------------------------------------------- residual norm
+// integral_field(Pow(Physical_residual, 2)) (src/Solver.cpp:1113-1131): per-CTA partial
+// sums in a fixed order, then one CTA sums the partials in order (deterministic).
+template <int ND, int RS, typename FaceT>
+__global__ void __launch_bounds__(256) k_residual_partial(Dev<FaceT> m, Tab<RS> tab, double* partials)
+{
+  using S = Shape<ND, RS>;
+  constexpr int nq = S::nq, nv = S::nv;
+  double acc[nv];
+  for (int v = 0; v < nv; ++v) acc[v] = 0.;
+  const long total = (long)m.n_elem*nq;
+  for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
+    const int e = int(t/nq), q = int(t%nq);
+    double w = 1.;
+    for (int d = 0; d < ND; ++d) w *= tab.weight[(q/ipow(RS, ND - 1 - d))%RS];
+    double vol = 1.;
+    for (int d = 0; d < ND; ++d) vol *= m.nom_size[e];
+    const double* st = m.elem + (size_t)e*(nv + 3)*nq;
+    const double* rc = m.rcache + (size_t)e*nv*nq;
+    const double jd = e >= m.n_car ? m.jac[((size_t)(e - m.n_car)*(ND*ND + 1) + ND*ND)*nq + q] : 1.;
+    const double tss = st[nv*nq + q];
+    for (int v = 0; v < nv; ++v) {
+      double r = rc[v*nq + q]/tss;
+      acc[v] += w*vol*(r*r)*jd;
+    }
+  }
+  __shared__ double s_acc[256][nv];
+  for (int v = 0; v < nv; ++v) s_acc[threadIdx.x][v] = acc[v];
+  __syncthreads();
+  for (int half = blockDim.x/2; half > 0; half >>= 1) {
+    if ((int)threadIdx.x < half) for (int v = 0; v < nv; ++v) s_acc[threadIdx.x][v] += s_acc[threadIdx.x + half][v];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) for (int v = 0; v < nv; ++v) partials[blockIdx.x*nv + v] = s_acc[0][v];
+}
+
+template <int NV>
+__global__ void k_residual_final(const double* partials, int n_part, double* out)
+{
+  if (threadIdx.x != 0) return;
+  double acc[NV];
+  for (int v = 0; v < NV; ++v) acc[v] = 0.;
+  for (int i = 0; i < n_part; ++i) for (int v = 0; v < NV; ++v) acc[v] += partials[i*NV + v];
+  double mom = 0.;
+  for (int d = 0; d < NV - 2; ++d) mom += acc[d];
+  out[0] = sqrt(mom);
+  out[1] = sqrt(acc[NV - 2]);
+  out[2] = sqrt(acc[NV - 1]);
+}
+
+} // namespace hx

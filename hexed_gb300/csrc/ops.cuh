@@ -1,0 +1,233 @@
+// ops.cuh -- host-side launch sequences for one (n_dim, row_size).
+//
+// The instantiation units (inst_<nd>_<rs>.cu) include this file once each, so the
+// kernels of different row sizes compile in parallel. The sequences mirror the
+// reference's kernel calls: compute_euler (src/kernels_convective.cpp:8-19),
+// compute_navier_stokes (src/kernels_diffusive.cpp:8-32), max_dt_* (src/kernels_max_dt.cpp).
+#pragma once
+#include "kernels.cuh"
+#include "ctx.h"
+
+namespace hx {
+
+inline int grid_for(long items, int block, int max_blocks = 152*16)
+{
+  long g = (items + block - 1)/block;
+  if (g < 1) g = 1;
+  if (g > max_blocks) g = max_blocks;
+  return int(g);
+}
+
+template <int ND, int RS, typename R>
+struct Runner
+{
+  using S = Shape<ND, RS>;
+  using FaceT = double;
+
+  static Dev<FaceT> dev(Ctx& c)
+  {
+    Dev<FaceT> m;
+    m.n_car = c.n_car; m.n_def = c.n_def; m.n_elem = c.n_car + c.n_def; m.n_slot = c.n_slot;
+    m.n_car_con = c.n_car_con; m.n_def_con = c.n_def_con; m.n_bc_con = c.n_bc_con; m.n_ref = c.n_ref;
+    m.elem = c.elem; m.rcache = c.rcache; m.face = c.face;
+    m.nom_size = c.nom_size; m.vert_tss = c.vert_tss; m.jac = c.jac; m.face_nrml = c.face_nrml;
+    m.car_con = c.car_con; m.def_con = c.def_con; m.def_con_nrml = c.def_con_nrml;
+    m.bc_con = c.bc_con; m.bc_nrml = c.bc_nrml; m.bc_cache = c.bc_cache; m.ref_face = c.ref_face;
+    m.bc_spec = c.bc_spec; m.scalars = c.scalars; m.partials = c.partials; m.status = c.status;
+    return m;
+  }
+
+  static Tab<RS> tab(const Ctx& c)
+  {
+    Tab<RS> t;
+    const HostTables& h = c.tables;
+    for (int i = 0; i < RS*RS; ++i) { t.diff[i] = h.diff[i]; t.filter[i] = h.filter[i]; }
+    for (int i = 0; i < 2*RS; ++i) { t.bound[i] = h.bound[i]; }
+    for (int i = 0; i < RS; ++i) {
+      double inv_w = 1./h.weight[i];
+      t.lift[i*2] = -(inv_w*h.bound[i]);
+      t.lift[i*2 + 1] = inv_w*h.bound[RS + i];
+      t.node[i] = h.node[i];
+      t.weight[i] = h.weight[i];
+    }
+    for (int i = 0; i < 2*RS*RS; ++i) { t.prolong[i] = h.prolong[i]; t.restrict_[i] = h.restrict_[i]; }
+    t.max_cfl = h.max_cfl; t.min_eig_diffusion = h.min_eig_diffusion; t.step_ratio = h.step_ratio;
+    return t;
+  }
+
+  template <bool DEF, bool VISC>
+  static void local(Ctx& c, int stage, int cr, int uf, const hexed_transport& visc, const hexed_transport& cond)
+  {
+    const int e_begin = DEF ? c.n_car : 0;
+    const int e_end = DEF ? c.n_car + c.n_def : c.n_car;
+    if (e_end <= e_begin) return;
+    const int blocks = (e_end - e_begin + S::epb - 1)/S::epb;
+    constexpr size_t smem = LocalSmem<ND, RS, R, DEF, VISC>::bytes;
+    auto kern = k_local<ND, RS, R, DEF, VISC, FaceT>;
+    static bool configured = false;
+    if (!configured) {
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      configured = true;
+    }
+    ProfScope ps(c, DEF ? (VISC ? "local_def_ns" : "local_def_euler") : (VISC ? "local_car_ns" : "local_car_euler"));
+    kern<<<blocks, S::threads, smem, c.stream>>>(dev(c), tab(c), e_begin, e_end, stage, cr, uf, visc, cond);
+  }
+
+  template <bool DEF>
+  static void reconcile(Ctx& c, int cr, int uf)
+  {
+    const int e_begin = DEF ? c.n_car : 0;
+    const int e_end = DEF ? c.n_car + c.n_def : c.n_car;
+    if (e_end <= e_begin) return;
+    const int blocks = (e_end - e_begin + S::epb - 1)/S::epb;
+    constexpr size_t smem = ReconcileSmem<ND, RS, R, DEF>::bytes;
+    auto kern = k_reconcile_ldg<ND, RS, R, DEF, FaceT>;
+    static bool configured = false;
+    if (!configured) {
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      configured = true;
+    }
+    ProfScope ps(c, DEF ? "reconcile_ldg_def" : "reconcile_ldg_car");
+    kern<<<blocks, S::threads, smem, c.stream>>>(dev(c), tab(c), e_begin, e_end, cr, uf);
+  }
+
+  template <bool VISC>
+  static void neighbor(Ctx& c, bool fuse_bc)
+  {
+    const int block = 256;
+    if (c.n_car_con) {
+      ProfScope ps(c, "neighbor_car");
+      k_neighbor<ND, RS, R, false, VISC, FaceT><<<grid_for((long)c.n_car_con*S::nfq, block), block, 0, c.stream>>>(dev(c));
+    }
+    if (c.n_def_con) {
+      ProfScope ps(c, "neighbor_def");
+      k_neighbor<ND, RS, R, true, VISC, FaceT><<<grid_for((long)c.n_def_con*S::nfq, block), block, 0, c.stream>>>(dev(c));
+    }
+    if (c.n_bc_con) {
+      ProfScope ps(c, fuse_bc ? "neighbor_bc_fused" : "neighbor_bc");
+      if (fuse_bc) k_bc_neighbor<ND, RS, R, VISC, true, FaceT><<<grid_for((long)c.n_bc_con*S::nfq, block), block, 0, c.stream>>>(dev(c));
+      else k_bc_neighbor<ND, RS, R, VISC, false, FaceT><<<grid_for((long)c.n_bc_con*S::nfq, block), block, 0, c.stream>>>(dev(c));
+    }
+  }
+
+  static void refine(Ctx& c, bool prolong, bool scale, bool offset)
+  {
+    if (!c.n_ref) return;
+    ProfScope ps(c, prolong ? "prolong" : "restrict");
+    if (prolong) k_refine<ND, RS, true, FaceT><<<c.n_ref, 256, 0, c.stream>>>(dev(c), tab(c), scale, offset);
+    else k_refine<ND, RS, false, FaceT><<<c.n_ref, 256, 0, c.stream>>>(dev(c), tab(c), scale, offset);
+  }
+
+  static void bc_state(Ctx& c)
+  {
+    ProfScope ps(c, "bc_state");
+    if (c.n_bc_con) k_bc_state<ND, RS, FaceT><<<grid_for((long)c.n_bc_con*S::nfq, 256), 256, 0, c.stream>>>(dev(c));
+  }
+
+  static void bc_flux(Ctx& c)
+  {
+    ProfScope ps(c, "bc_flux");
+    if (c.n_bc_con) k_bc_flux<ND, RS, FaceT><<<grid_for((long)c.n_bc_con*S::nfq, 256), 256, 0, c.stream>>>(dev(c));
+  }
+
+  static void neighbor_reconcile(Ctx& c, bool fuse_bc)
+  {
+    const int block = 256;
+    if (c.n_car_con) {
+      ProfScope ps(c, "neighbor_reconcile_car");
+      k_neighbor_reconcile<ND, RS, R, 0, false, FaceT><<<grid_for((long)c.n_car_con*S::nfq, block), block, 0, c.stream>>>(dev(c));
+    }
+    if (c.n_def_con) {
+      ProfScope ps(c, "neighbor_reconcile_def");
+      k_neighbor_reconcile<ND, RS, R, 1, false, FaceT><<<grid_for((long)c.n_def_con*S::nfq, block), block, 0, c.stream>>>(dev(c));
+    }
+    if (c.n_bc_con) {
+      ProfScope ps(c, fuse_bc ? "neighbor_reconcile_bc_fused" : "neighbor_reconcile_bc");
+      if (fuse_bc) k_neighbor_reconcile<ND, RS, R, 2, true, FaceT><<<grid_for((long)c.n_bc_con*S::nfq, block), block, 0, c.stream>>>(dev(c));
+      else k_neighbor_reconcile<ND, RS, R, 2, false, FaceT><<<grid_for((long)c.n_bc_con*S::nfq, block), block, 0, c.stream>>>(dev(c));
+    }
+  }
+
+  // compute_euler (src/kernels_convective.cpp:8-19). fuse_bc: apply the state BCs inside
+  // the boundary part of Neighbor (used by the solver layer, which would otherwise run
+  // Solver::apply_state_bcs immediately before).
+  static void compute_euler(Ctx& c, int stage, int cr, int uf, bool fuse_bc)
+  {
+    hexed_transport inv{0., 0., 1., 1., 0};
+    neighbor<false>(c, fuse_bc);
+    refine(c, false, true, false);
+    local<false, false>(c, stage, cr, uf, inv, inv);
+    local<true, false>(c, stage, cr, uf, inv, inv);
+    refine(c, true, false, false);
+  }
+
+  // compute_navier_stokes (src/kernels_diffusive.cpp:8-32) with the flux BCs on the device
+  static void compute_navier_stokes(Ctx& c, int stage, int cr, int uf, const hexed_transport& visc,
+                                    const hexed_transport& cond, bool fuse_bc)
+  {
+    neighbor<true>(c, fuse_bc);
+    refine(c, false, true, false);
+    refine(c, false, false, true);
+    local<false, true>(c, stage, cr, uf, visc, cond);
+    local<true, true>(c, stage, cr, uf, visc, cond);
+    if (!stage) {
+      refine(c, true, true, true);
+      neighbor_reconcile(c, true);   // flux BCs fused into the boundary part
+      refine(c, false, true, true);
+      reconcile<false>(c, cr, uf);
+      reconcile<true>(c, cr, uf);
+    }
+    refine(c, true, false, false);
+  }
+
+  static void max_dt(Ctx& c, double msc, double msd, int local_time, int viscous, const hexed_transport& visc,
+                     const hexed_transport& cond, double max_time_step, double cheby)
+  {
+    const long total = (long)(c.n_car + c.n_def)*S::nq;
+    const int grid = grid_for(total, 256, c.max_partials);
+    {
+      ProfScope ps(c, "max_dt");
+      if (viscous) k_max_dt<ND, RS, true, FaceT><<<grid, 256, 0, c.stream>>>(dev(c), tab(c), msc, msd, local_time, visc, cond, c.partials);
+      else k_max_dt<ND, RS, false, FaceT><<<grid, 256, 0, c.stream>>>(dev(c), tab(c), msc, msd, local_time, visc, cond, c.partials);
+    }
+    ProfScope ps(c, "finalize_dt");
+    k_finalize_dt<<<1, 256, 0, c.stream>>>(c.scalars, c.partials, grid, local_time, max_time_step, cheby);
+  }
+
+  static void write_face(Ctx& c)
+  {
+    const long total = (long)(c.n_car + c.n_def)*ND*S::nv*S::nfq;
+    ProfScope ps(c, "write_face");
+    k_write_face<ND, RS, FaceT><<<grid_for(total, 256), 256, 0, c.stream>>>(dev(c), tab(c));
+  }
+
+  static void residual_norm(Ctx& c, double* d_out)
+  {
+    const long total = (long)(c.n_car + c.n_def)*S::nq;
+    const int grid = grid_for(total, 256, c.max_partials/S::nv);
+    {
+      ProfScope ps(c, "residual_partial");
+      k_residual_partial<ND, RS, FaceT><<<grid, 256, 0, c.stream>>>(dev(c), tab(c), c.partials);
+    }
+    ProfScope ps(c, "residual_final");
+    k_residual_final<S::nv><<<1, 32, 0, c.stream>>>(c.partials, grid, d_out);
+  }
+
+  static const OpsTable* table()
+  {
+    static const OpsTable t = {
+      compute_euler, compute_navier_stokes, max_dt, refine, write_face, bc_state, bc_flux, residual_norm,
+    };
+    return &t;
+  }
+};
+
+} // namespace hx
+
+#define HEXED_INSTANTIATE(ND, RS) \
+  namespace hx { \
+  const OpsTable* ops_##ND##_##RS(int precision) \
+  { \
+    return precision == HEXED_MIXED ? Runner<ND, RS, float>::table() : Runner<ND, RS, double>::table(); \
+  } \
+  }

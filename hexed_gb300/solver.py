@@ -1,0 +1,197 @@
+"""Python host mirror of hexed's Solver / kernel layer over the C ABI of libhexed_gpu.so.
+
+``Context`` exposes one method per entry point of include/hexed_gpu.h (the free
+functions of the reference's include/kernels.hpp:22-42). ``Solver`` mirrors the
+reference's Solver methods used on the hot path (include/Solver.hpp:107-236):
+``update``, ``max_dt``, ``compute_residual``, ``initialize`` and the residual norms that
+Case.hil's ``compute_residuals`` reports. There is no CPU fallback: constructing a
+Context without the built library or without a GPU raises.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import abi
+
+
+class Context:
+    def __init__(self, arena, precision=abi.FP64):
+        self.lib = abi.load_library()
+        self.arena = arena
+        self.precision = precision
+        self._desc = arena.desc()
+        handle = ctypes.c_void_p()
+        abi.check(self.lib.hexed_gpu_create(ctypes.byref(self._desc), precision, ctypes.byref(handle)))
+        self.handle = handle
+
+    # -------------------------------------------------------------- lifetime / data
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.hexed_gpu_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _array(self, which):
+        a = self.arena
+        return {abi.ARRAY_ELEM: a.elem, abi.ARRAY_RCACHE: a.rcache, abi.ARRAY_FACE: a.face,
+                abi.ARRAY_BC_CACHE: a.bc_cache}[which]
+
+    def upload(self, which, host=None):
+        host = self._array(which) if host is None else host
+        host = np.ascontiguousarray(host, dtype=np.float64)
+        abi.check(self.lib.hexed_gpu_upload(self.handle, which, host.ctypes.data_as(abi.P_double)))
+
+    def download(self, which, out=None):
+        ref = self._array(which)
+        out = np.empty_like(ref) if out is None else out
+        abi.check(self.lib.hexed_gpu_download(self.handle, which, out.ctypes.data_as(abi.P_double)))
+        return out
+
+    def upload_all(self):
+        for w in (abi.ARRAY_ELEM, abi.ARRAY_RCACHE, abi.ARRAY_FACE, abi.ARRAY_BC_CACHE):
+            self.upload(w)
+
+    def download_all(self):
+        """Copy the device arena back into the host arena (in place)."""
+        for w in (abi.ARRAY_ELEM, abi.ARRAY_RCACHE, abi.ARRAY_FACE, abi.ARRAY_BC_CACHE):
+            self.download(w, self._array(w))
+
+    def synchronize(self):
+        abi.check(self.lib.hexed_gpu_synchronize(self.handle))
+
+    # -------------------------------------------------------------- kernel layer
+    def compute_euler(self, dt, i_stage, compute_residual=False, use_filter=False):
+        abi.check(self.lib.hexed_gpu_compute_euler(self.handle, dt, i_stage, int(compute_residual), int(use_filter)))
+
+    def compute_navier_stokes(self, dt, i_stage, visc, cond, compute_residual=False, use_filter=False):
+        abi.check(self.lib.hexed_gpu_compute_navier_stokes(self.handle, dt, i_stage, int(compute_residual),
+                                                           int(use_filter), ctypes.byref(visc), ctypes.byref(cond)))
+
+    def max_dt(self, msc, msd, local_time=False, viscous=False, visc=None, cond=None, use_filter=False):
+        visc = visc or abi.transport_inviscid()
+        cond = cond or abi.transport_inviscid()
+        out = ctypes.c_double()
+        abi.check(self.lib.hexed_gpu_max_dt(self.handle, msc, msd, int(local_time), int(use_filter), int(viscous),
+                                            ctypes.byref(visc), ctypes.byref(cond), ctypes.byref(out)))
+        return out.value
+
+    def prolong(self, scale=False, offset=False):
+        abi.check(self.lib.hexed_gpu_compute_prolong(self.handle, int(scale), int(offset)))
+
+    def restrict(self, scale=True, offset=False):
+        abi.check(self.lib.hexed_gpu_compute_restrict(self.handle, int(scale), int(offset)))
+
+    def write_face(self):
+        abi.check(self.lib.hexed_gpu_compute_write_face(self.handle))
+
+    def apply_state_bcs(self):
+        abi.check(self.lib.hexed_gpu_apply_state_bcs(self.handle))
+
+    def apply_flux_bcs(self):
+        abi.check(self.lib.hexed_gpu_apply_flux_bcs(self.handle))
+
+    # -------------------------------------------------------------- solver layer
+    def update(self, params, read_dt=True):
+        out = ctypes.c_double()
+        abi.check(self.lib.hexed_gpu_update(self.handle, ctypes.byref(params),
+                                            ctypes.byref(out) if read_dt else None))
+        return out.value if read_dt else None
+
+    def compute_residual(self, params):
+        abi.check(self.lib.hexed_gpu_compute_residual(self.handle, ctypes.byref(params)))
+
+    def residual_norm(self):
+        out = (ctypes.c_double * 3)()
+        abi.check(self.lib.hexed_gpu_residual_norm(self.handle, out))
+        return list(out)
+
+    # -------------------------------------------------------------- instrumentation
+    @property
+    def stream_ptr(self):
+        """cudaStream_t (as int) the context's kernels run on."""
+        return self.lib.hexed_gpu_stream(self.handle)
+
+    def profile_enable(self, enable=True):
+        abi.check(self.lib.hexed_gpu_profile_enable(self.handle, int(enable)))
+
+    def profile_read(self):
+        """{kernel name: (launches, total device ms)} since profile_enable."""
+        buf = (abi.KernelTime * 64)()
+        n = ctypes.c_int()
+        abi.check(self.lib.hexed_gpu_profile_read(self.handle, buf, 64, ctypes.byref(n)))
+        return {buf[i].name.decode(): (buf[i].launches, buf[i].total_ms) for i in range(n.value)}
+
+
+class Solver:
+    """Solver-shaped driver (src/Solver.cpp:834-913) on one GPU context."""
+
+    def __init__(self, arena, params=None, precision=abi.FP64):
+        self.arena = arena
+        self.params = params or abi.update_params()
+        self.ctx = Context(arena, precision)
+        self.iteration = 0
+        self.flow_time = 0.
+        self.init_residual = None
+
+    def initialize(self):
+        """Solver::initialize after the state has been sampled (src/Solver.cpp:398-407):
+        extrapolate to the faces and prolong to hanging-face mortars."""
+        self.ctx.write_face()
+        self.ctx.prolong()
+
+    def update(self):
+        dt = self.ctx.update(self.params)
+        self.iteration += 1
+        self.flow_time += dt * self.params.flow_iters * self.params.n_cheby_flow
+        return dt
+
+    def max_dt(self):
+        p = self.params
+        from .solver import chebyshev_step  # noqa: F401  (documented helper)
+        return self.ctx.max_dt(p.max_safety / chebyshev_step(p.n_cheby_flow, p.n_cheby_flow - 1), p.max_safety,
+                               p.local_time, p.use_ldg, p.visc, p.cond)
+
+    def compute_residuals(self):
+        """Case.hil compute_residuals: residual norms (momentum, density, energy)."""
+        self.ctx.compute_residual(self.params)
+        return self.ctx.residual_norm()
+
+    def normalized_residual(self):
+        """Mean of the three residual ratios to the first iteration's (include/Case.hil:23)."""
+        r = self.compute_residuals()
+        if self.init_residual is None:
+            self.init_residual = r
+        return sum(a / b for a, b in zip(r, self.init_residual)) / 3.
+
+    def state(self):
+        return self.ctx.download(abi.ARRAY_ELEM)[:, :self.arena.nv]
+
+    def close(self):
+        self.ctx.close()
+
+
+def fp64_peak_tflops():
+    """Measured FP64 FMA throughput of the current device (TFLOP/s)."""
+    lib = abi.load_library()
+    out = ctypes.c_double()
+    abi.check(lib.hexed_gpu_fp64_peak(ctypes.byref(out)))
+    return out.value
+
+
+def chebyshev_step(n_steps, i_step):
+    """math::chebyshev_step (src/math.cpp:104-107)."""
+    import math
+    return 1 / (1 - math.cos((n_steps - i_step - 0.5) * math.pi / n_steps))

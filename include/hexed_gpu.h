@@ -1,0 +1,245 @@
+/* hexed_gpu.h -- C ABI of the GB300 (sm_103a) DG spatial-operator / stage-update library.
+ *
+ * The library replaces the OpenMP kernel layer of hexed (ARTLab-GT/hexed): the free
+ * functions of include/kernels.hpp:22-42 and the Solver stage loop of
+ * src/Solver.cpp:56-133,834-913 that calls them. A caller hands over one flat
+ * "mesh arena" (plain host pointers and sizes, described below) that mirrors the
+ * storage the reference's Kernel_element / Kernel_connection / Refined_face views
+ * point into (include/Kernel_element.hpp:14-45, include/Kernel_connection.hpp:55-102,
+ * include/Refined_face.hpp:9-15); the library keeps a device copy and runs every
+ * kernel on it. All entry points return 0 on success or a negative hexed_status;
+ * hexed_gpu_last_error() gives the message of the last failure in the calling thread.
+ *
+ * Sizes: nd = n_dim (2 or 3), rs = row_size (2..8), nq = rs^nd, nfq = rs^(nd-1),
+ * nv = nd + 2 (momentum[nd], density, total energy; include/pde.hpp:48-50),
+ * nvert = 2^nd.
+ *
+ * Arena layout (all double, C order, outermost index first):
+ *   elem      [n_elem][nv + 3][nq]  rows 0..nv-1 conserved state, row nv time-step scale,
+ *                                   row nv+1 bulk AV coefficient, row nv+2 Laplacian AV
+ *                                   coefficient (src/Element.cpp:119-142, include/pde.hpp:17-21)
+ *   rcache    [n_elem][nv][nq]      residual cache (Kernel_element::residual_cache)
+ *   face      [n_slot][2][nv][nfq]  face traces; [0] extrapolated state / numerical flux,
+ *                                   [1] LDG storage (include/connection.hpp:52-67).
+ *                                   Slot e*2nd + i_face is face i_face of element e; slots
+ *                                   beyond n_elem*2nd are boundary ghost faces and the fine
+ *                                   mortar faces of hanging-node connections.
+ *   nom_size  [n_elem]              nominal element edge length
+ *   vert_tss  [n_elem][nvert]       vertex time-step scale, already min-shared over vertices
+ *   jac       [n_def][nd*nd + 1][nq] reference-level normals [i][j][nq] then Jacobian
+ *                                   determinant [nq] (src/Deformed_element.cpp:60-116)
+ *   face_nrml [n_def][2nd][nd][nfq] area-weighted face normal each deformed element sees on
+ *                                   each face (identity where the reference passes null)
+ * Elements are ordered Cartesian first (0..n_car_elem-1), then deformed.
+ *
+ * Connection lists (int32):
+ *   car_con  [n_car_con][3]   slot0, slot1, i_dim  (direction {{d,d},{1,0}}: slot0 is the
+ *                             + face of its element, slot1 the - face)
+ *   def_con  [n_def_con][3]   slot0, slot1, packed direction:
+ *                             i_dim0 | i_dim1 << 2 | face_sign0 << 4 | face_sign1 << 5
+ *   def_con_nrml [n_def_con][nd][nfq]  shared face normal in face-0 order (con.normal())
+ *   bc_con   [n_bc_con][4]    inside slot, ghost slot, i_dim | inside_face_sign << 2,
+ *                             index into bc_spec
+ *   bc_nrml  [n_bc_con][nd][nfq]  surface normal of the boundary face (not flipped)
+ *   bc_cache [n_bc_con][2][nv][nfq] state cache, flux cache (include/connection.hpp:342-377)
+ *   ref_face [n_ref_face][7]  coarse slot, fine mortar slots[4] (-1 = unused), stretch0,
+ *                             stretch1 (include/Refined_face.hpp:9-15)
+ */
+#ifndef HEXED_GPU_H_
+#define HEXED_GPU_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+enum hexed_status {
+  HEXED_OK = 0,
+  HEXED_ERR_INVALID = -1,     /* bad argument, e.g. invalid (n_dim, row_size) -- the
+                                 reference throws "demand for invalid kernel"
+                                 (include/kernel_factory.hpp:111-119) */
+  HEXED_ERR_CUDA = -2,        /* CUDA runtime failure */
+  HEXED_ERR_NUMERICAL = -3,   /* device kernels flagged a non-finite or non-admissible state */
+  HEXED_ERR_NO_DEVICE = -4,   /* no CUDA device visible */
+  HEXED_ERR_ALLOC = -5,       /* device memory exhausted */
+  HEXED_ERR_PRECONDITION = -6 /* a HEXED_ASSERT of the reference would fire, e.g. two-stage
+                                 stabilization requested for diffusion (include/Spatial.hpp:322) */
+};
+
+/* Boundary-condition kinds (include/Boundary_condition.hpp, src/Boundary_condition.cpp). */
+enum hexed_bc_kind {
+  HEXED_BC_FREESTREAM = 0,        /* src/Boundary_condition.cpp:62-76, 299 */
+  HEXED_BC_RIEMANN_INVARIANTS = 1,/* src/Boundary_condition.cpp:78-182 */
+  HEXED_BC_NONPENETRATION = 2,    /* src/Boundary_condition.cpp:302-344 */
+  HEXED_BC_COPY = 3,              /* src/Boundary_condition.cpp:450-458 */
+  HEXED_BC_OUTFLOW = 4,           /* src/Boundary_condition.cpp:465-477 */
+  HEXED_BC_PRESSURE_OUTFLOW = 5,  /* src/Boundary_condition.cpp:184-223 */
+  HEXED_BC_NO_SLIP = 6            /* src/Boundary_condition.cpp:371-427 */
+};
+
+/* Thermal sub-model of the no-slip wall (include/Boundary_condition.hpp:140-190). */
+enum hexed_thermal_kind {
+  HEXED_THERMAL_HEAT_FLUX = 0,    /* Prescribed_heat_flux (default: adiabatic, 0) */
+  HEXED_THERMAL_ENERGY = 1,       /* Prescribed_energy (isothermal) */
+  HEXED_THERMAL_EQUILIBRIUM = 2   /* Thermal_equilibrium */
+};
+
+typedef struct hexed_bc_spec {
+  int kind;                /* hexed_bc_kind */
+  int thermal_kind;        /* hexed_thermal_kind, no-slip only */
+  double freestream[5];    /* conserved freestream state (first nv entries used) */
+  double pressure;         /* Pressure_outflow: prescribed pressure */
+  double coercion;         /* No_slip heat-flux coercion (reference default 2) */
+  double thermal_value;    /* heat flux (HEAT_FLUX) or energy per mass (ENERGY) */
+  double emissivity, heat_transfer_coef, temperature; /* Thermal_equilibrium */
+} hexed_bc_spec;
+
+/* Transport model: coefficient(sqrt T) = const_val + ref_val (sqrtT/sqrt(ref_temp))^3
+ * (ref_temp + temp_offset)/(T + temp_offset) (include/Transport_model.hpp:21-44). */
+typedef struct hexed_transport {
+  double const_val, ref_val, ref_temp, temp_offset;
+  int is_viscous;
+} hexed_transport;
+
+typedef struct hexed_mesh_desc {
+  int n_dim, row_size;
+  int n_car_elem, n_def_elem;
+  int n_slot;
+  int n_car_con, n_def_con, n_bc_con, n_ref_face, n_bc_spec;
+  double* elem;
+  double* rcache;
+  double* face;
+  const double* nom_size;
+  const double* vert_tss;
+  const double* jac;
+  const double* face_nrml;
+  const int* car_con;
+  const int* def_con;
+  const double* def_con_nrml;
+  const int* bc_con;
+  const double* bc_nrml;
+  double* bc_cache;
+  const int* ref_face;
+  const hexed_bc_spec* bc_spec;
+} hexed_mesh_desc;
+
+/* Arrays that can be copied in and out of the device arena. */
+enum hexed_array {
+  HEXED_ARRAY_ELEM = 0,
+  HEXED_ARRAY_RCACHE = 1,
+  HEXED_ARRAY_FACE = 2,
+  HEXED_ARRAY_BC_CACHE = 3
+};
+
+/* Arithmetic of the volume and face kernels. */
+enum hexed_precision {
+  HEXED_FP64 = 0,   /* everything in double: the parity path */
+  HEXED_MIXED = 1   /* fluxes, derivatives and face traces in float; state, stage update,
+                       metrics, time step and residual norms in double */
+};
+
+/* Parameters of one Solver::update (src/Solver.cpp:834-886, defaults set at 151-174). */
+typedef struct hexed_update_params {
+  double max_safety;     /* "max_safety" (CFL fraction of the basis limit) */
+  double max_time_step;  /* "max_time_step" */
+  int n_cheby_flow;      /* Chebyshev sub-steps */
+  int flow_iters;        /* repetitions per update */
+  int local_time;        /* local time stepping */
+  int use_filter;        /* modal filter */
+  int use_ldg;           /* viscous / artificial-viscosity path (Solver::use_ldg) */
+  hexed_transport visc, cond;
+} hexed_update_params;
+
+typedef struct hexed_gpu_ctx hexed_gpu_ctx;
+
+/* Thread-local message of the last failing call. */
+const char* hexed_gpu_last_error(void);
+
+/* Library build information: "sm_103a" plus the maximum row size. */
+const char* hexed_gpu_version(void);
+
+/* Creates a context on the current CUDA device and uploads the whole arena.
+ * Replaces the setup the reference performs once per mesh (Solver::calc_jacobian +
+ * initialize, src/Solver.cpp:273-408) as far as the kernels see it. */
+int hexed_gpu_create(const hexed_mesh_desc* desc, int precision, hexed_gpu_ctx** out);
+int hexed_gpu_destroy(hexed_gpu_ctx* ctx);
+
+/* Host <-> device copies of one arena array (hexed_array); sizes follow the layout above. */
+int hexed_gpu_upload(hexed_gpu_ctx* ctx, int which, const double* host);
+int hexed_gpu_download(hexed_gpu_ctx* ctx, int which, double* host);
+int hexed_gpu_synchronize(hexed_gpu_ctx* ctx);
+
+/* --- kernel layer: one call per free function of include/kernels.hpp:22-42 --- */
+
+/* compute_euler (src/kernels_convective.cpp:8-19, 36): Neighbor (Cartesian, deformed and
+ * boundary connections), Restrict_refined, Local, Prolong_refined. */
+int hexed_gpu_compute_euler(hexed_gpu_ctx* ctx, double dt, int i_stage, int compute_residual,
+                            int use_filter);
+
+/* compute_navier_stokes (src/kernels_diffusive.cpp:8-32): the LDG chain. The flux
+ * boundary conditions (Solver::apply_flux_bcs, src/Solver.cpp:69-81) run on the device
+ * between Prolong and Neighbor_reconcile, so no host callback is needed. */
+int hexed_gpu_compute_navier_stokes(hexed_gpu_ctx* ctx, double dt, int i_stage,
+                                    int compute_residual, int use_filter,
+                                    const hexed_transport* visc, const hexed_transport* cond);
+
+/* max_dt_euler / max_dt_navier_stokes (src/kernels_max_dt.cpp:8-21): writes the local
+ * time-step scale (local_time) or returns the global step in *out_dt. */
+int hexed_gpu_max_dt(hexed_gpu_ctx* ctx, double convective_safety, double diffusive_safety,
+                     int local_time, int use_filter, int viscous, const hexed_transport* visc,
+                     const hexed_transport* cond, double* out_dt);
+
+/* compute_prolong / compute_restrict / compute_write_face (src/kernels_convective.cpp:21-44). */
+int hexed_gpu_compute_prolong(hexed_gpu_ctx* ctx, int scale, int offset);
+int hexed_gpu_compute_restrict(hexed_gpu_ctx* ctx, int scale, int offset);
+int hexed_gpu_compute_write_face(hexed_gpu_ctx* ctx);
+
+/* Solver::apply_state_bcs / apply_flux_bcs (src/Solver.cpp:56-81). */
+int hexed_gpu_apply_state_bcs(hexed_gpu_ctx* ctx);
+int hexed_gpu_apply_flux_bcs(hexed_gpu_ctx* ctx);
+
+/* --- solver layer --- */
+
+/* Solver::update (src/Solver.cpp:834-886): time step, state BCs and both stages, all
+ * enqueued without a host round trip (the time step stays on the device). *out_dt
+ * (may be NULL) receives the last step taken; reading it synchronizes. */
+int hexed_gpu_update(hexed_gpu_ctx* ctx, const hexed_update_params* params, double* out_dt);
+
+/* Solver::compute_residual (src/Solver.cpp:899-913). */
+int hexed_gpu_compute_residual(hexed_gpu_ctx* ctx, const hexed_update_params* params);
+
+/* Residual norms of Case.hil's compute_residuals (src/Solver.cpp:1113-1131,
+ * src/Qpoint_func.cpp:37-45): sqrt of the integral of (rcache/tss)^2 over the domain,
+ * summed over momentum components, density, energy -> out[3]. */
+int hexed_gpu_residual_norm(hexed_gpu_ctx* ctx, double out[3]);
+
+/* --- instrumentation --- */
+
+/* Per-kernel CUDA-event timing on the context's stream, the device counterpart of the
+ * reference's per-kernel stopwatch hooks (include/kernel_factory.hpp:32-45,
+ * src/Stopwatch_tree.cpp). enable != 0 starts recording (and clears earlier records). */
+int hexed_gpu_profile_enable(hexed_gpu_ctx* ctx, int enable);
+
+typedef struct hexed_kernel_time {
+  char name[48];
+  int launches;
+  double total_ms;
+} hexed_kernel_time;
+
+/* Waits for the recorded launches and reports launches and total device time per kernel
+ * (at most `capacity` entries; *n_out = number written). Clears the records. */
+int hexed_gpu_profile_read(hexed_gpu_ctx* ctx, hexed_kernel_time* out, int capacity, int* n_out);
+
+/* The cudaStream_t every kernel of the context runs on (for callers that time or order
+ * work against it). No counterpart in the reference, which has no device stream. */
+void* hexed_gpu_stream(hexed_gpu_ctx* ctx);
+
+/* Measures the FP64 FMA throughput of the current device with a dependent-chain DFMA
+ * kernel (TFLOP/s, 2 flops per FMA) -- the FP64 roofline denominator. No counterpart in
+ * the reference. */
+int hexed_gpu_fp64_peak(double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

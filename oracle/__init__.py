@@ -1,0 +1,120 @@
+"""TEST INFRASTRUCTURE: ctypes wrapper of the CPU oracle (oracle/hexed_oracle.cpp).
+
+Only the tests, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use this
+package; the product (hexed_gb300) never imports it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "hexed_oracle.cpp")
+LIB = os.path.join(HERE, "_build", "libhexed_oracle.so")
+
+_lib = None
+
+
+def build(force=False):
+    """g++ -O3 -fopenmp -ffp-contract=off (no FMA contraction: identical results on x86 and Arm)."""
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(
+            os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "..", "include", "hexed_gpu.h"))):
+        return LIB
+    cmd = ["g++", "-std=c++17", "-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+           "-o", LIB + ".tmp", SRC]
+    subprocess.run(cmd, check=True)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+def load():
+    global _lib
+    if _lib is None:
+        from hexed_gb300 import abi
+        build()
+        lib = ctypes.CDLL(LIB)
+        D = ctypes.POINTER(abi.MeshDesc)
+        T = ctypes.POINTER(abi.Transport)
+        U = ctypes.POINTER(abi.UpdateParams)
+        c_int, c_double = ctypes.c_int, ctypes.c_double
+        P = ctypes.POINTER(c_double)
+        sig = {
+            "oracle_write_face": [D],
+            "oracle_prolong": [D, c_int, c_int],
+            "oracle_restrict": [D, c_int, c_int],
+            "oracle_apply_state_bcs": [D],
+            "oracle_apply_flux_bcs": [D],
+            "oracle_neighbor": [D, c_int],
+            "oracle_compute_euler": [D, c_double, c_int, c_int, c_int],
+            "oracle_compute_navier_stokes": [D, c_double, c_int, c_int, c_int, T, T],
+            "oracle_max_dt": [D, c_double, c_double, c_int, c_int, T, T, P],
+            "oracle_residual_norm": [D, P],
+            "oracle_update": [D, U, P],
+            "oracle_compute_residual": [D, U],
+        }
+        for name, args in sig.items():
+            fn = getattr(lib, name)
+            fn.argtypes = args
+            fn.restype = c_int
+        _lib = lib
+    return _lib
+
+
+class Oracle:
+    """Runs the oracle in place on a hexed_gb300.mesh.Arena."""
+
+    def __init__(self, arena):
+        self.arena = arena
+        self.desc = arena.desc()
+        self.lib = load()
+
+    def _chk(self, st):
+        if st != 0:
+            raise RuntimeError(f"oracle call failed with status {st}")
+
+    def write_face(self):
+        self._chk(self.lib.oracle_write_face(ctypes.byref(self.desc)))
+
+    def prolong(self, scale=False, offset=False):
+        self._chk(self.lib.oracle_prolong(ctypes.byref(self.desc), int(scale), int(offset)))
+
+    def restrict(self, scale=True, offset=False):
+        self._chk(self.lib.oracle_restrict(ctypes.byref(self.desc), int(scale), int(offset)))
+
+    def apply_state_bcs(self):
+        self._chk(self.lib.oracle_apply_state_bcs(ctypes.byref(self.desc)))
+
+    def apply_flux_bcs(self):
+        self._chk(self.lib.oracle_apply_flux_bcs(ctypes.byref(self.desc)))
+
+    def compute_euler(self, dt, i_stage, compute_residual=False, use_filter=False):
+        self._chk(self.lib.oracle_compute_euler(ctypes.byref(self.desc), dt, i_stage, int(compute_residual),
+                                                int(use_filter)))
+
+    def compute_navier_stokes(self, dt, i_stage, visc, cond, compute_residual=False, use_filter=False):
+        self._chk(self.lib.oracle_compute_navier_stokes(ctypes.byref(self.desc), dt, i_stage, int(compute_residual),
+                                                        int(use_filter), ctypes.byref(visc), ctypes.byref(cond)))
+
+    def max_dt(self, msc, msd, local_time=False, viscous=False, visc=None, cond=None):
+        from hexed_gb300 import abi
+        visc = visc or abi.transport_inviscid()
+        cond = cond or abi.transport_inviscid()
+        out = ctypes.c_double()
+        self._chk(self.lib.oracle_max_dt(ctypes.byref(self.desc), msc, msd, int(local_time), int(viscous),
+                                         ctypes.byref(visc), ctypes.byref(cond), ctypes.byref(out)))
+        return out.value
+
+    def update(self, params):
+        out = ctypes.c_double()
+        self._chk(self.lib.oracle_update(ctypes.byref(self.desc), ctypes.byref(params), ctypes.byref(out)))
+        return out.value
+
+    def compute_residual(self, params):
+        self._chk(self.lib.oracle_compute_residual(ctypes.byref(self.desc), ctypes.byref(params)))
+
+    def residual_norm(self):
+        out = (ctypes.c_double * 3)()
+        self._chk(self.lib.oracle_residual_norm(ctypes.byref(self.desc), out))
+        return list(out)

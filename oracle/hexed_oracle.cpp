@@ -1,0 +1,1127 @@
+// hexed_oracle.cpp -- TEST INFRASTRUCTURE ONLY: the CPU oracle of the DG hot path.
+//
+// A plain C++ (no Eigen) restatement of hexed's OpenMP kernels, operating in place on
+// the flat mesh arena declared in include/hexed_gpu.h. It is the checker the parity
+// tests hold the CUDA library against and the CPU baseline the benchmark times; the
+// product (hexed_gb300/csrc) never includes or links it.
+//
+// Each function follows the reference operation by operation so that its rounding
+// matches the reference's own arithmetic; the file:line it restates is cited on it.
+// Deliberate differences, all at the roundoff level:
+//  * small matrix products and norms sum in ascending index order (Eigen may use
+//    SIMD partial sums);
+//  * the 3x3 characteristic system of the Riemann-invariant BC is solved by Gaussian
+//    elimination with partial pivoting instead of Eigen's column-pivoted QR (the
+//    solutions agree to roundoff whenever pressure > 0, i.e. the system is regular);
+//  * the build uses -ffp-contract=off so results do not depend on the host ISA.
+// Parity of this restatement with the reference is pinned by the reference's own
+// tests (analytic and property checks, restated under tests/) and by the basis
+// tables generated with the reference's generator (tests/golden/).
+#include <cmath>
+#include <cstring>
+#include <cstdint>
+#include <algorithm>
+#include <limits>
+#include <vector>
+#include "../include/hexed_gpu.h"
+#include "../hexed_gb300/csrc/basis_tables.h"
+
+namespace {
+
+constexpr double heat_rat = 1.4;                 // include/pde.hpp:51
+constexpr double specific_gas_air = 287.05287;   // include/constants.hpp:44
+
+constexpr int ipow(int b, int e) { int r = 1; for (int i = 0; i < e; ++i) r *= b; return r; }
+
+struct Tables {
+  const double* node; const double* weight; const double* diff; const double* bound;
+  const double* filter; const double* prolong; const double* restrict_; const double* ortho;
+  double max_cfl, min_eig_diffusion, step_ratio;
+};
+
+Tables tables(int rs)
+{
+  using namespace hexed_tables;
+  switch (rs) {
+#define HEXED_T(n) case n: return {node##n, weight##n, diff_mat##n, boundary##n, filter##n, prolong##n, restrict_##n, orthogonal##n, max_cfl##n, min_eig_diffusion##n, step_ratio};
+    HEXED_T(2) HEXED_T(3) HEXED_T(4) HEXED_T(5) HEXED_T(6) HEXED_T(7) HEXED_T(8)
+#undef HEXED_T
+  }
+  return {};
+}
+
+// Transport_model::coefficient (include/Transport_model.hpp:35-38)
+inline double transport_coef(const hexed_transport& t, double sqrt_temp)
+{
+  double r = sqrt_temp/std::sqrt(t.ref_temp);
+  double p3 = 1.; p3 *= r; p3 *= r; p3 *= r;   // math::pow(x, 3), include/math.hpp:30-36
+  return t.const_val + t.ref_val*p3*(t.ref_temp + t.temp_offset)/(sqrt_temp*sqrt_temp + t.temp_offset);
+}
+
+template <int ND, int RS>
+struct K
+{
+  static constexpr int nq = ipow(RS, ND);
+  static constexpr int nfq = nq/RS;
+  static constexpr int nv = ND + 2;
+  static constexpr int nvert = 1 << ND;
+  static constexpr int n_slot_dof = 2*nv*nfq;
+
+  const hexed_mesh_desc& m;
+  Tables t;
+  double lift[RS][2];   // Derivative::lift (include/Derivative.hpp:22-28)
+  explicit K(const hexed_mesh_desc& mesh) : m{mesh}, t{tables(RS)}
+  {
+    for (int i = 0; i < RS; ++i) {
+      double inv_w = 1./t.weight[i];
+      lift[i][0] = -(inv_w*t.bound[0*RS + i]);
+      lift[i][1] = inv_w*t.bound[1*RS + i];
+    }
+  }
+
+  int n_elem() const { return m.n_car_elem + m.n_def_elem; }
+  double* elem(int e) const { return m.elem + (size_t)e*(nv + 3)*nq; }
+  double* rcache(int e) const { return m.rcache + (size_t)e*nv*nq; }
+  double* slot(int s, bool ldg) const { return m.face + (size_t)s*n_slot_dof + ldg*nv*nfq; }
+  double* face(int e, int i_face, bool ldg) const { return slot(e*2*ND + i_face, ldg); }
+
+  // Row_index (include/Row_index.hpp:14-64)
+  static int row_stride(int i_dim) { return ipow(RS, ND - 1 - i_dim); }
+  static int row_qpoint(int i_dim, int i_fq, int i_node)
+  {
+    int stride = row_stride(i_dim);
+    return (i_fq/stride)*stride*RS + i_fq%stride + i_node*stride;
+  }
+
+  // Derivative::operator() (include/Derivative.hpp:50-55): diff*f + lift*(fb - B*f)
+  void derivative(const double* f, const double* fb, double* out) const
+  {
+    double bf[2];
+    for (int s = 0; s < 2; ++s) {
+      double acc = 0.;
+      for (int j = 0; j < RS; ++j) acc += t.bound[s*RS + j]*f[j];
+      bf[s] = fb[s] - acc;
+    }
+    for (int i = 0; i < RS; ++i) {
+      double d = 0.;
+      for (int j = 0; j < RS; ++j) d += t.diff[i*RS + j]*f[j];
+      double l = 0.;
+      l += lift[i][0]*bf[0];
+      l += lift[i][1]*bf[1];
+      out[i] = d + l;
+    }
+  }
+  void derivative_interior(const double* f, double* out) const // Derivative.hpp:56-60
+  {
+    for (int i = 0; i < RS; ++i) {
+      double d = 0.;
+      for (int j = 0; j < RS; ++j) d += t.diff[i*RS + j]*f[j];
+      out[i] = d;
+    }
+  }
+
+  // Spatial::Write_face::operator() (include/Spatial.hpp:41-57)
+  void write_face_elem(const double* state, double* const* faces) const
+  {
+    for (int d = 0; d < ND; ++d) {
+      for (int i_fq = 0; i_fq < nfq; ++i_fq) {
+        for (int v = 0; v < nv; ++v) {
+          for (int s = 0; s < 2; ++s) {
+            double acc = 0.;
+            for (int i = 0; i < RS; ++i) acc += t.bound[s*RS + i]*state[v*nq + row_qpoint(d, i_fq, i)];
+            faces[2*d + s][v*nfq + i_fq] = acc;
+          }
+        }
+      }
+    }
+  }
+
+  void write_face() const // Write_face over all elements (Spatial.hpp:60-70)
+  {
+    #pragma omp parallel for
+    for (int e = 0; e < n_elem(); ++e) {
+      double* faces[6];
+      for (int i = 0; i < 2*ND; ++i) faces[i] = face(e, i, false);
+      write_face_elem(elem(e), faces);
+    }
+  }
+
+  // ---------------------------------------------------------------- PDE pieces
+  // Navier_stokes::Pde::Computation::compute_scalars_conv (include/pde.hpp:97-104)
+  struct Conv { double mass, kin_ener, pressure; };
+  static Conv scalars_conv(const double* s)
+  {
+    Conv c;
+    c.mass = s[ND];
+    c.kin_ener = 0;
+    for (int d = 0; d < ND; ++d) c.kin_ener += s[d]*s[d];
+    c.kin_ener *= .5/c.mass;
+    c.pressure = (heat_rat - 1.)*(s[ND + 1] - c.kin_ener);
+    return c;
+  }
+  // compute_flux_conv for one flux direction given by column `n` (pde.hpp:108-122)
+  static void flux_conv(const double* s, const Conv& c, const double* n, double* f)
+  {
+    f[ND] = 0;
+    for (int j = 0; j < ND; ++j) f[ND] += s[j]*n[j];
+    double vol_flux = f[ND]/c.mass;
+    f[ND + 1] = (s[ND + 1] + c.pressure)*vol_flux;
+    for (int j = 0; j < ND; ++j) f[j] = s[j]*vol_flux + c.pressure*n[j];
+  }
+  // compute_char_speed (pde.hpp:161-166)
+  static double char_speed(const double* s)
+  {
+    double sound_speed = std::sqrt(heat_rat*(heat_rat - 1)*s[ND + 1]/s[ND]);
+    double sq = 0.;
+    for (int d = 0; d < ND; ++d) sq += s[d]*s[d];
+    return sound_speed + std::sqrt(sq)/s[ND];
+  }
+  struct Diff { double bulk_av, laplacian_av, sqrt_temp, mu, k, energy_cond; };
+  // compute_scalars_diff (pde.hpp:130-138); s has nv + 2 entries (bulk, Laplacian AV)
+  static Diff scalars_diff(const double* s, const Conv& c, const hexed_transport& visc, const hexed_transport& cond)
+  {
+    Diff d;
+    d.bulk_av = std::abs(s[ND + 2]);
+    d.laplacian_av = std::abs(s[ND + 3]);
+    d.sqrt_temp = std::sqrt(std::max((s[ND + 1] - c.kin_ener)/c.mass, 0.)*(heat_rat - 1)/specific_gas_air);
+    d.mu = transport_coef(visc, d.sqrt_temp);
+    d.k = transport_coef(cond, d.sqrt_temp);
+    d.energy_cond = d.k*(heat_rat - 1)/specific_gas_air;
+    return d;
+  }
+  // compute_flux_diff (pde.hpp:142-158). g[nv][ND] gradient, nrm[ND][ND] (row = physical
+  // dim, column = reference dim), out fd[nv][ND].
+  static void flux_diff(const double* s, const Conv& c, const Diff& df, const double (*g)[ND],
+                        const double (*nrm)[ND], bool identity, double (*out)[ND])
+  {
+    double mass = c.mass;
+    double veloc[ND];
+    for (int i = 0; i < ND; ++i) veloc[i] = s[i]/mass;
+    double vg[ND][ND];
+    for (int i = 0; i < ND; ++i) for (int j = 0; j < ND; ++j) vg[i][j] = (g[i][j] - veloc[i]*g[ND][j])/mass;
+    double trace = 0.;
+    for (int i = 0; i < ND; ++i) trace += vg[i][i];
+    double bulk_term = (df.bulk_av*mass - 2./3.*df.mu)*trace;
+    double stress[ND][ND];
+    for (int i = 0; i < ND; ++i) for (int j = 0; j < ND; ++j)
+      stress[i][j] = df.mu*(vg[i][j] + vg[j][i]) + bulk_term*(i == j ? 1. : 0.);
+    double fd[ND + 2][ND];
+    for (int v = 0; v < ND + 2; ++v) for (int j = 0; j < ND; ++j) fd[v][j] = -df.laplacian_av*g[v][j];
+    for (int i = 0; i < ND; ++i) for (int j = 0; j < ND; ++j) fd[i][j] -= stress[i][j];
+    double coef = -s[ND + 1]/mass/mass;
+    for (int j = 0; j < ND; ++j) {
+      double vvg = 0.;
+      for (int i = 0; i < ND; ++i) vvg += veloc[i]*vg[i][j];
+      double ieg = coef*g[ND][j] + g[ND + 1][j]/mass - vvg;
+      double vs = 0.;
+      for (int i = 0; i < ND; ++i) vs += veloc[i]*stress[i][j];
+      fd[ND + 1][j] -= vs + df.energy_cond*ieg;
+    }
+    for (int v = 0; v < ND + 2; ++v) {
+      for (int i = 0; i < ND; ++i) {
+        if (identity) { out[v][i] = fd[v][i]; continue; }
+        double acc = 0.;
+        for (int j = 0; j < ND; ++j) acc += fd[v][j]*nrm[j][i];
+        out[v][i] = acc;
+      }
+    }
+  }
+
+  // ---------------------------------------------------------------- Face_permutation
+  // Index in face-1 storage of the value that lands at face-0 qpoint q after
+  // Face_permutation::match_faces (transpose then flip; include/Spatial.hpp:85-129).
+  static int perm_index(int dir_packed, int q)
+  {
+    int i_dim0 = dir_packed & 3, i_dim1 = (dir_packed >> 2) & 3;
+    bool s0 = (dir_packed >> 4) & 1, s1 = (dir_packed >> 5) & 1;
+    bool flip_n0 = (s0 == 0), flip_n1 = (s1 == 1);           // Connection_direction::flip_normal
+    bool flip_tan = (i_dim0 != i_dim1) && (flip_n0 == flip_n1);
+    bool transpose = ((i_dim0 == 0) && (i_dim1 == 2)) || ((i_dim0 == 2) && (i_dim1 == 0));
+    if (ND == 3) {
+      // column-major rs x rs map: (r, c) at r + c*rs
+      int r = q%RS, c = q/RS;
+      if (flip_tan) {
+        bool colwise = (i_dim0 > 3 - i_dim0 - i_dim1) != transpose;
+        if (colwise) r = RS - 1 - r; else c = RS - 1 - c;
+      }
+      int idx = r + c*RS;
+      if (transpose) idx = (idx%RS)*RS + idx/RS;
+      return idx;
+    } else if (ND == 2) {
+      return flip_tan ? RS - 1 - q : q;
+    }
+    return q;
+  }
+
+  // ---------------------------------------------------------------- Neighbor
+  // Spatial::Neighbor::operator() (include/Spatial.hpp:613-705) for one connection.
+  // `nrml` is null for Cartesian connections (normal = unit vector along i_dim0).
+  void neighbor_con(int slot0, int slot1, int dir, const double* nrml, bool viscous) const
+  {
+    int i_dim0 = dir & 3;
+    int sign[2] = {1, 1};
+    bool deformed = nrml != nullptr;
+    if (deformed) {
+      bool s0 = (dir >> 4) & 1, s1 = (dir >> 5) & 1;
+      sign[0] = 1 - 2*(s0 == 0);
+      sign[1] = 1 - 2*(s1 == 1);
+    }
+    double* f0 = slot(slot0, false);
+    double* f1 = slot(slot1, false);
+    double* l0 = slot(slot0, true);
+    double* l1 = slot(slot1, true);
+    double out0[nv*nfq], out1[nv*nfq];
+    double avg0[nv*nfq], avg1[nv*nfq];
+    for (int q = 0; q < nfq; ++q) {
+      int q1 = deformed ? perm_index(dir, q) : q;
+      double u[2][nv + 2];
+      for (int v = 0; v < nv; ++v) { u[0][v] = f0[v*nfq + q]; u[1][v] = f1[v*nfq + q1]; }
+      if (viscous) {
+        for (int v = 0; v < nv; ++v) {
+          double avg = .5*(u[0][v] + u[1][v]);
+          avg0[v*nfq + q] = avg;
+          avg1[v*nfq + q1] = avg;
+        }
+      }
+      double n[ND];
+      if (deformed) for (int d = 0; d < ND; ++d) n[d] = sign[0]*nrml[d*nfq + q];
+      else for (int d = 0; d < ND; ++d) n[d] = (d == i_dim0) ? 1. : 0.;
+      double fl[2][nv], cs[2];
+      for (int side = 0; side < 2; ++side) {
+        Conv c = scalars_conv(u[side]);
+        flux_conv(u[side], c, n, fl[side]);
+        cs[side] = char_speed(u[side]);
+      }
+      double nn = 0.;
+      for (int d = 0; d < ND; ++d) nn += n[d]*n[d];
+      double mult = std::max(cs[0], cs[1])*std::sqrt(nn);
+      for (int v = 0; v < nv; ++v) {
+        double flux = .5*(fl[0][v] + fl[1][v] + mult*(u[0][v] - u[1][v]));
+        out0[v*nfq + q] = sign[0]*flux;
+        out1[v*nfq + q1] = sign[1]*flux;
+      }
+    }
+    std::memcpy(f0, out0, sizeof(out0));
+    std::memcpy(f1, out1, sizeof(out1));
+    if (viscous) {
+      std::memcpy(l0, avg0, sizeof(avg0));
+      std::memcpy(l1, avg1, sizeof(avg1));
+    }
+  }
+
+  void neighbor(bool viscous) const
+  {
+    #pragma omp parallel for
+    for (int i = 0; i < m.n_car_con; ++i) {
+      const int* c = m.car_con + 3*i;
+      neighbor_con(c[0], c[1], c[2] | (c[2] << 2) | (1 << 4), nullptr, viscous);
+    }
+    #pragma omp parallel for
+    for (int i = 0; i < m.n_def_con; ++i) {
+      const int* c = m.def_con + 3*i;
+      neighbor_con(c[0], c[1], c[2], m.def_con_nrml + (size_t)i*ND*nfq, viscous);
+    }
+    // boundary connections are deformed connections with direction {{d,d},{ifs,!ifs}}
+    // (include/connection.hpp:378, src/Accessible_mesh.cpp:136-146)
+    #pragma omp parallel for
+    for (int i = 0; i < m.n_bc_con; ++i) {
+      const int* c = m.bc_con + 4*i;
+      int d = c[2] & 3, ifs = (c[2] >> 2) & 1;
+      int dir = d | (d << 2) | (ifs << 4) | ((!ifs) << 5);
+      neighbor_con(c[0], c[1], dir, m.bc_nrml + (size_t)i*ND*nfq, viscous);
+    }
+  }
+
+  // Spatial::Neighbor_reconcile (include/Spatial.hpp:716-759) for one connection
+  void reconcile_con(int slot0, int slot1, int dir, bool deformed) const
+  {
+    int sign[2] = {1, 1};
+    if (deformed) {
+      bool s0 = (dir >> 4) & 1, s1 = (dir >> 5) & 1;
+      sign[0] = 1 - 2*(s0 == 0);
+      sign[1] = 1 - 2*(s1 == 1);
+    }
+    double* l0 = slot(slot0, true);
+    double* l1 = slot(slot1, true);
+    double out0[nv*nfq], out1[nv*nfq];
+    for (int q = 0; q < nfq; ++q) {
+      int q1 = deformed ? perm_index(dir, q) : q;
+      for (int v = 0; v < nv; ++v) {
+        double a = l0[v*nfq + q], b = l1[v*nfq + q1];
+        double avg = 0;
+        avg += .5*sign[0]*a;
+        avg += .5*sign[1]*b;
+        out0[v*nfq + q] = sign[0]*avg - a;
+        out1[v*nfq + q1] = sign[1]*avg - b;
+      }
+    }
+    std::memcpy(l0, out0, sizeof(out0));
+    std::memcpy(l1, out1, sizeof(out1));
+  }
+
+  void neighbor_reconcile() const
+  {
+    #pragma omp parallel for
+    for (int i = 0; i < m.n_car_con; ++i) {
+      const int* c = m.car_con + 3*i;
+      reconcile_con(c[0], c[1], 0, false);
+    }
+    #pragma omp parallel for
+    for (int i = 0; i < m.n_def_con; ++i) {
+      const int* c = m.def_con + 3*i;
+      reconcile_con(c[0], c[1], c[2], true);
+    }
+    #pragma omp parallel for
+    for (int i = 0; i < m.n_bc_con; ++i) {
+      const int* c = m.bc_con + 4*i;
+      int d = c[2] & 3, ifs = (c[2] >> 2) & 1;
+      reconcile_con(c[0], c[1], d | (d << 2) | (ifs << 4) | ((!ifs) << 5), true);
+    }
+  }
+
+  // ---------------------------------------------------------------- Local
+  // Spatial::Local::operator() (include/Spatial.hpp:326-509) for one element.
+  void local_elem(int e, bool deformed, bool viscous, double update_coef, int stage,
+                  bool compute_residual, bool use_filter,
+                  const hexed_transport& visc, const hexed_transport& cond) const
+  {
+    double* state = elem(e);
+    double* tss = state + nv*nq;
+    double d_pos = m.nom_size[e];
+    double* faces[6];
+    double* visc_faces[6];
+    for (int i = 0; i < 2*ND; ++i) { faces[i] = face(e, i, false); visc_faces[i] = face(e, i, true); }
+    const double* nrml = nullptr;
+    const double* det = nullptr;
+    const double* face_nrml[6] = {};
+    if (deformed) {
+      int ed = e - m.n_car_elem;
+      nrml = m.jac + (size_t)ed*(ND*ND + 1)*nq;
+      det = nrml + ND*ND*nq;
+      for (int i = 0; i < 2*ND; ++i) face_nrml[i] = m.face_nrml + ((size_t)ed*2*ND + i)*ND*nfq;
+    }
+    static thread_local std::vector<double> buf;
+    buf.assign((size_t)(2*nv*nq + ND*nv*nq + ND*nv*nq), 0.);
+    double (*time_rate)[nv][nq] = reinterpret_cast<double (*)[nv][nq]>(buf.data());
+    double (*visc_storage)[nv][nq] = reinterpret_cast<double (*)[nv][nq]>(buf.data() + 2*nv*nq);
+    double (*flux)[nv][nq] = reinterpret_cast<double (*)[nv][nq]>(buf.data() + 2*nv*nq + ND*nv*nq);
+
+    if (viscous) {
+      // gradient times Jacobian determinant (Spatial.hpp:371-402)
+      for (int v = 0; v < nv; ++v) for (int q = 0; q < nq; ++q) time_rate[0][v][q] = state[v*nq + q];
+      for (int d = 0; d < ND; ++d) {
+        for (int i_fq = 0; i_fq < nfq; ++i_fq) {
+          double row_r[nv][RS], fs[nv][2];
+          for (int v = 0; v < nv; ++v) {
+            for (int i = 0; i < RS; ++i) row_r[v][i] = time_rate[0][v][row_qpoint(d, i_fq, i)];
+            for (int s = 0; s < 2; ++s) fs[v][s] = visc_faces[2*d + s][v*nfq + i_fq];
+          }
+          if (deformed) {
+            for (int j = 0; j < ND; ++j) {
+              double row_n[RS], face_n[2];
+              for (int i = 0; i < RS; ++i) row_n[i] = nrml[(d*ND + j)*nq + row_qpoint(d, i_fq, i)];
+              for (int s = 0; s < 2; ++s) face_n[s] = face_nrml[2*d + s][j*nfq + i_fq];
+              for (int v = 0; v < nv; ++v) {
+                double row[RS], bound[2], der[RS];
+                for (int i = 0; i < RS; ++i) row[i] = row_n[i]*row_r[v][i];
+                for (int s = 0; s < 2; ++s) bound[s] = face_n[s]*fs[v][s];
+                derivative(row, bound, der);
+                for (int i = 0; i < RS; ++i) {
+                  double& x = visc_storage[j][v][row_qpoint(d, i_fq, i)];
+                  x = 1.*x + der[i]/d_pos;
+                }
+              }
+            }
+          } else {
+            for (int v = 0; v < nv; ++v) {
+              double der[RS];
+              derivative(row_r[v], fs[v], der);
+              for (int i = 0; i < RS; ++i) {
+                double& x = visc_storage[d][v][row_qpoint(d, i_fq, i)];
+                x = 0*x + der[i]/d_pos;
+              }
+            }
+          }
+        }
+      }
+      for (int v = 0; v < nv; ++v) for (int q = 0; q < nq; ++q) { time_rate[0][v][q] = 0; time_rate[1][v][q] = 0; }
+    }
+
+    // flux (Spatial.hpp:405-442)
+    for (int q = 0; q < nq; ++q) {
+      double s[nv + 2];
+      for (int v = 0; v < nv; ++v) s[v] = state[v*nq + q];
+      s[nv] = state[(nv + 1)*nq + q];
+      s[nv + 1] = state[(nv + 2)*nq + q];
+      double nmat[ND][ND]; // nmat[j][i] = comp.normal(j, i)
+      for (int i = 0; i < ND; ++i) for (int j = 0; j < ND; ++j)
+        nmat[j][i] = deformed ? nrml[(i*ND + j)*nq + q] : (i == j ? 1. : 0.);
+      Conv c = scalars_conv(s);
+      for (int i = 0; i < ND; ++i) {
+        double col[ND], f[nv];
+        for (int j = 0; j < ND; ++j) col[j] = nmat[j][i];
+        flux_conv(s, c, col, f);
+        for (int v = 0; v < nv; ++v) flux[i][v][q] = f[v];
+      }
+      if (viscous) {
+        double g[nv][ND];
+        for (int d = 0; d < ND; ++d) for (int v = 0; v < nv; ++v) g[v][d] = visc_storage[d][v][q];
+        if (deformed) for (int v = 0; v < nv; ++v) for (int d = 0; d < ND; ++d) g[v][d] /= det[q];
+        Diff df = scalars_diff(s, c, visc, cond);
+        double fd[nv][ND];
+        flux_diff(s, c, df, g, nmat, !deformed, fd);
+        for (int d = 0; d < ND; ++d) for (int v = 0; v < nv; ++v) visc_storage[d][v][q] = fd[v][d];
+      }
+    }
+
+    // residual (Spatial.hpp:445-470)
+    for (int d = 0; d < ND; ++d) {
+      for (int i_fq = 0; i_fq < nfq; ++i_fq) {
+        for (int v = 0; v < nv; ++v) {
+          double row_f[RS], face_f[2], der[RS];
+          for (int i = 0; i < RS; ++i) row_f[i] = flux[d][v][row_qpoint(d, i_fq, i)];
+          for (int s = 0; s < 2; ++s) face_f[s] = faces[2*d + s][v*nfq + i_fq];
+          derivative(row_f, face_f, der);
+          for (int i = 0; i < RS; ++i) {
+            double& x = time_rate[0][v][row_qpoint(d, i_fq, i)];
+            x = 1.*x + -der[i];
+          }
+          if (viscous) {
+            for (int i = 0; i < RS; ++i) row_f[i] = visc_storage[d][v][row_qpoint(d, i_fq, i)];
+            for (int s = 0; s < 2; ++s) {
+              double acc = 0.;
+              for (int i = 0; i < RS; ++i) acc += t.bound[s*RS + i]*row_f[i];
+              visc_faces[2*d + s][v*nfq + i_fq] = acc;
+            }
+            derivative_interior(row_f, der);
+            for (int i = 0; i < RS; ++i) {
+              double& x = time_rate[1][v][row_qpoint(d, i_fq, i)];
+              x = 1.*x + -der[i];
+            }
+          }
+        }
+      }
+    }
+
+    // modal filter (Spatial.hpp:473-481)
+    if (use_filter) {
+      for (int d = 0; d < ND; ++d) {
+        for (int i_fq = 0; i_fq < nfq; ++i_fq) {
+          for (int k = 0; k < 2; ++k) for (int v = 0; v < nv; ++v) {
+            double row[RS];
+            for (int i = 0; i < RS; ++i) row[i] = time_rate[k][v][row_qpoint(d, i_fq, i)];
+            for (int i = 0; i < RS; ++i) {
+              double acc = 0.;
+              for (int j = 0; j < RS; ++j) acc += t.filter[i*RS + j]*row[j];
+              double& x = time_rate[k][v][row_qpoint(d, i_fq, i)];
+              x = 0.*x + acc;
+            }
+          }
+        }
+      }
+    }
+
+    // update (Spatial.hpp:484-503)
+    double* ref_state = rcache(e);
+    for (int q = 0; q < nq; ++q) {
+      double update[nv] = {};
+      double mult = update_coef*tss[q]/d_pos;
+      if (deformed) mult /= det[q];
+      for (int v = 0; v < nv; ++v) {
+        double u = time_rate[0][v][q];
+        if (stage) {
+          u -= ref_state[v*nq + q];
+        } else {
+          ref_state[v*nq + q] = u;
+          if (viscous) u += time_rate[1][v][q];
+        }
+        u *= mult;
+        if (compute_residual) ref_state[v*nq + q] = u;
+        else update[v] = u;
+      }
+      for (int v = 0; v < nv; ++v) state[v*nq + q] += update[v];
+    }
+    if (!viscous) write_face_elem(state, faces);
+  }
+
+  void local(bool viscous, double dt, int stage, bool compute_residual, bool use_filter,
+             const hexed_transport& visc, const hexed_transport& cond) const
+  {
+    double update_coef = stage ? dt*t.step_ratio : dt;
+    #pragma omp parallel for
+    for (int e = 0; e < m.n_car_elem; ++e)
+      local_elem(e, false, viscous, update_coef, stage, compute_residual, use_filter, visc, cond);
+    #pragma omp parallel for
+    for (int e = m.n_car_elem; e < n_elem(); ++e)
+      local_elem(e, true, viscous, update_coef, stage, compute_residual, use_filter, visc, cond);
+  }
+
+  // Spatial::Reconcile_ldg_flux (include/Spatial.hpp:543-594)
+  void reconcile_ldg_elem(int e, bool deformed, double dt, bool compute_residual, bool use_filter) const
+  {
+    double* state = elem(e);
+    double* tss = state + nv*nq;
+    double d_pos = m.nom_size[e];
+    const double* det = nullptr;
+    if (deformed) det = m.jac + (size_t)(e - m.n_car_elem)*(ND*ND + 1)*nq + ND*ND*nq;
+    double time_rate[nv][nq];
+    for (int v = 0; v < nv; ++v) for (int q = 0; q < nq; ++q) time_rate[v][q] = 0.;
+    for (int d = 0; d < ND; ++d) {
+      for (int i_fq = 0; i_fq < nfq; ++i_fq) {
+        for (int v = 0; v < nv; ++v) {
+          double b0 = face(e, 2*d, true)[v*nfq + i_fq];
+          double b1 = face(e, 2*d + 1, true)[v*nfq + i_fq];
+          for (int i = 0; i < RS; ++i) {
+            double l = 0.;
+            l += lift[i][0]*b0;
+            l += lift[i][1]*b1;
+            double& x = time_rate[v][row_qpoint(d, i_fq, i)];
+            x = 1.*x + -l;
+          }
+        }
+      }
+    }
+    if (use_filter) {
+      for (int d = 0; d < ND; ++d) for (int i_fq = 0; i_fq < nfq; ++i_fq) for (int v = 0; v < nv; ++v) {
+        double row[RS];
+        for (int i = 0; i < RS; ++i) row[i] = time_rate[v][row_qpoint(d, i_fq, i)];
+        for (int i = 0; i < RS; ++i) {
+          double acc = 0.;
+          for (int j = 0; j < RS; ++j) acc += t.filter[i*RS + j]*row[j];
+          double& x = time_rate[v][row_qpoint(d, i_fq, i)];
+          x = 0.*x + acc;
+        }
+      }
+    }
+    double* to_update = compute_residual ? rcache(e) : state;
+    for (int q = 0; q < nq; ++q) {
+      double mult = dt*tss[q]/d_pos;
+      if (deformed) mult /= det[q];
+      for (int v = 0; v < nv; ++v) to_update[v*nq + q] += time_rate[v][q]*mult;
+    }
+    double* faces[6];
+    for (int i = 0; i < 2*ND; ++i) faces[i] = face(e, i, false);
+    write_face_elem(state, faces);
+  }
+
+  void reconcile_ldg_flux(double dt, bool compute_residual, bool use_filter) const
+  {
+    #pragma omp parallel for
+    for (int e = 0; e < m.n_car_elem; ++e) reconcile_ldg_elem(e, false, dt, compute_residual, use_filter);
+    #pragma omp parallel for
+    for (int e = m.n_car_elem; e < n_elem(); ++e) reconcile_ldg_elem(e, true, dt, compute_residual, use_filter);
+  }
+
+  // ---------------------------------------------------------------- hanging faces
+  // Spatial::Prolong_refined / Restrict_refined (include/Spatial.hpp:153-206, 230-285)
+  void refine(bool prolong, bool scale, bool offset) const
+  {
+    const int n_face = 1 << (ND - 1);
+    #pragma omp parallel for
+    for (int i_ref = 0; i_ref < m.n_ref_face; ++i_ref) {
+      const int* rf = m.ref_face + 7*i_ref;
+      bool str[2] = {rf[5] != 0, rf[6] != 0};
+      double* coarse = slot(rf[0], false) + offset*nv*nfq;
+      if (!prolong) for (int i = 0; i < nv*nfq; ++i) coarse[i] = 0.;
+      int nf = n_face;
+      for (int d = 0; d < ND - 1; ++d) nf /= 1 + str[d];
+      for (int i_face = 0; i_face < nf; ++i_face) {
+        double* fine = slot(rf[1 + i_face], false) + offset*nv*nfq;
+        for (int v = 0; v < nv; ++v) {
+          double* var_face = fine + v*nfq;
+          if (prolong) for (int q = 0; q < nfq; ++q) var_face[q] = coarse[v*nfq + q];
+          for (int d = 0; d < ND - 1; ++d) {
+            if (str[d]) {
+              for (int q = 0; q < nfq; ++q) {
+                if (prolong) var_face[q] *= 1 + scale;
+                else var_face[q] /= 1 + scale;
+              }
+            } else {
+              const int pw = ND - 2 - d;
+              const int face_stride = str[ND - 2] ? 1 : ipow(2, pw);
+              const int qstride = ipow(RS, pw);
+              const int i_half = (i_face/face_stride)%2;
+              const double* mat = (prolong ? t.prolong : t.restrict_) + i_half*RS*RS;
+              for (int outer = 0; outer < nfq/(RS*qstride); ++outer) {
+                for (int inner = 0; inner < qstride; ++inner) {
+                  double row[RS], res[RS];
+                  for (int k = 0; k < RS; ++k) row[k] = var_face[(outer*RS + k)*qstride + inner];
+                  for (int i = 0; i < RS; ++i) {
+                    double acc = 0.;
+                    for (int j = 0; j < RS; ++j) acc += mat[i*RS + j]*row[j];
+                    res[i] = acc;
+                  }
+                  for (int k = 0; k < RS; ++k) var_face[(outer*RS + k)*qstride + inner] = res[k];
+                }
+              }
+            }
+          }
+          if (!prolong) for (int q = 0; q < nfq; ++q) coarse[v*nfq + q] += var_face[q];
+        }
+      }
+    }
+  }
+
+  // ---------------------------------------------------------------- Max_dt
+  // Spatial::Max_dt::operator() (include/Spatial.hpp:784-828)
+  double max_dt(bool viscous, double msc, double msd, bool local_time,
+                const hexed_transport& visc, const hexed_transport& cond) const
+  {
+    const double max_cfl_c = t.max_cfl*msc;
+    const double max_cfl_d = -2/t.min_eig_diffusion*msd;
+    double dt = std::numeric_limits<double>::max();
+    #pragma omp parallel for reduction(min:dt)
+    for (int e = 0; e < n_elem(); ++e) {
+      double* state = elem(e);
+      double* tss = state + nv*nq;
+      const double* vt = m.vert_tss + (size_t)e*nvert;
+      for (int q = 0; q < nq; ++q) {
+        double vals[nvert];
+        for (int i = 0; i < nvert; ++i) vals[i] = vt[i];
+        int stride = nvert;
+        for (int d = 0; d < ND; ++d) {
+          double coord = t.node[(q/ipow(RS, ND - 1 - d))%RS];
+          stride /= 2;
+          for (int i = 0; i < stride; ++i) vals[i] += coord*(vals[i + stride] - vals[i]);
+        }
+        double spacing = vals[0];    // math::interp (include/math.hpp:207-218)
+        double s[nv + 2];
+        for (int v = 0; v < nv; ++v) s[v] = state[v*nq + q];
+        s[nv] = state[(nv + 1)*nq + q];
+        s[nv + 1] = state[(nv + 2)*nq + q];
+        double scale = 0;
+        scale += char_speed(s)/max_cfl_c/spacing;
+        if (viscous) {
+          Conv c = scalars_conv(s);
+          Diff df = scalars_diff(s, c, visc, cond);
+          double diffusivity = std::abs(df.laplacian_av) + std::max(std::abs(df.bulk_av) + df.mu/c.mass, df.energy_cond/c.mass);
+          scale += diffusivity/max_cfl_d/spacing/spacing;
+        }
+        if (local_time) tss[q] = 1./scale;
+        else {
+          tss[q] = 1.;
+          dt = std::min(dt, 1./scale);
+        }
+      }
+    }
+    return local_time ? 1. : dt;
+  }
+
+  // ---------------------------------------------------------------- boundary conditions
+  // Navier_stokes::Pde::Characteristics (include/pde.hpp:182-256) plus apply_char
+  // (src/Boundary_condition.cpp:82-95).
+  struct Characteristics {
+    double vals[3], vecs[3][3], dir[ND], mass, veloc[ND];
+    double lu[3][3]; int piv[3];
+    double nrml(const double* v) const { double r = 0.; for (int d = 0; d < ND; ++d) r += dir[d]*v[d]; return r; }
+    void tang(const double* v, double* out) const { double n = nrml(v); for (int d = 0; d < ND; ++d) out[d] = v[d] - dir[d]*n; }
+    Characteristics(const double* state, const double* direction)
+    {
+      double nsq = 0.;
+      for (int d = 0; d < ND; ++d) nsq += direction[d]*direction[d];
+      double norm = std::sqrt(nsq);
+      for (int d = 0; d < ND; ++d) dir[d] = direction[d]/norm;
+      mass = state[ND];
+      for (int d = 0; d < ND; ++d) veloc[d] = state[d]/mass;
+      double vsq = 0.;
+      for (int d = 0; d < ND; ++d) vsq += veloc[d]*veloc[d];
+      double pres = .4*(state[ND + 1] - .5*mass*vsq);
+      double sound_speed = std::sqrt(1.4*std::max(pres, 0.)/mass);
+      vals[2] = nrml(veloc);
+      vals[0] = vals[2] - sound_speed;
+      vals[1] = vals[2] + sound_speed;
+      double d_mass = 1;
+      for (int sign = 0; sign < 2; ++sign) {
+        double d_veloc = (2*sign - 1)*sound_speed/mass*d_mass;
+        double d_pres = 1.4*pres/mass*d_mass;
+        vecs[0][sign] = d_mass*vals[2] + mass*d_veloc;
+        vecs[1][sign] = d_mass;
+        vecs[2][sign] = d_pres/.4 + .5*d_mass*vsq + mass*vals[2]*d_veloc;
+      }
+      vecs[0][2] = d_mass*vals[2];
+      vecs[1][2] = d_mass;
+      vecs[2][2] = .5*d_mass*vsq;
+      // LU with partial pivoting of vecs
+      for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) lu[i][j] = vecs[i][j];
+      for (int i = 0; i < 3; ++i) piv[i] = i;
+      for (int k = 0; k < 3; ++k) {
+        int p = k;
+        for (int i = k + 1; i < 3; ++i) if (std::abs(lu[i][k]) > std::abs(lu[p][k])) p = i;
+        if (p != k) { for (int j = 0; j < 3; ++j) std::swap(lu[k][j], lu[p][j]); std::swap(piv[k], piv[p]); }
+        for (int i = k + 1; i < 3; ++i) {
+          double f = lu[k][k] != 0. ? lu[i][k]/lu[k][k] : 0.;
+          lu[i][k] = f;
+          for (int j = k + 1; j < 3; ++j) lu[i][j] -= f*lu[k][j];
+        }
+      }
+    }
+    void solve(const double* b, double* x) const
+    {
+      double y[3];
+      for (int i = 0; i < 3; ++i) {
+        double acc = b[piv[i]];
+        for (int j = 0; j < i; ++j) acc -= lu[i][j]*y[j];
+        y[i] = acc;
+      }
+      for (int i = 2; i >= 0; --i) {
+        double acc = y[i];
+        for (int j = i + 1; j < 3; ++j) acc -= lu[i][j]*x[j];
+        x[i] = lu[i][i] != 0. ? acc/lu[i][i] : 0.;
+      }
+    }
+    // decomp (pde.hpp:234-255): d[nv][3]
+    void decomp(const double* state, double (*d)[3]) const
+    {
+      double mmtm[ND], tm[ND], tv[ND], corr[ND];
+      for (int i = 0; i < ND; ++i) mmtm[i] = state[i];
+      tang(mmtm, tm);
+      tang(veloc, tv);
+      for (int i = 0; i < ND; ++i) corr[i] = tm[i] - state[ND]*tv[i];
+      double vc = 0.;
+      for (int i = 0; i < ND; ++i) vc += veloc[i]*corr[i];
+      double s1d[3] = {nrml(mmtm), state[ND], state[ND + 1] - vc};
+      double eb[3];
+      solve(s1d, eb);
+      double ed[3][3];
+      for (int r = 0; r < 3; ++r) for (int c = 0; c < 3; ++c) ed[r][c] = vecs[r][c]*eb[c];
+      for (int c = 0; c < 3; ++c) {
+        d[ND][c] = ed[1][c];
+        d[ND + 1][c] = ed[2][c];
+        for (int i = 0; i < ND; ++i) d[i][c] = dir[i]*ed[0][c] + tv[i]*eb[c];
+      }
+      for (int i = 0; i < ND; ++i) d[i][2] += corr[i];
+      d[ND + 1][2] += vc;
+    }
+  };
+
+  static void apply_char(const double* state, const double* normal, int sign, const double* inside,
+                         const double* outside, double* out)
+  {
+    Characteristics ch(state, normal);
+    double di[nv][3], fo[nv][3];
+    ch.decomp(inside, di);
+    ch.decomp(outside, fo);
+    for (int i = 0; i < 3; ++i) {
+      if (sign*ch.vals[i] > 0) for (int r = 0; r < nv; ++r) di[r][i] = fo[r][i];
+    }
+    for (int r = 0; r < nv; ++r) {
+      double acc = 0.;
+      for (int c = 0; c < 3; ++c) acc += di[r][c];
+      out[r] = acc;
+    }
+  }
+
+  static void reflect_normal(double* gh, const double* nrml) // Boundary_condition.cpp:302-317
+  {
+    for (int q = 0; q < nfq; ++q) {
+      double dot = 0., norm_sq = 0.;
+      for (int d = 0; d < ND; ++d) {
+        double n = nrml[d*nfq + q];
+        dot += gh[d*nfq + q]*n;
+        norm_sq += n*n;
+      }
+      for (int d = 0; d < ND; ++d) gh[d*nfq + q] -= 2*dot*nrml[d*nfq + q]/norm_sq;
+    }
+  }
+
+  void copy_state(double* in, double* gh) const // Boundary_condition.cpp:12-22 (both slots)
+  {
+    std::memcpy(gh, in, sizeof(double)*2*nv*nfq);
+  }
+
+  // Thermal_bc (include/Boundary_condition.hpp:140-190; src/Boundary_condition.cpp:373-379)
+  static double ghost_energy(const hexed_bc_spec& b, const double* s)
+  {
+    if (b.thermal_kind == HEXED_THERMAL_ENERGY) return b.thermal_value*s[nv - 2];
+    return s[nv - 1];
+  }
+  static double ghost_heat_flux(const hexed_bc_spec& b, const double* s, double heat_flux)
+  {
+    if (b.thermal_kind == HEXED_THERMAL_ENERGY) return heat_flux;
+    if (b.thermal_kind == HEXED_THERMAL_HEAT_FLUX) return b.thermal_value;
+    double temp = s[nv - 1]*.4/s[nv - 2]/specific_gas_air;
+    const double sb = 2*ipow_d(M_PI, 5)*ipow_d(1.380649e-23, 4)/(15*ipow_d(299792458., 2)*ipow_d(6.62607015e-34, 3));
+    double radiative = b.emissivity*sb*ipow_d(temp, 4);
+    double conductive = b.heat_transfer_coef*(temp - b.temperature);
+    return radiative + conductive;
+  }
+  static double ipow_d(double x, int e) { double r = 1; for (int i = 0; i < e; ++i) r *= x; return r; }
+
+  void apply_state_bc(int i) const
+  {
+    const int* c = m.bc_con + 4*i;
+    const hexed_bc_spec& b = m.bc_spec[c[3]];
+    int ifs = (c[2] >> 2) & 1;
+    double* in = slot(c[0], false);
+    double* gh = slot(c[1], false);
+    const double* nrml = m.bc_nrml + (size_t)i*ND*nfq;
+    double* sc = m.bc_cache + (size_t)i*2*nv*nfq;
+    switch (b.kind) {
+      case HEXED_BC_FREESTREAM:
+        for (int v = 0; v < nv; ++v) for (int q = 0; q < nfq; ++q) gh[v*nfq + q] = b.freestream[v];
+        break;
+      case HEXED_BC_RIEMANN_INVARIANTS: {
+        int sign = 1 - 2*ifs;
+        for (int q = 0; q < nfq; ++q) {
+          double inside[nv], n[ND], st[nv];
+          for (int v = 0; v < nv; ++v) inside[v] = in[v*nfq + q];
+          for (int d = 0; d < ND; ++d) n[d] = nrml[d*nfq + q];
+          apply_char(inside, n, sign, inside, b.freestream, st);
+          st[ND] = std::max(st[ND], inside[ND]/2);
+          double sq = 0., isq = 0.;
+          for (int d = 0; d < ND; ++d) { sq += st[d]*st[d]; isq += inside[d]*inside[d]; }
+          double kin = .5*sq/st[ND];
+          double ikin = .5*isq/inside[ND];
+          st[ND + 1] = std::max(kin + std::max(st[ND + 1] - kin, (inside[ND + 1] - ikin)/2), 0.);
+          for (int v = 0; v < nv; ++v) gh[v*nfq + q] = st[v];
+        }
+        for (int k = 0; k < nv*nfq; ++k) sc[k] = in[k];
+        break;
+      }
+      case HEXED_BC_NONPENETRATION:
+        for (int k = 0; k < nv*nfq; ++k) gh[k] = in[k];
+        reflect_normal(gh, nrml);
+        break;
+      case HEXED_BC_COPY:
+      case HEXED_BC_OUTFLOW:
+        copy_state(in, gh);
+        break;
+      case HEXED_BC_PRESSURE_OUTFLOW: {
+        int sign = 2*ifs - 1;
+        for (int q = 0; q < nfq; ++q) {
+          double inside[nv], n[ND];
+          for (int v = 0; v < nv; ++v) inside[v] = in[v*nfq + q];
+          for (int d = 0; d < ND; ++d) n[d] = nrml[d*nfq + q];
+          double dot = 0., nsq = 0., msq = 0.;
+          for (int d = 0; d < ND; ++d) { dot += inside[d]*n[d]; nsq += n[d]*n[d]; msq += inside[d]*inside[d]; }
+          double nrml_veloc = dot/inside[ND]/std::sqrt(nsq);
+          double kin = .5*msq/inside[ND];
+          double pres = std::max(.4*(inside[ND + 1] - kin), 0.);
+          double sound = std::sqrt(1.4*pres/inside[ND]);
+          double ghost[nv];
+          for (int v = 0; v < nv; ++v) ghost[v] = inside[v];
+          if (nrml_veloc*sign < sound) ghost[ND + 1] = b.pressure/.4 + kin;
+          for (int v = 0; v < nv; ++v) gh[v*nfq + q] = ghost[v];
+        }
+        break;
+      }
+      case HEXED_BC_NO_SLIP: {
+        for (int k = 0; k < ND*nfq; ++k) gh[k] = -in[k];
+        for (int k = ND*nfq; k < (ND + 1)*nfq; ++k) gh[k] = in[k];
+        for (int q = 0; q < nfq; ++q) {
+          double s[nv];
+          for (int v = 0; v < nv; ++v) s[v] = in[v*nfq + q];
+          double ge = ghost_energy(b, s);
+          gh[(ND + 1)*nfq + q] = ge*ge/s[nv - 1];
+        }
+        for (int k = 0; k < nv*nfq; ++k) sc[k] = (gh[k] + in[k])/2;
+        break;
+      }
+    }
+  }
+
+  void apply_state_bcs() const
+  {
+    #pragma omp parallel for
+    for (int i = 0; i < m.n_bc_con; ++i) apply_state_bc(i);
+  }
+
+  void apply_flux_bc(int i) const // Solver::apply_flux_bcs (src/Solver.cpp:69-81)
+  {
+    const int* c = m.bc_con + 4*i;
+    const hexed_bc_spec& b = m.bc_spec[c[3]];
+    int ifs = (c[2] >> 2) & 1;
+    double* in_l = slot(c[0], true);
+    double* gh_l = slot(c[1], true);
+    const double* nrml = m.bc_nrml + (size_t)i*ND*nfq;
+    double* sc = m.bc_cache + (size_t)i*2*nv*nfq;
+    double* fc = sc + nv*nfq;
+    for (int k = 0; k < nv*nfq; ++k) fc[k] = in_l[k];
+    switch (b.kind) {
+      case HEXED_BC_FREESTREAM:
+      case HEXED_BC_COPY:
+        copy_state(slot(c[0], false), slot(c[1], false));
+        break;
+      case HEXED_BC_RIEMANN_INVARIANTS: {
+        int sign = 1 - 2*ifs;
+        double zero[nv] = {};
+        for (int q = 0; q < nfq; ++q) {
+          double inside[nv], cache[nv], n[ND], st[nv];
+          for (int v = 0; v < nv; ++v) { inside[v] = in_l[v*nfq + q]; cache[v] = sc[v*nfq + q]; }
+          for (int d = 0; d < ND; ++d) n[d] = nrml[d*nfq + q];
+          apply_char(cache, n, sign, zero, inside, st);
+          for (int v = 0; v < nv; ++v) gh_l[v*nfq + q] = st[v];
+        }
+        break;
+      }
+      case HEXED_BC_NONPENETRATION:
+        for (int k = 0; k < nv*nfq; ++k) gh_l[k] = -in_l[k];
+        reflect_normal(gh_l, nrml);
+        break;
+      case HEXED_BC_OUTFLOW:
+      case HEXED_BC_PRESSURE_OUTFLOW:
+        for (int k = 0; k < nv*nfq; ++k) gh_l[k] = -in_l[k];
+        break;
+      case HEXED_BC_NO_SLIP: {
+        for (int k = 0; k < ND*nfq; ++k) gh_l[k] = in_l[k];
+        for (int k = ND*nfq; k < (ND + 1)*nfq; ++k) gh_l[k] = -in_l[k];
+        for (int q = 0; q < nfq; ++q) {
+          int k = q + (ND + 1)*nfq;
+          double normal = 0;
+          for (int d = 0; d < ND; ++d) { double n = nrml[d*nfq + q]; normal += n*n; }
+          normal = std::sqrt(normal);
+          int flux_sign = 2*ifs - 1;
+          double s[nv];
+          for (int v = 0; v < nv; ++v) s[v] = sc[v*nfq + q];
+          gh_l[k] = b.coercion*(normal*flux_sign*ghost_heat_flux(b, s, in_l[k]*flux_sign/normal) - in_l[k]) + in_l[k];
+        }
+        break;
+      }
+    }
+  }
+
+  void apply_flux_bcs() const
+  {
+    #pragma omp parallel for
+    for (int i = 0; i < m.n_bc_con; ++i) apply_flux_bc(i);
+  }
+
+  // ---------------------------------------------------------------- kernel sequences
+  // compute_euler (src/kernels_convective.cpp:8-19)
+  void compute_euler(double dt, int stage, bool cr, bool uf) const
+  {
+    hexed_transport inv{0., 0., 1., 1., 0};
+    neighbor(false);
+    refine(false, true, false);
+    local(false, dt, stage, cr, uf, inv, inv);
+    refine(true, false, false);
+  }
+  // compute_navier_stokes (src/kernels_diffusive.cpp:8-32)
+  void compute_navier_stokes(double dt, int stage, bool cr, bool uf,
+                             const hexed_transport& visc, const hexed_transport& cond) const
+  {
+    neighbor(true);
+    refine(false, true, false);
+    refine(false, false, true);
+    local(true, dt, stage, cr, uf, visc, cond);
+    if (!stage) {
+      refine(true, true, true);
+      apply_flux_bcs();
+      neighbor_reconcile();
+      refine(false, true, true);
+      reconcile_ldg_flux(dt, cr, uf);
+    }
+    refine(true, false, false);
+  }
+
+  // integral_field of Physical_residual^2 (src/Solver.cpp:1113-1131, src/Qpoint_func.cpp:37-45)
+  void residual_norm(double* out) const
+  {
+    double w[nq];
+    for (int q = 0; q < nq; ++q) {
+      double p = 1.;
+      for (int d = 0; d < ND; ++d) p *= t.weight[(q/ipow(RS, ND - 1 - d))%RS];
+      w[q] = p;
+    }
+    double acc[nv] = {};
+    for (int e = 0; e < n_elem(); ++e) {
+      double vol = 1.;
+      for (int d = 0; d < ND; ++d) vol *= m.nom_size[e];
+      const double* st = elem(e);
+      const double* rc = rcache(e);
+      const double* det = e >= m.n_car_elem ? m.jac + (size_t)(e - m.n_car_elem)*(ND*ND + 1)*nq + ND*ND*nq : nullptr;
+      for (int q = 0; q < nq; ++q) {
+        double tss = st[nv*nq + q];
+        double jd = det ? det[q] : 1.;
+        for (int v = 0; v < nv; ++v) {
+          double r = rc[v*nq + q]/tss;
+          acc[v] += w[q]*vol*(r*r)*jd;
+        }
+      }
+    }
+    double mom = 0.;
+    for (int d = 0; d < ND; ++d) mom += acc[d];
+    out[0] = std::sqrt(mom);
+    out[1] = std::sqrt(acc[ND]);
+    out[2] = std::sqrt(acc[ND + 1]);
+  }
+};
+
+template <int ND, int RS>
+struct Dispatch;
+
+template <typename F>
+int dispatch(const hexed_mesh_desc* m, F&& f)
+{
+  if (!m) return HEXED_ERR_INVALID;
+  switch (m->n_dim*16 + m->row_size) {
+#define HEXED_D(nd, rs) case nd*16 + rs: { K<nd, rs> k(*m); f(k); return HEXED_OK; }
+    HEXED_D(2, 2) HEXED_D(2, 3) HEXED_D(2, 4) HEXED_D(2, 5) HEXED_D(2, 6) HEXED_D(2, 7) HEXED_D(2, 8)
+    HEXED_D(3, 2) HEXED_D(3, 3) HEXED_D(3, 4) HEXED_D(3, 5) HEXED_D(3, 6) HEXED_D(3, 7) HEXED_D(3, 8)
+#undef HEXED_D
+  }
+  return HEXED_ERR_INVALID;
+}
+
+// chebyshev_step (src/math.cpp:104-107)
+double chebyshev_step(int n_steps, int i_step)
+{
+  return 1/(1 - std::cos((n_steps - i_step - 0.5)*M_PI/n_steps));
+}
+
+} // namespace
+
+extern "C" {
+
+int oracle_write_face(const hexed_mesh_desc* m) { return dispatch(m, [](auto& k) { k.write_face(); }); }
+int oracle_prolong(const hexed_mesh_desc* m, int scale, int offset)
+{ return dispatch(m, [&](auto& k) { k.refine(true, scale, offset); }); }
+int oracle_restrict(const hexed_mesh_desc* m, int scale, int offset)
+{ return dispatch(m, [&](auto& k) { k.refine(false, scale, offset); }); }
+int oracle_apply_state_bcs(const hexed_mesh_desc* m) { return dispatch(m, [](auto& k) { k.apply_state_bcs(); }); }
+int oracle_apply_flux_bcs(const hexed_mesh_desc* m) { return dispatch(m, [](auto& k) { k.apply_flux_bcs(); }); }
+int oracle_neighbor(const hexed_mesh_desc* m, int viscous) { return dispatch(m, [&](auto& k) { k.neighbor(viscous); }); }
+int oracle_compute_euler(const hexed_mesh_desc* m, double dt, int stage, int cr, int uf)
+{ return dispatch(m, [&](auto& k) { k.compute_euler(dt, stage, cr, uf); }); }
+int oracle_compute_navier_stokes(const hexed_mesh_desc* m, double dt, int stage, int cr, int uf,
+                                 const hexed_transport* visc, const hexed_transport* cond)
+{ return dispatch(m, [&](auto& k) { k.compute_navier_stokes(dt, stage, cr, uf, *visc, *cond); }); }
+int oracle_max_dt(const hexed_mesh_desc* m, double msc, double msd, int local_time, int viscous,
+                  const hexed_transport* visc, const hexed_transport* cond, double* out)
+{ return dispatch(m, [&](auto& k) { *out = k.max_dt(viscous, msc, msd, local_time, *visc, *cond); }); }
+int oracle_residual_norm(const hexed_mesh_desc* m, double* out)
+{ return dispatch(m, [&](auto& k) { k.residual_norm(out); }); }
+
+// Solver::update (src/Solver.cpp:834-886); returns the last dt through *out_dt
+int oracle_update(const hexed_mesh_desc* m, const hexed_update_params* p, double* out_dt)
+{
+  return dispatch(m, [&](auto& k) {
+    double dt = 0.;
+    for (int i_flow = 0; i_flow < p->flow_iters; ++i_flow) {
+      double max_cheby = chebyshev_step(p->n_cheby_flow, p->n_cheby_flow - 1);
+      for (int i_cheby = 0; i_cheby < p->n_cheby_flow; ++i_cheby) {
+        double nominal = std::min(k.max_dt(p->use_ldg, p->max_safety/max_cheby, p->max_safety, p->local_time,
+                                           p->visc, p->cond), p->max_time_step);
+        dt = nominal*chebyshev_step(p->n_cheby_flow, i_cheby);
+        for (int i = 0; i < 2; ++i) {
+          k.apply_state_bcs();
+          if (p->use_ldg && !i) k.compute_navier_stokes(dt, i, false, p->use_filter, p->visc, p->cond);
+          else k.compute_euler(dt, i, false, p->use_filter);
+        }
+      }
+    }
+    if (out_dt) *out_dt = dt;
+  });
+}
+
+// Solver::compute_residual (src/Solver.cpp:899-913)
+int oracle_compute_residual(const hexed_mesh_desc* m, const hexed_update_params* p)
+{
+  return dispatch(m, [&](auto& k) {
+    k.apply_state_bcs();
+    if (p->use_ldg) k.compute_navier_stokes(1., 0, true, p->use_filter, p->visc, p->cond);
+    else k.compute_euler(1., 0, true, p->use_filter);
+  });
+}
+
+}

@@ -1,0 +1,172 @@
+"""FP64 parity: every kernel of the CUDA library against the CPU oracle on identical
+arenas (max-norm relative error per variable <= 1e-12)."""
+import numpy as np
+import pytest
+
+from hexed_gb300 import abi, problems
+from hexed_gb300.solver import Context
+import oracle
+from helpers import FP64_TOL, air_transport, cartesian_case, compare_arenas, deformed_case
+
+pytestmark = pytest.mark.gpu
+
+
+def run_pair(ar, op_oracle, op_gpu, precision=abi.FP64):
+    a = ar.copy()
+    b = ar.copy()
+    op_oracle(oracle.Oracle(a))
+    ctx = Context(b, precision)
+    out = op_gpu(ctx)
+    ctx.download_all()
+    ctx.close()
+    return a, b, out
+
+
+def assert_close(a, b, tol=FP64_TOL):
+    errs, bad = compare_arenas(a, b, tol)
+    assert not bad, f"parity errors above {tol}: {bad} (all: {errs})"
+
+
+@pytest.mark.parametrize("nd,rs", [(2, 2), (2, 4), (2, 6), (2, 8), (3, 3), (3, 4), (3, 6)])
+def test_write_face(nd, rs):
+    ar = cartesian_case(nd, rs, 3)
+    a, b, _ = run_pair(ar, lambda o: o.write_face(), lambda c: c.write_face())
+    assert_close(a, b)
+
+
+@pytest.mark.parametrize("kind", [abi.BC_FREESTREAM, abi.BC_RIEMANN, abi.BC_NONPENETRATION, abi.BC_COPY,
+                                  abi.BC_OUTFLOW, abi.BC_PRESSURE_OUTFLOW, abi.BC_NO_SLIP])
+@pytest.mark.parametrize("deformed", [False, True])
+def test_boundary_conditions(kind, deformed):
+    ar = deformed_case(2, 4, 3, kind) if deformed else cartesian_case(2, 4, 3, kind)
+    oracle.Oracle(ar).write_face()
+    ar.face[:, 1] = ar.face[:, 0] * 0.37  # something non-trivial in the LDG slots
+
+    def o_op(o):
+        o.apply_state_bcs()
+        o.apply_flux_bcs()
+
+    def g_op(c):
+        c.apply_state_bcs()
+        c.apply_flux_bcs()
+    a, b, _ = run_pair(ar, o_op, g_op)
+    assert_close(a, b)
+
+
+@pytest.mark.parametrize("nd,rs,n", [(2, 4, 5), (2, 6, 4), (3, 3, 3), (3, 4, 2), (3, 6, 2)])
+@pytest.mark.parametrize("deformed", [False, True])
+@pytest.mark.parametrize("stage", [0, 1])
+@pytest.mark.parametrize("use_filter", [False, True])
+def test_compute_euler(nd, rs, n, deformed, stage, use_filter):
+    kind = abi.BC_RIEMANN
+    ar = deformed_case(nd, rs, n, kind) if deformed else cartesian_case(nd, rs, n, kind)
+    oracle.Oracle(ar).write_face()
+    rng = np.random.default_rng(1)
+    ar.rcache[:] = rng.normal(size=ar.rcache.shape) * 1e2
+    ar.elem[:, ar.nv] = rng.uniform(0.5, 1.5, size=ar.elem[:, ar.nv].shape)   # local time-step scale
+
+    def o_op(o):
+        o.apply_state_bcs()
+        o.compute_euler(1e-5, stage, False, use_filter)
+
+    def g_op(c):
+        c.apply_state_bcs()
+        c.compute_euler(1e-5, stage, False, use_filter)
+    a, b, _ = run_pair(ar, o_op, g_op)
+    assert_close(a, b)
+
+
+@pytest.mark.parametrize("nd,rs,n", [(2, 4, 4), (3, 3, 3), (3, 4, 2), (3, 6, 2)])
+@pytest.mark.parametrize("deformed", [False, True])
+@pytest.mark.parametrize("residual", [False, True])
+def test_compute_navier_stokes(nd, rs, n, deformed, residual):
+    kind = abi.BC_NONPENETRATION
+    ar = deformed_case(nd, rs, n, kind) if deformed else cartesian_case(nd, rs, n, kind)
+    rng = np.random.default_rng(2)
+    ar.elem[:, ar.nv + 1] = rng.uniform(0, 1e-3, size=ar.elem[:, 0].shape)   # bulk AV
+    ar.elem[:, ar.nv + 2] = rng.uniform(0, 1e-3, size=ar.elem[:, 0].shape)   # Laplacian AV
+    oracle.Oracle(ar).write_face()
+    visc, cond = air_transport()
+
+    def o_op(o):
+        o.apply_state_bcs()
+        o.compute_navier_stokes(1e-6, 0, visc, cond, residual)
+
+    def g_op(c):
+        c.apply_state_bcs()
+        c.compute_navier_stokes(1e-6, 0, visc, cond, residual)
+    a, b, _ = run_pair(ar, o_op, g_op)
+    assert_close(a, b)
+
+
+@pytest.mark.parametrize("viscous", [False, True])
+@pytest.mark.parametrize("local_time", [False, True])
+@pytest.mark.parametrize("deformed", [False, True])
+def test_max_dt(viscous, local_time, deformed):
+    ar = deformed_case(3, 4, 3) if deformed else cartesian_case(3, 4, 3)
+    visc, cond = air_transport()
+    res = {}
+
+    def o_op(o):
+        res["o"] = o.max_dt(0.7, 0.5, local_time, viscous, visc, cond)
+
+    def g_op(c):
+        res["g"] = c.max_dt(0.7, 0.5, local_time, viscous, visc, cond)
+    a, b, _ = run_pair(ar, o_op, g_op)
+    assert_close(a, b)
+    assert abs(res["o"] - res["g"]) <= FP64_TOL * abs(res["o"])
+
+
+def test_update_vortex_2d():
+    """Config 1 at reduced size: 20 full Solver::update steps of the isentropic vortex."""
+    ar = problems.vortex_2d(n_per_side=12, row_size=6)
+    oracle.Oracle(ar).write_face()
+    p = abi.update_params(max_safety=0.5)
+    dts = {}
+
+    def o_op(o):
+        dts["o"] = [o.update(p) for _ in range(20)]
+        o.compute_residual(p)
+        dts["on"] = o.residual_norm()
+
+    def g_op(c):
+        dts["g"] = [c.update(p) for _ in range(20)]
+        c.compute_residual(p)
+        dts["gn"] = c.residual_norm()
+    a, b, _ = run_pair(ar, o_op, g_op)
+    assert_close(a, b)
+    np.testing.assert_allclose(dts["g"], dts["o"], rtol=FP64_TOL)
+    np.testing.assert_allclose(dts["gn"], dts["on"], rtol=1e-11)
+
+
+def test_update_taylor_green_small():
+    """Config 2 at reduced size (4^3 deformed, row size 4): 5 viscous updates."""
+    ar = problems.taylor_green_3d(n_per_side=4, row_size=4)
+    oracle.Oracle(ar).write_face()
+    p = abi.update_params(max_safety=0.5, visc=ar.visc, cond=ar.cond)
+    dts = {}
+
+    def o_op(o):
+        dts["o"] = [o.update(p) for _ in range(5)]
+
+    def g_op(c):
+        dts["g"] = [c.update(p) for _ in range(5)]
+    a, b, _ = run_pair(ar, o_op, g_op)
+    assert_close(a, b)
+    np.testing.assert_allclose(dts["g"], dts["o"], rtol=FP64_TOL)
+
+
+def test_local_time_stepping_update():
+    ar = cartesian_case(2, 4, 4)
+    oracle.Oracle(ar).write_face()
+    p = abi.update_params(max_safety=0.5, local_time=True)
+
+    def o_op(o):
+        for _ in range(3):
+            o.update(p)
+
+    def g_op(c):
+        for _ in range(3):
+            c.update(p)
+    a, b, _ = run_pair(ar, o_op, g_op)
+    assert_close(a, b)
