@@ -182,6 +182,40 @@ def run_reference(args):
     return 0
 
 
+def state_errors(a, b, nv):
+    """L2 and Linf errors of state a against reference b: per variable (each relative to
+    that variable's own norm) and per conserved quantity (momentum vector, density, energy)."""
+    out = {"l2_rel": [], "linf_rel": []}
+    for v in range(nv):
+        d, r = a[:, v] - b[:, v], b[:, v]
+        out["l2_rel"].append(float(np.linalg.norm(d) / max(np.linalg.norm(r), 1e-300)))
+        out["linf_rel"].append(float(np.abs(d).max() / max(np.abs(r).max(), 1e-300)))
+    groups = {"momentum": slice(0, nv - 2), "density": slice(nv - 2, nv - 1), "energy": slice(nv - 1, nv)}
+    out["l2_rel_by_quantity"] = {k: float(np.linalg.norm(a[:, s] - b[:, s]) / np.linalg.norm(b[:, s]))
+                                 for k, s in groups.items()}
+    return out
+
+
+def mixed_vs_fp64(n, rs, steps):
+    """Run the same case `steps` updates in FP64 and in mixed precision on the GPU and
+    report the mixed state's error against the FP64 state."""
+    from hexed_gb300.solver import Context
+    states = {}
+    base = make_case(n, rs)
+    for prec in (abi.FP64, abi.MIXED):
+        ar = base.copy()
+        with Context(ar, prec) as c:
+            c.write_face()
+            p = abi.update_params(max_safety=0.5, visc=ar.visc, cond=ar.cond)
+            for _ in range(steps):
+                c.update(p, read_dt=False)
+            states[prec] = c.download(abi.ARRAY_ELEM)[:, :ar.nv]
+    err = state_errors(states[abi.MIXED], states[abi.FP64], ar.nv)
+    err["steps"] = steps
+    err["reference"] = "FP64 GPU path, same mesh and initial state"
+    return err
+
+
 # ------------------------------------------------------------------ GPU arm
 def main():
     ap = argparse.ArgumentParser()
@@ -194,6 +228,7 @@ def main():
     ap.add_argument("--rs", type=int, default=6, help="row size")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=None)
+    ap.add_argument("--err-steps", type=int, default=200, help="updates for the mixed-vs-FP64 error report")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -290,6 +325,11 @@ def main():
     kernels = {k: {"launches": v[0], "total_ms": round(v[1], 4), "share": round(v[1] / sum(x[1] for x in prof.values()), 4)}
                for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])}
 
+    mixed_err = None
+    if precision == abi.MIXED and rank == 0:
+        ctx.close()
+        mixed_err = mixed_vs_fp64(args.n, args.rs, args.err_steps)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         ctx.close()
@@ -313,6 +353,8 @@ def main():
                 "roofline": roofline,
                 "kernels": kernels,
                 "cpu_baseline": cpu}
+        if mixed_err is not None:
+            line["mixed_vs_fp64"] = mixed_err
         print(json.dumps(line))
     if pg:
         pg.destroy_process_group()

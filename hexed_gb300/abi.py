@@ -44,7 +44,8 @@ class MeshDesc(ctypes.Structure):
                 ("nom_size", P_double), ("vert_tss", P_double), ("jac", P_double), ("face_nrml", P_double),
                 ("car_con", P_int), ("def_con", P_int), ("def_con_nrml", P_double),
                 ("bc_con", P_int), ("bc_nrml", P_double), ("bc_cache", P_double),
-                ("ref_face", P_int), ("bc_spec", ctypes.POINTER(BcSpec))]
+                ("ref_face", P_int), ("bc_spec", ctypes.POINTER(BcSpec)),
+                ("n_vert", c_int), ("vert_id", P_int)]
 
 
 class KernelTime(ctypes.Structure):
@@ -54,7 +55,7 @@ class KernelTime(ctypes.Structure):
 class UpdateParams(ctypes.Structure):
     _fields_ = [("max_safety", c_double), ("max_time_step", c_double), ("n_cheby_flow", c_int),
                 ("flow_iters", c_int), ("local_time", c_int), ("use_filter", c_int), ("use_ldg", c_int),
-                ("visc", Transport), ("cond", Transport)]
+                ("visc", Transport), ("cond", Transport), ("av_admis_char_speed", c_double)]
 
 
 def transport_inviscid():
@@ -73,14 +74,15 @@ def transport_sutherland(ref_value, ref_temp, offset):
 
 
 def update_params(max_safety=0.7, max_time_step=1.7976931348623157e308, n_cheby_flow=1, flow_iters=1,
-                  local_time=False, use_filter=False, visc=None, cond=None, use_ldg=None):
-    """Defaults of the Solver namespace (src/Solver.cpp:151-174)."""
+                  local_time=False, use_filter=False, visc=None, cond=None, use_ldg=None, av_admis_char_speed=0.):
+    """Defaults of the Solver namespace (src/Solver.cpp:151-174). use_ldg follows
+    Solver::use_ldg (src/Solver.cpp:117-120): viscous transport or artificial viscosity."""
     visc = visc or transport_inviscid()
     cond = cond or transport_inviscid()
     if use_ldg is None:
-        use_ldg = bool(visc.is_viscous or cond.is_viscous)
+        use_ldg = bool(visc.is_viscous or cond.is_viscous or av_admis_char_speed > 0)
     return UpdateParams(max_safety, max_time_step, n_cheby_flow, flow_iters, int(local_time),
-                        int(use_filter), int(use_ldg), visc, cond)
+                        int(use_filter), int(use_ldg), visc, cond, av_admis_char_speed)
 
 
 class HexedError(RuntimeError):
@@ -119,6 +121,7 @@ def load_library(path=LIB_PATH):
         "hexed_gpu_compute_restrict": ([vp, c_int, c_int], c_int),
         "hexed_gpu_compute_write_face": ([vp], c_int),
         "hexed_gpu_apply_state_bcs": ([vp], c_int),
+        "hexed_gpu_set_art_visc_admis": ([vp, c_double], c_int),
         "hexed_gpu_apply_flux_bcs": ([vp], c_int),
         "hexed_gpu_update": ([vp, ctypes.POINTER(UpdateParams), P_double], c_int),
         "hexed_gpu_compute_residual": ([vp, ctypes.POINTER(UpdateParams)], c_int),

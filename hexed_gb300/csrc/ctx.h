@@ -41,6 +41,7 @@ struct OpsTable {
   void (*bc_state)(Ctx&);
   void (*bc_flux)(Ctx&);
   void (*residual_norm)(Ctx&, double* d_out);
+  void (*set_art_visc_admis)(Ctx&, double char_speed);
 };
 
 struct Ctx {
@@ -55,6 +56,8 @@ struct Ctx {
   double* nom_size; double* vert_tss; double* jac; double* face_nrml;
   int* car_con; int* def_con; double* def_con_nrml;
   int* bc_con; double* bc_nrml; double* bc_cache; int* ref_face; hexed_bc_spec* bc_spec;
+  int n_vert; int* vert_id;            // vertex table (optional)
+  double* uncert; double* vmax;        // artificial-viscosity scratch: [n_elem], [n_vert]
   // scratch
   double* scalars;       // SC_* slots
   double* partials;      // reduction partials, max_partials doubles

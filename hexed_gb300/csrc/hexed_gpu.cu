@@ -117,6 +117,14 @@ int validate(const hexed_mesh_desc* d)
   for (int i = 0; i < d->n_bc_spec; ++i)
     if (d->bc_spec[i].kind < 0 || d->bc_spec[i].kind > HEXED_BC_NO_SLIP)
       return fail(HEXED_ERR_INVALID, "boundary condition %d has unknown kind %d", i, d->bc_spec[i].kind);
+  if (d->n_vert < 0) return fail(HEXED_ERR_INVALID, "negative vertex count");
+  if (d->n_vert > 0) {
+    if (!d->vert_id) return fail(HEXED_ERR_INVALID, "n_vert > 0 but no vertex table");
+    const long n = n_elem << d->n_dim;
+    for (long i = 0; i < n; ++i)
+      if (d->vert_id[i] < 0 || d->vert_id[i] >= d->n_vert)
+        return fail(HEXED_ERR_INVALID, "vertex id %d of entry %ld out of range", d->vert_id[i], i);
+  }
   for (int i = 0; i < d->n_ref_face; ++i) {
     const int* r = d->ref_face + 7*i;
     int nf = 1 << (d->n_dim - 1);
@@ -249,6 +257,13 @@ int hexed_gpu_create(const hexed_mesh_desc* d, int precision, hexed_gpu_ctx** ou
   up(&c->bc_cache, d->bc_cache, (size_t)c->n_bc_con*2*c->nv*c->nfq, "bc_cache");
   up(&c->ref_face, d->ref_face, (size_t)c->n_ref*7, "ref_face");
   up(&c->bc_spec, d->bc_spec, (size_t)c->n_bc_spec, "bc_spec");
+  c->n_vert = d->n_vert;
+  if (c->n_vert > 0) {
+    up(&c->vert_id, d->vert_id, n_elem*nvert, "vert_id");
+    if (st == HEXED_OK && (cudaMalloc((void**)&c->uncert, n_elem*sizeof(double)) != cudaSuccess ||
+                           cudaMalloc((void**)&c->vmax, c->n_vert*sizeof(double)) != cudaSuccess))
+      st = fail(HEXED_ERR_ALLOC, "vertex scratch allocation failed");
+  }
   if (st != HEXED_OK) { hexed_gpu_destroy(c); return st; }
   c->max_partials = 152*16*8;
   if (cudaMalloc((void**)&c->partials, c->max_partials*sizeof(double)) != cudaSuccess ||
@@ -272,7 +287,7 @@ int hexed_gpu_destroy(hexed_gpu_ctx* c)
   if (c->stream) cudaStreamSynchronize(c->stream);
   void* ptrs[] = {c->elem, c->rcache, c->face, c->nom_size, c->vert_tss, c->jac, c->face_nrml, c->car_con,
                   c->def_con, c->def_con_nrml, c->bc_con, c->bc_nrml, c->bc_cache, c->ref_face, c->bc_spec,
-                  c->scalars, c->partials, c->status, c->d_norm};
+                  c->scalars, c->partials, c->status, c->d_norm, c->vert_id, c->uncert, c->vmax};
   for (void* p : ptrs) if (p) cudaFree(p);
   if (c->h_pinned) cudaFreeHost(c->h_pinned);
   if (c->prof) {
@@ -379,6 +394,15 @@ int hexed_gpu_compute_write_face(hexed_gpu_ctx* c)
   return HEXED_OK;
 }
 
+int hexed_gpu_set_art_visc_admis(hexed_gpu_ctx* c, double char_speed)
+{
+  if (int st = check_ctx(c)) return st;
+  if (c->n_vert <= 0) return fail(HEXED_ERR_INVALID, "set_art_visc_admis needs the arena's vertex table");
+  c->ops->set_art_visc_admis(*c, char_speed);
+  HX_LAUNCHED();
+  return HEXED_OK;
+}
+
 int hexed_gpu_apply_state_bcs(hexed_gpu_ctx* c)
 {
   if (int st = check_ctx(c)) return st;
@@ -399,6 +423,10 @@ int hexed_gpu_update(hexed_gpu_ctx* c, const hexed_update_params* p, double* out
 {
   if (int st = check_ctx(c)) return st;
   if (!p || p->n_cheby_flow < 1 || p->flow_iters < 0) return fail(HEXED_ERR_INVALID, "bad update parameters");
+  if (p->av_admis_char_speed > 0) {
+    // Case.cpp:432: set_art_visc_admis before the update when diffusive_admissibility is on
+    if (int st = hexed_gpu_set_art_visc_admis(c, p->av_admis_char_speed)) return st;
+  }
   const double max_cheby = chebyshev_step(p->n_cheby_flow, p->n_cheby_flow - 1);
   for (int i_flow = 0; i_flow < p->flow_iters; ++i_flow) {
     for (int i_cheby = 0; i_cheby < p->n_cheby_flow; ++i_cheby) {

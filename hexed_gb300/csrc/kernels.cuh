@@ -16,6 +16,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <type_traits>
 #include "../../include/hexed_gpu.h"
 
 namespace hx {
@@ -36,6 +37,7 @@ struct Tab {
   double weight[RS];
   double prolong[2*RS*RS];
   double restrict_[2*RS*RS];
+  double ortho_last[RS];   // highest-degree orthonormal Legendre mode at the nodes
   double max_cfl, min_eig_diffusion, step_ratio;
 };
 
@@ -84,60 +86,76 @@ template <typename T> __device__ __forceinline__ T load(const T* p) { return __l
 // Navier_stokes<visc>::Pde::Computation (include/pde.hpp:72-175), one qpoint.
 template <int ND, typename R>
 struct Conv {
-  R mass, kin_ener, pressure;
+  // Divisions by the density are multiplications by its reciprocal (one division per
+  // qpoint): the FP64 pipe of this GPU is the bound, and each double division costs
+  // several FMAs. This moves results by at most an ulp per operation.
+  R mass, inv_mass, kin_ener, pressure;
   __device__ __forceinline__ explicit Conv(const R* s)
   {
     mass = s[ND];
+    inv_mass = R(1)/mass;
     kin_ener = 0;
     #pragma unroll
     for (int d = 0; d < ND; ++d) kin_ener += s[d]*s[d];
-    kin_ener *= R(.5)/mass;
+    kin_ener *= R(.5)*inv_mass;
     pressure = R(heat_rat - 1.)*(s[ND + 1] - kin_ener);
   }
-  // compute_flux_conv for one flux direction n (pde.hpp:108-122)
-  __device__ __forceinline__ void flux(const R* s, const R* n, R* f) const
+  // compute_flux_conv for one flux direction n (pde.hpp:108-122). `p_mom` is the pressure
+  // used in the momentum flux: the pressure itself, or (mixed form) its deviation from an
+  // element reference pressure whose contribution is accounted for in double elsewhere.
+  __device__ __forceinline__ void flux(const R* s, const R* n, R* f, R p_mom) const
   {
     R fm = 0;
     #pragma unroll
     for (int j = 0; j < ND; ++j) fm += s[j]*n[j];
     f[ND] = fm;
-    R vol_flux = fm/mass;
+    R vol_flux = fm*inv_mass;
     f[ND + 1] = (s[ND + 1] + pressure)*vol_flux;
     #pragma unroll
-    for (int j = 0; j < ND; ++j) f[j] = s[j]*vol_flux + pressure*n[j];
+    for (int j = 0; j < ND; ++j) f[j] = s[j]*vol_flux + p_mom*n[j];
   }
+  __device__ __forceinline__ void flux(const R* s, const R* n, R* f) const { flux(s, n, f, pressure); }
 };
 
 template <int ND, typename R>
-__device__ __forceinline__ R char_speed(const R* s) // pde.hpp:161-166
+__device__ __forceinline__ R char_speed(const R* s, R inv_mass) // pde.hpp:161-166
 {
-  R sound_speed = sqrt(R(heat_rat*(heat_rat - 1))*s[ND + 1]/s[ND]);
+  R sound_speed = sqrt(R(heat_rat*(heat_rat - 1))*s[ND + 1]*inv_mass);
   R sq = 0;
   #pragma unroll
   for (int d = 0; d < ND; ++d) sq += s[d]*s[d];
-  return sound_speed + sqrt(sq)/s[ND];
+  return sound_speed + sqrt(sq)*inv_mass;
+}
+
+// Transport_model with its constants folded on the host (include/Transport_model.hpp:21-44)
+struct Tm {
+  double const_val, ref_val, inv_sqrt_ref_temp, ref_temp_plus_offset, temp_offset;
+};
+inline Tm make_tm(const hexed_transport& t)
+{
+  return {t.const_val, t.ref_val, 1./sqrt(t.ref_temp), t.ref_temp + t.temp_offset, t.temp_offset};
 }
 
 template <typename R>
-__device__ __forceinline__ R transport_coef(const hexed_transport& t, R sqrt_temp) // Transport_model.hpp:35-38
+__device__ __forceinline__ R transport_coef(const Tm& t, R sqrt_temp) // Transport_model.hpp:35-38
 {
-  R r = sqrt_temp/R(sqrt(t.ref_temp));
+  R r = sqrt_temp*R(t.inv_sqrt_ref_temp);
   R p3 = r*r*r;
-  return R(t.const_val) + R(t.ref_val)*p3*R(t.ref_temp + t.temp_offset)/(sqrt_temp*sqrt_temp + R(t.temp_offset));
+  return R(t.const_val) + R(t.ref_val)*p3*R(t.ref_temp_plus_offset)/(sqrt_temp*sqrt_temp + R(t.temp_offset));
 }
 
 template <int ND, typename R>
 struct DiffScalars { // compute_scalars_diff (pde.hpp:130-138)
   R bulk_av, laplacian_av, mu, energy_cond;
   __device__ __forceinline__ DiffScalars(const R* s, const Conv<ND, R>& c, R bulk, R lap,
-                                         const hexed_transport& visc, const hexed_transport& cond)
+                                         const Tm& visc, const Tm& cond)
   {
     bulk_av = fabs(bulk);
     laplacian_av = fabs(lap);
-    R sqrt_temp = sqrt(fmax((s[ND + 1] - c.kin_ener)/c.mass, R(0))*R(heat_rat - 1)/R(specific_gas_air));
+    R sqrt_temp = sqrt(fmax((s[ND + 1] - c.kin_ener)*c.inv_mass, R(0))*R(heat_rat - 1)*R(1./specific_gas_air));
     mu = transport_coef(visc, sqrt_temp);
     R k = transport_coef(cond, sqrt_temp);
-    energy_cond = k*R(heat_rat - 1)/R(specific_gas_air);
+    energy_cond = k*R(heat_rat - 1)*R(1./specific_gas_air);
   }
 };
 
@@ -146,15 +164,15 @@ template <int ND, typename R, bool IDENT>
 __device__ __forceinline__ void flux_diff(const R* s, const Conv<ND, R>& c, const DiffScalars<ND, R>& df,
                                           const R (&g)[ND + 2][ND], const R (&nrm)[ND][ND], R (&out)[ND + 2][ND])
 {
-  const R mass = c.mass;
+  const R mass = c.mass, inv_mass = c.inv_mass;
   R veloc[ND];
   #pragma unroll
-  for (int i = 0; i < ND; ++i) veloc[i] = s[i]/mass;
+  for (int i = 0; i < ND; ++i) veloc[i] = s[i]*inv_mass;
   R vg[ND][ND];
   #pragma unroll
   for (int i = 0; i < ND; ++i)
     #pragma unroll
-    for (int j = 0; j < ND; ++j) vg[i][j] = (g[i][j] - veloc[i]*g[ND][j])/mass;
+    for (int j = 0; j < ND; ++j) vg[i][j] = (g[i][j] - veloc[i]*g[ND][j])*inv_mass;
   R trace = 0;
   #pragma unroll
   for (int i = 0; i < ND; ++i) trace += vg[i][i];
@@ -173,13 +191,13 @@ __device__ __forceinline__ void flux_diff(const R* s, const Conv<ND, R>& c, cons
   for (int i = 0; i < ND; ++i)
     #pragma unroll
     for (int j = 0; j < ND; ++j) fd[i][j] -= stress[i][j];
-  const R coef = -s[ND + 1]/mass/mass;
+  const R coef = -s[ND + 1]*inv_mass*inv_mass;
   #pragma unroll
   for (int j = 0; j < ND; ++j) {
     R vvg = 0;
     #pragma unroll
     for (int i = 0; i < ND; ++i) vvg += veloc[i]*vg[i][j];
-    R ieg = coef*g[ND][j] + g[ND + 1][j]/mass - vvg;
+    R ieg = coef*g[ND][j] + g[ND + 1][j]*inv_mass - vvg;
     R vs = 0;
     #pragma unroll
     for (int i = 0; i < ND; ++i) vs += veloc[i]*stress[i][j];
@@ -285,13 +303,14 @@ struct LocalSmem {
                                 + ND*S::nv*S::nq         // s_f
                                 + (VISC ? ND*S::nv*S::nq : 0)   // s_g
                                 + ND*2*S::nv*S::nfq;     // s_bf
-  static constexpr size_t bytes = sizeof(STab<RS, R>) + sizeof(R)*(size_t)per_elem*S::epb + 16;
+  static constexpr size_t bytes = sizeof(STab<RS, R>) + sizeof(R)*(size_t)per_elem*S::epb + 16
+                                  + sizeof(double)*S::epb + 16;
 };
 
 template <int ND, int RS, typename R, bool DEF, bool VISC, typename FaceT>
 __global__ void __launch_bounds__(Shape<ND, RS>::threads)
 k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int compute_residual, int use_filter,
-        hexed_transport visc, hexed_transport cond)
+        Tm visc, Tm cond)
 {
   using S = Shape<ND, RS>;
   constexpr int nq = S::nq, nfq = S::nfq, nv = S::nv, EPB = S::epb;
@@ -301,8 +320,14 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
   R* s_f = s_u + EPB*nv*nq;
   R* s_g = s_f + EPB*ND*nv*nq;
   R* s_bf = s_g + (VISC ? EPB*ND*nv*nq : 0);
+  double* s_pref = reinterpret_cast<double*>(
+      (reinterpret_cast<uintptr_t>(s_bf + EPB*ND*2*nv*nfq) + 15)/16*16);
   st.load(tab);
-
+  // Mixed form: the momentum flux carries p - p_ref, with p_ref the element's pressure at
+  // its first qpoint (in double); p_ref*n is taken out of the face fluxes in double as well.
+  // The identity sum_d [D.n_d + lift.(n_face - B.n_d)] = 0 (free-stream preservation) makes
+  // this exact up to roundoff while removing the cancellation of p ~ p_ref in float.
+  constexpr bool split = !std::is_same<R, double>::value;
   const int le = threadIdx.x/nq;
   const int q = threadIdx.x%nq;
   const int e0 = e_begin + blockIdx.x*EPB;
@@ -310,9 +335,11 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
   const bool active = threadIdx.x < EPB*nq && e < e_end;
   const int ed = e - m.n_car;
   const double d_pos = active ? m.nom_size[e] : 1.;
+  const double inv_dpos = 1./d_pos;
   const double* state_g = m.elem + (size_t)e*(nv + 3)*nq;
 
   R u[nv + 2];   // state + bulk AV + Laplacian AV (include/pde.hpp:79-84)
+  R p_rel = 0;
   R nrm[ND][ND]; // nrm[j][i] = comp.normal(j, i)
   #pragma unroll
   for (int i = 0; i < ND; ++i)
@@ -323,6 +350,21 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
     for (int v = 0; v < nv; ++v) u[v] = R(state_g[v*nq + q]);
     u[nv] = R(state_g[(nv + 1)*nq + q]);
     u[nv + 1] = R(state_g[(nv + 2)*nq + q]);
+    if constexpr (split) {
+      // reference kinetic energy in float: p_ref below is formed from the same value, so
+      // p_rel + p_ref is the pressure whatever its rounding (one FP64 op per thread)
+      R kin_ref = 0;
+      #pragma unroll
+      for (int d = 0; d < ND; ++d) { R m0 = R(state_g[d*nq]); kin_ref += m0*m0; }
+      kin_ref *= R(.5)/R(state_g[ND*nq]);
+      const double e_ref = state_g[(nv - 1)*nq];
+      R kin = 0;
+      #pragma unroll
+      for (int d = 0; d < ND; ++d) kin += u[d]*u[d];
+      kin *= R(.5)/u[ND];
+      p_rel = R(heat_rat - 1.)*(R(state_g[(nv - 1)*nq + q] - e_ref) - (kin - kin_ref));
+      if (q == 0) s_pref[le] = (heat_rat - 1.)*(e_ref - double(kin_ref));
+    }
     if constexpr (DEF) {
       const double* nr = m.jac + (size_t)ed*(ND*ND + 1)*nq;
       #pragma unroll
@@ -395,7 +437,7 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
             R l = 0;
             l += st.lift[i*2]*bf[v*nfq + row_of[d]];
             l += st.lift[i*2 + 1]*bf[(nv + v)*nfq + row_of[d]];
-            grad[v][d] = (acc + l)/R(d_pos);
+            grad[v][d] = (acc + l)*R(inv_dpos);
           }
         }
       }
@@ -450,7 +492,7 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
               R l = 0;
               l += st.lift[i*2]*bf[v*nfq + row_of[d]];
               l += st.lift[i*2 + 1]*bf[(nv + v)*nfq + row_of[d]];
-              grad[v][j] = grad[v][j] + (acc + l)/R(d_pos);
+              grad[v][j] = grad[v][j] + (acc + l)*R(inv_dpos);
             }
           }
         }
@@ -463,22 +505,23 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
   // ---- fluxes (Spatial.hpp:405-442)
   if (active) {
     Conv<ND, R> c(u);
+    const R p_mom = split ? p_rel : c.pressure;
     #pragma unroll
     for (int i = 0; i < ND; ++i) {
       R col[ND], f[nv];
       #pragma unroll
       for (int j = 0; j < ND; ++j) col[j] = nrm[j][i];
-      c.flux(u, col, f);
+      c.flux(u, col, f, p_mom);
       #pragma unroll
       for (int v = 0; v < nv; ++v) my_f[(i*nv + v)*nq + q] = f[v];
     }
     if constexpr (VISC) {
       R g[nv][ND];
-      const R det = DEF ? R(m.jac[((size_t)ed*(ND*ND + 1) + ND*ND)*nq + q]) : R(1);
+      const R inv_det = DEF ? R(1./m.jac[((size_t)ed*(ND*ND + 1) + ND*ND)*nq + q]) : R(1);
       #pragma unroll
       for (int v = 0; v < nv; ++v)
         #pragma unroll
-        for (int j = 0; j < ND; ++j) g[v][j] = DEF ? grad[v][j]/det : grad[v][j];
+        for (int j = 0; j < ND; ++j) g[v][j] = DEF ? grad[v][j]*inv_det : grad[v][j];
       DiffScalars<ND, R> df(u, c, u[nv], u[nv + 1], visc, cond);
       R fd[nv][ND];
       flux_diff<ND, R, !DEF>(u, c, df, g, nrm, fd);
@@ -507,8 +550,22 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
       for (int i = 0; i < RS; ++i) { R x = row[i*stride]; a0 += st.bound[i]*x; a1 += st.bound[RS + i]*x; }
       FaceT* fl = m.face + (size_t)(ee*2*ND + 2*d)*S::slot_dof + v*nfq + r;
       R* bf = s_bf + ((l*ND + d)*2*nv)*nfq;
-      bf[v*nfq + r] = R(fl[0]) - a0;
-      bf[(nv + v)*nfq + r] = R(fl[S::slot_dof]) - a1;
+      R fb0, fb1;
+      if (split && v < ND) {
+        double n0 = (v == d) ? 1. : 0., n1 = n0;
+        if constexpr (DEF) {
+          const double* fnr = m.face_nrml + ((size_t)(ee - m.n_car)*2*ND + 2*d)*ND*nfq + v*nfq + r;
+          n0 = fnr[0];
+          n1 = fnr[ND*nfq];
+        }
+        fb0 = R(double(fl[0]) - s_pref[l]*n0);
+        fb1 = R(double(fl[S::slot_dof]) - s_pref[l]*n1);
+      } else {
+        fb0 = R(fl[0]);
+        fb1 = R(fl[S::slot_dof]);
+      }
+      bf[v*nfq + r] = fb0 - a0;
+      bf[(nv + v)*nfq + r] = fb1 - a1;
       if constexpr (VISC) {
         const R* rg = s_g + ((l*ND + d)*nv + v)*nq + off;
         R g0 = 0, g1 = 0;
@@ -583,8 +640,8 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
     const double update_coef = stage ? dt*tab.step_ratio : dt;
     double* st_w = m.elem + (size_t)e*(nv + 3)*nq;
     double* rc = m.rcache + (size_t)e*nv*nq;
-    double mult = update_coef*st_w[nv*nq + q]/d_pos;
-    if constexpr (DEF) mult /= m.jac[((size_t)ed*(ND*ND + 1) + ND*ND)*nq + q];
+    double mult = update_coef*st_w[nv*nq + q]*inv_dpos;
+    if constexpr (DEF) mult *= 1./m.jac[((size_t)ed*(ND*ND + 1) + ND*ND)*nq + q];
     #pragma unroll
     for (int v = 0; v < nv; ++v) {
       double uu = double(rate[v]);
@@ -693,8 +750,8 @@ k_reconcile_ldg(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int compute_r
   if (active) {
     const double dt = m.scalars[SC_DT];
     double* st_w = m.elem + (size_t)e*(nv + 3)*nq;
-    double mult = dt*st_w[nv*nq + q]/m.nom_size[e];
-    if constexpr (DEF) mult /= m.jac[((size_t)(e - m.n_car)*(ND*ND + 1) + ND*ND)*nq + q];
+    double mult = dt*st_w[nv*nq + q]*(1./m.nom_size[e]);
+    if constexpr (DEF) mult *= 1./m.jac[((size_t)(e - m.n_car)*(ND*ND + 1) + ND*ND)*nq + q];
     double* to_update = compute_residual ? m.rcache + (size_t)e*nv*nq : st_w;
     const int ld = compute_residual ? nq : nq;
     #pragma unroll
@@ -711,7 +768,7 @@ k_reconcile_ldg(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int compute_r
 // to both faces with sign; LDG face average for the viscous path. One thread per face qpoint.
 template <int ND, int RS, typename R, typename FaceT>
 __device__ __forceinline__ void neighbor_point(const Dev<FaceT>& m, int slot0, int slot1, int dir, int q,
-                                               const double* nrml, bool viscous, const R* ghost_override)
+                                               const double* nrml, bool viscous, const double* ghost_override)
 {
   using S = Shape<ND, RS>;
   constexpr int nfq = S::nfq, nv = S::nv;
@@ -724,11 +781,14 @@ __device__ __forceinline__ void neighbor_point(const Dev<FaceT>& m, int slot0, i
   const int q1 = deformed ? perm_index<ND, RS>(dir, q) : q;
   FaceT* f0 = m.face + (size_t)slot0*S::slot_dof;
   FaceT* f1 = m.face + (size_t)slot1*S::slot_dof;
-  R u0[nv], u1[nv];
+  R u0[nv], u1[nv], jump[nv];
   #pragma unroll
   for (int v = 0; v < nv; ++v) {
-    u0[v] = R(f0[v*nfq + q]);
-    u1[v] = ghost_override ? ghost_override[v] : R(f1[v*nfq + q1]);
+    const double a = double(f0[v*nfq + q]);
+    const double b = ghost_override ? double(ghost_override[v]) : double(f1[v*nfq + q1]);
+    u0[v] = R(a);
+    u1[v] = R(b);
+    jump[v] = R(a - b);   // state jump of nearly equal traces: formed in double, then narrowed
   }
   if (viscous) {
     #pragma unroll
@@ -738,24 +798,39 @@ __device__ __forceinline__ void neighbor_point(const Dev<FaceT>& m, int slot0, i
       f1[nv*nfq + v*nfq + q1] = FaceT(avg);
     }
   }
+  constexpr bool split = !std::is_same<R, double>::value;
+  double nd_[ND];
   R n[ND];
   const int i_dim0 = dir & 3;
   #pragma unroll
-  for (int d = 0; d < ND; ++d) n[d] = deformed ? R(sign0)*R(nrml[d*nfq + q]) : (d == i_dim0 ? R(1) : R(0));
+  for (int d = 0; d < ND; ++d) {
+    nd_[d] = deformed ? sign0*nrml[d*nfq + q] : (d == i_dim0 ? 1. : 0.);
+    n[d] = R(nd_[d]);
+  }
   R fl0[nv], fl1[nv];
   Conv<ND, R> c0(u0), c1(u1);
-  c0.flux(u0, n, fl0);
-  c1.flux(u1, n, fl1);
-  const R cs0 = char_speed<ND, R>(u0), cs1 = char_speed<ND, R>(u1);
+  c0.flux(u0, n, fl0, split ? R(0) : c0.pressure);
+  c1.flux(u1, n, fl1, split ? R(0) : c1.pressure);
+  const R cs0 = char_speed<ND, R>(u0, c0.inv_mass), cs1 = char_speed<ND, R>(u1, c1.inv_mass);
   R nn = 0;
   #pragma unroll
   for (int d = 0; d < ND; ++d) nn += n[d]*n[d];
   const R mult = fmax(cs0, cs1)*sqrt(nn);
+  // mixed form: the pressure term of the momentum flux is formed in double from the
+  // double energy, since p*n is large against its variation across the face
+  double p_sum = 0.;
+  if constexpr (split) {
+    double e0 = double(f0[(nv - 1)*nfq + q]);
+    double e1 = ghost_override ? ghost_override[nv - 1] : double(f1[(nv - 1)*nfq + q1]);
+    p_sum = (heat_rat - 1.)*(e0 - double(c0.kin_ener)) + (heat_rat - 1.)*(e1 - double(c1.kin_ener));
+  }
   #pragma unroll
   for (int v = 0; v < nv; ++v) {
-    R flux = R(.5)*(fl0[v] + fl1[v] + mult*(u0[v] - u1[v]));
-    f0[v*nfq + q] = FaceT(R(sign0)*flux);
-    f1[v*nfq + q1] = FaceT(R(sign1)*flux);
+    double flux;
+    if (split && v < ND) flux = .5*(double(fl0[v] + fl1[v] + mult*jump[v]) + p_sum*nd_[v]);
+    else flux = double(R(.5)*(fl0[v] + fl1[v] + mult*jump[v]));
+    f0[v*nfq + q] = FaceT(sign0*flux);
+    f1[v*nfq + q1] = FaceT(sign1*flux);
   }
 }
 
@@ -984,13 +1059,11 @@ __global__ void k_bc_neighbor(Dev<FaceT> m)
   for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
     const int i = int(t/nfq), q = int(t%nfq);
     const int* c = m.bc_con + 4*i;
-    R gr[ND + 2];
-    const R* ov = nullptr;
+    double gh[ND + 2];
+    const double* ov = nullptr;
     if (FUSE) {
-      double gh[ND + 2];
       bc_state_point<ND, RS, FaceT>(m, i, q, gh);
-      for (int v = 0; v < ND + 2; ++v) gr[v] = R(gh[v]);
-      ov = gr;
+      ov = gh;
     }
     neighbor_point<ND, RS, R, FaceT>(m, c[0], c[1], bc_dir(c[2]), q, m.bc_nrml + (size_t)i*ND*nfq, VISC, ov);
   }
@@ -1214,47 +1287,51 @@ __global__ void k_write_face(Dev<FaceT> m, Tab<RS> tab)
 
 // ------------------------------------------------------------------- Max_dt
 // Spatial::Max_dt (include/Spatial.hpp:784-828); global minimum through per-CTA partials.
-template <int ND, int RS, bool VISC, typename FaceT>
+// R is the compute type: double for the FP64 form; float for the mixed form, whose time
+// step is a CFL limit with a safety factor and needs no more than float accuracy.
+template <int ND, int RS, typename R, bool VISC, typename FaceT>
 __global__ void __launch_bounds__(256)
-k_max_dt(Dev<FaceT> m, Tab<RS> tab, double msc, double msd, int local_time, hexed_transport visc,
-         hexed_transport cond, double* partials)
+k_max_dt(Dev<FaceT> m, Tab<RS> tab, double msc, double msd, int local_time, Tm visc,
+         Tm cond, double* partials)
 {
   using S = Shape<ND, RS>;
   constexpr int nq = S::nq, nv = S::nv, nvert = S::nvert;
-  const double max_cfl_c = tab.max_cfl*msc;
-  const double max_cfl_d = -2/tab.min_eig_diffusion*msd;
+  const R inv_cfl_c = R(1./(tab.max_cfl*msc));
+  const R inv_cfl_d = R(1./(-2/tab.min_eig_diffusion*msd));
   double dt = 1.7976931348623157e308;
   const long total = (long)m.n_elem*nq;
   for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
     const int e = int(t/nq), q = int(t%nq);
     double* state = m.elem + (size_t)e*(nv + 3)*nq;
-    double vals[nvert];
+    R vals[nvert];
     #pragma unroll
-    for (int i = 0; i < nvert; ++i) vals[i] = m.vert_tss[(size_t)e*nvert + i];
+    for (int i = 0; i < nvert; ++i) vals[i] = R(m.vert_tss[(size_t)e*nvert + i]);
     int stride = nvert;
     #pragma unroll
     for (int d = 0; d < ND; ++d) {
-      const double coord = tab.node[(q/ipow(RS, ND - 1 - d))%RS];
+      const R coord = R(tab.node[(q/ipow(RS, ND - 1 - d))%RS]);
       stride /= 2;
       #pragma unroll
       for (int i = 0; i < (nvert >> (d + 1)); ++i) vals[i] += coord*(vals[i + stride] - vals[i]);
     }
-    const double spacing = vals[0];
-    double s[nv];
+    const R spacing = vals[0];
+    R s[nv];
     #pragma unroll
-    for (int v = 0; v < nv; ++v) s[v] = state[v*nq + q];
-    double scale = 0;
-    scale += char_speed<ND, double>(s)/max_cfl_c/spacing;
+    for (int v = 0; v < nv; ++v) s[v] = R(state[v*nq + q]);
+    const R inv_spacing = R(1)/spacing;
+    Conv<ND, R> c(s);
+    R scale = 0;
+    scale += char_speed<ND, R>(s, c.inv_mass)*inv_cfl_c*inv_spacing;
     if constexpr (VISC) {
-      Conv<ND, double> c(s);
-      DiffScalars<ND, double> df(s, c, state[(nv + 1)*nq + q], state[(nv + 2)*nq + q], visc, cond);
-      double diffusivity = fabs(df.laplacian_av) + fmax(fabs(df.bulk_av) + df.mu/c.mass, df.energy_cond/c.mass);
-      scale += diffusivity/max_cfl_d/spacing/spacing;
+      DiffScalars<ND, R> df(s, c, R(state[(nv + 1)*nq + q]), R(state[(nv + 2)*nq + q]), visc, cond);
+      R diffusivity = fabs(df.laplacian_av) + fmax(fabs(df.bulk_av) + df.mu*c.inv_mass, df.energy_cond*c.inv_mass);
+      scale += diffusivity*inv_cfl_d*inv_spacing*inv_spacing;
     }
-    if (local_time) state[nv*nq + q] = 1./scale;
+    const double step = double(R(1)/scale);
+    if (local_time) state[nv*nq + q] = step;
     else {
       state[nv*nq + q] = 1.;
-      dt = fmin(dt, 1./scale);
+      dt = fmin(dt, step);
     }
   }
   // CTA minimum
@@ -1306,6 +1383,93 @@ static __global__ void k_fp64_fma(double* out, int iters, double a)
   #pragma unroll
   for (int k = 0; k < fp64_fma_chains; ++k) s += x[k];
   out[blockIdx.x*blockDim.x + threadIdx.x] = s;
+}
+
+// ------------------------------------------------------------------- artificial viscosity
+// Stab_art_visc (src/stabilizing_art_visc.cpp:26-60): per-element smoothness indicator of the
+// specific volume. The CTA stages 1/rho in shared memory; one thread per element forms the
+// sums in the reference's order.
+template <int ND, int RS>
+__global__ void __launch_bounds__(Shape<ND, RS>::threads)
+k_av_uncert(const double* elem, const double* nom_size, int n_elem, Tab<RS> tab, double char_speed, double* uncert)
+{
+  using S = Shape<ND, RS>;
+  constexpr int nq = S::nq, nfq = S::nfq, nv = S::nv, EPB = S::epb;
+  __shared__ double s_iv[EPB*nq];
+  const int le = threadIdx.x/nq, q = threadIdx.x%nq;
+  const int e = blockIdx.x*EPB + le;
+  const bool active = threadIdx.x < EPB*nq && e < n_elem;
+  if (active) s_iv[le*nq + q] = 1./elem[(size_t)e*(nv + 3)*nq + ND*nq + q];
+  __syncthreads();
+  if (!active || q != 0) return;
+  const double* iv = s_iv + le*nq;
+  double norm_sq = 0;
+  for (int qq = 0; qq < nq; ++qq) {
+    double w = 1.;
+    for (int d = 0; d < ND; ++d) w *= tab.weight[(qq/ipow(RS, ND - 1 - d))%RS];
+    norm_sq += iv[qq]*iv[qq]*w;
+  }
+  double proj[RS];
+  for (int i = 0; i < RS; ++i) proj[i] = tab.ortho_last[i]*tab.weight[i];
+  double nonsmooth = 0;
+  for (int d = 0; d < ND; ++d) {
+    const int stride = S::stride(d);
+    for (int r = 0; r < nfq; ++r) {
+      const double* row = iv + (r/stride)*stride*RS + r%stride;
+      double dot = 0.;
+      for (int i = 0; i < RS; ++i) dot += row[i*stride]*proj[i];
+      double fw = 1.;
+      for (int k = 0; k < ND - 1; ++k) fw *= tab.weight[(r/ipow(RS, ND - 2 - k))%RS];
+      nonsmooth += dot*dot*fw;
+    }
+  }
+  nonsmooth /= norm_sq*ND;
+  const double ramp_center = -4.25*log(double(RS - 1))/log(10.);
+  const double half_width = 0.5;
+  double indicator = log(nonsmooth)/log(10.);
+  if (indicator <= ramp_center - half_width) indicator = 0;
+  else if (indicator < ramp_center + half_width)
+    indicator = .5*(1 + sin(3.14159265358979323846*(indicator - ramp_center)/2/half_width));
+  else indicator = 1;
+  uncert[e] = (RS - 1)*char_speed*nom_size[e]*indicator;
+}
+
+// share_vertex_data with Vertex::vector_max (src/Solver.cpp:35-54): the values are >= 0, so
+// their IEEE bit patterns order like the values and an integer atomicMax takes the maximum.
+template <int ND>
+__global__ void k_av_vertex_max(const int* vert_id, int n_elem, const double* uncert, double* vmax)
+{
+  constexpr int nvert = 1 << ND;
+  const long total = (long)n_elem*nvert;
+  for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
+    const double x = uncert[t/nvert];
+    atomicMax(reinterpret_cast<unsigned long long*>(vmax) + vert_id[t], (unsigned long long)__double_as_longlong(x));
+  }
+}
+
+// Multilinear interpolation of the vertex values to the qpoints (Gauss_lobatto(2).interpolate
+// + math::hypercube_matvec, src/Solver.cpp:648-656): last reference dimension first.
+template <int ND, int RS>
+__global__ void k_av_interp(double* elem, const int* vert_id, int n_elem, Tab<RS> tab, const double* vmax)
+{
+  using S = Shape<ND, RS>;
+  constexpr int nq = S::nq, nv = S::nv, nvert = S::nvert;
+  const long total = (long)n_elem*nq;
+  for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
+    const int e = int(t/nq), q = int(t%nq);
+    double vals[nvert];
+    #pragma unroll
+    for (int v = 0; v < nvert; ++v) vals[v] = vmax[vert_id[e*nvert + v]];
+    int n = nvert;
+    #pragma unroll
+    for (int d = ND - 1; d >= 0; --d) {
+      const double x = tab.node[(q/ipow(RS, ND - 1 - d))%RS];
+      #pragma unroll
+      for (int i = 0; i < (nvert >> (ND - d)); ++i) vals[i] = (1. - x)*vals[2*i] + x*vals[2*i + 1];
+      n /= 2;
+    }
+    elem[(size_t)e*(nv + 3)*nq + (nv + 2)*nq + q] = vals[0];
+  }
 }
 
 // ------------------------------------------------------------------- residual norm

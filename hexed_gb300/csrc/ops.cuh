@@ -51,6 +51,7 @@ struct Runner
       t.weight[i] = h.weight[i];
     }
     for (int i = 0; i < 2*RS*RS; ++i) { t.prolong[i] = h.prolong[i]; t.restrict_[i] = h.restrict_[i]; }
+    for (int i = 0; i < RS; ++i) t.ortho_last[i] = h.ortho[(RS - 1)*RS + i];
     t.max_cfl = h.max_cfl; t.min_eig_diffusion = h.min_eig_diffusion; t.step_ratio = h.step_ratio;
     return t;
   }
@@ -70,7 +71,7 @@ struct Runner
       configured = true;
     }
     ProfScope ps(c, DEF ? (VISC ? "local_def_ns" : "local_def_euler") : (VISC ? "local_car_ns" : "local_car_euler"));
-    kern<<<blocks, S::threads, smem, c.stream>>>(dev(c), tab(c), e_begin, e_end, stage, cr, uf, visc, cond);
+    kern<<<blocks, S::threads, smem, c.stream>>>(dev(c), tab(c), e_begin, e_end, stage, cr, uf, make_tm(visc), make_tm(cond));
   }
 
   template <bool DEF>
@@ -187,8 +188,8 @@ struct Runner
     const int grid = grid_for(total, 256, c.max_partials);
     {
       ProfScope ps(c, "max_dt");
-      if (viscous) k_max_dt<ND, RS, true, FaceT><<<grid, 256, 0, c.stream>>>(dev(c), tab(c), msc, msd, local_time, visc, cond, c.partials);
-      else k_max_dt<ND, RS, false, FaceT><<<grid, 256, 0, c.stream>>>(dev(c), tab(c), msc, msd, local_time, visc, cond, c.partials);
+      if (viscous) k_max_dt<ND, RS, R, true, FaceT><<<grid, 256, 0, c.stream>>>(dev(c), tab(c), msc, msd, local_time, make_tm(visc), make_tm(cond), c.partials);
+      else k_max_dt<ND, RS, R, false, FaceT><<<grid, 256, 0, c.stream>>>(dev(c), tab(c), msc, msd, local_time, make_tm(visc), make_tm(cond), c.partials);
     }
     ProfScope ps(c, "finalize_dt");
     k_finalize_dt<<<1, 256, 0, c.stream>>>(c.scalars, c.partials, grid, local_time, max_time_step, cheby);
@@ -213,10 +214,29 @@ struct Runner
     k_residual_final<S::nv><<<1, 32, 0, c.stream>>>(c.partials, grid, d_out);
   }
 
+  // Solver::set_art_visc_admis (src/Solver.cpp:636-658)
+  static void set_art_visc_admis(Ctx& c, double char_speed)
+  {
+    const int n_elem = c.n_car + c.n_def;
+    {
+      ProfScope ps(c, "av_uncert");
+      k_av_uncert<ND, RS><<<(n_elem + S::epb - 1)/S::epb, S::threads, 0, c.stream>>>(c.elem, c.nom_size, n_elem, tab(c),
+                                                                                  char_speed, c.uncert);
+    }
+    cudaMemsetAsync(c.vmax, 0, sizeof(double)*c.n_vert, c.stream);
+    {
+      ProfScope ps(c, "av_vertex_max");
+      k_av_vertex_max<ND><<<grid_for((long)n_elem*S::nvert, 256), 256, 0, c.stream>>>(c.vert_id, n_elem, c.uncert, c.vmax);
+    }
+    ProfScope ps(c, "av_interp");
+    k_av_interp<ND, RS><<<grid_for((long)n_elem*S::nq, 256), 256, 0, c.stream>>>(c.elem, c.vert_id, n_elem, tab(c), c.vmax);
+  }
+
   static const OpsTable* table()
   {
     static const OpsTable t = {
       compute_euler, compute_navier_stokes, max_dt, refine, write_face, bc_state, bc_flux, residual_norm,
+      set_art_visc_admis,
     };
     return &t;
   }

@@ -103,6 +103,11 @@ class Arena:
         d.bc_nrml, d.bc_cache = _ptr(self.bc_nrml), _ptr(self.bc_cache)
         d.ref_face = _ptr(self.ref_face, ctypes.c_int)
         d.bc_spec = ctypes.cast(specs, ctypes.POINTER(abi.BcSpec))
+        if self.vert_ids is not None:
+            ids = np.ascontiguousarray(self.vert_ids, dtype=np.int32)
+            self._vid_keepalive = ids
+            d.n_vert = int(ids.max()) + 1
+            d.vert_id = _ptr(ids, ctypes.c_int)
         return d
 
     def copy(self):

@@ -117,6 +117,73 @@ def sinusoid_displacement(h, amplitude=0.1, seed=0, n_dim=3):
     return disp
 
 
+def sphere_refinement(n_base, radius=0.25, centre=0.5):
+    """Refinement predicate: cells of [0,1]^nd intersecting the sphere."""
+    def refine(level, idx):
+        h = 1.0 / (n_base * 2 ** level)
+        lo = np.array(idx) * h
+        p = np.clip(centre, lo, lo + h)
+        return float(np.linalg.norm(p - centre)) <= radius
+    return refine
+
+
+def pulse_state(pos, fs, amplitude, width, centre):
+    """Freestream plus a Gaussian pressure pulse of `amplitude` times the freestream pressure."""
+    nd = pos.shape[0]
+    rho, mom = fs[nd], fs[:nd]
+    p_inf = (HEAT_RAT - 1) * (fs[nd + 1] - 0.5 * float(mom @ mom) / rho)
+    r2 = sum((pos[d] - centre[d]) ** 2 for d in range(nd))
+    p = p_inf * (1 + amplitude * np.exp(-r2 / width ** 2))
+    st = [np.full_like(pos[0], m) for m in mom] + [np.full_like(pos[0], rho)]
+    st.append(p / (HEAT_RAT - 1) + 0.5 * float(mom @ mom) / rho)
+    return np.stack(st)
+
+
+def pulse_tree_3d(n_base=16, row_size=4, levels=2, mach=0.3, seed=0, amplitude=0.01, width=0.05):
+    """Config: 3D adapted mesh with hanging faces. 16^3 base hexes on [0,1]^3 refined
+    `levels` times in every cell intersecting a centred sphere of radius 0.25 (2:1
+    balanced), Euler at Mach 0.3 with a Gaussian pressure pulse (amplitude 0.01 p_inf,
+    width 0.05) at a seeded random point; Riemann-invariant freestream on the faces."""
+    from .tree import tree_mesh
+    rng = np.random.default_rng(seed)
+    centre = rng.uniform(0.3, 0.7, size=3)
+    fs = freestream_state(3, mach, 0., 1.2, 1e5)
+    spec = bc_spec(abi.BC_RIEMANN, freestream=fs)
+    ar = tree_mesh(3, row_size, n_base, levels, sphere_refinement(n_base),
+                   {(d, s): spec for d in range(3) for s in range(2)})
+    ar.set_state(lambda pos: pulse_state(pos, fs, amplitude, width, centre))
+    ar.freestream = fs
+    ar.pulse_centre = centre
+    return ar
+
+
+def mach2_jump_3d(n_per_side=32, row_size=6, seed=0, amplitude=0.1, density_ratio=2.5, mach=2.):
+    """Config: the deformed 32^3 mesh of the Taylor-Green case carrying an inviscid Mach 2
+    flow along x with a planar density jump (ratio 2.5, equal pressure) at x = pi, which the
+    stabilising artificial viscosity (Solver::set_art_visc_admis) must act on. Riemann-
+    invariant freestream on the x faces, Nonpenetration on the faces parallel to the flow.
+    `av_char_speed` is the freestream speed plus sound speed (src/Solver.cpp:640)."""
+    length = 2 * math.pi
+    h = length / n_per_side
+    fs = freestream_state(3, mach, 0., 1.2, 1e5)
+    riemann = bc_spec(abi.BC_RIEMANN, freestream=fs)
+    wall = bc_spec(abi.BC_NONPENETRATION)
+    bcs = {(d, s): (riemann if d == 0 else wall) for d in range(3) for s in range(2)}
+    ar = structured_mesh(3, row_size, n_per_side, 0., length, deformed=True,
+                         displacement=sinusoid_displacement(h, amplitude, seed), bcs=bcs)
+
+    def state(pos):
+        rho = np.where(pos[0] < math.pi, 1.2, 1.2 * density_ratio)
+        vel = fs[0] / fs[3]
+        p = 1e5
+        return np.stack([rho * vel, 0 * rho, 0 * rho, rho, p / (HEAT_RAT - 1) + 0.5 * rho * vel * vel])
+    ar.set_state(state)
+    ar.freestream = fs
+    sound = math.sqrt(HEAT_RAT * 1e5 / 1.2)
+    ar.av_char_speed = mach * sound + sound
+    return ar
+
+
 def taylor_green_3d(n_per_side=32, row_size=6, mach=0.1, reynolds=1600., seed=0, amplitude=0.1):
     """Config: 3D compressible Navier-Stokes Taylor-Green vortex on deformed hexes."""
     length = 2 * math.pi

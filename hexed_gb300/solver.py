@@ -100,6 +100,9 @@ class Context:
     def apply_state_bcs(self):
         abi.check(self.lib.hexed_gpu_apply_state_bcs(self.handle))
 
+    def set_art_visc_admis(self, char_speed):
+        abi.check(self.lib.hexed_gpu_set_art_visc_admis(self.handle, char_speed))
+
     def apply_flux_bcs(self):
         abi.check(self.lib.hexed_gpu_apply_flux_bcs(self.handle))
 

@@ -44,6 +44,8 @@
  *   bc_cache [n_bc_con][2][nv][nfq] state cache, flux cache (include/connection.hpp:342-377)
  *   ref_face [n_ref_face][7]  coarse slot, fine mortar slots[4] (-1 = unused), stretch0,
  *                             stretch1 (include/Refined_face.hpp:9-15)
+ *   vert_id  [n_elem][nvert]  global vertex index of each element vertex (optional; needed by
+ *                             hexed_gpu_set_art_visc_admis, which shares values over vertices)
  */
 #ifndef HEXED_GPU_H_
 #define HEXED_GPU_H_
@@ -121,6 +123,8 @@ typedef struct hexed_mesh_desc {
   double* bc_cache;
   const int* ref_face;
   const hexed_bc_spec* bc_spec;
+  int n_vert;              /* number of distinct vertices (0: no vertex table) */
+  const int* vert_id;
 } hexed_mesh_desc;
 
 /* Arrays that can be copied in and out of the device arena. */
@@ -148,6 +152,9 @@ typedef struct hexed_update_params {
   int use_filter;        /* modal filter */
   int use_ldg;           /* viscous / artificial-viscosity path (Solver::use_ldg) */
   hexed_transport visc, cond;
+  double av_admis_char_speed; /* > 0: Solver::set_art_visc_admis with this characteristic
+                                 speed before every update, as Case.cpp:432 does when
+                                 "diffusive_admissibility" is set; 0: off */
 } hexed_update_params;
 
 typedef struct hexed_gpu_ctx hexed_gpu_ctx;
@@ -193,6 +200,12 @@ int hexed_gpu_max_dt(hexed_gpu_ctx* ctx, double convective_safety, double diffus
 int hexed_gpu_compute_prolong(hexed_gpu_ctx* ctx, int scale, int offset);
 int hexed_gpu_compute_restrict(hexed_gpu_ctx* ctx, int scale, int offset);
 int hexed_gpu_compute_write_face(hexed_gpu_ctx* ctx);
+
+/* Solver::set_art_visc_admis (src/Solver.cpp:636-658): per-element smoothness indicator of
+ * the specific volume (Stab_art_visc, src/stabilizing_art_visc.cpp:8-66) scaled by
+ * char_speed, maximum over the elements sharing each vertex, multilinear interpolation to
+ * the quadrature points into the Laplacian AV row. Needs the arena's vertex table. */
+int hexed_gpu_set_art_visc_admis(hexed_gpu_ctx* ctx, double char_speed);
 
 /* Solver::apply_state_bcs / apply_flux_bcs (src/Solver.cpp:56-81). */
 int hexed_gpu_apply_state_bcs(hexed_gpu_ctx* ctx);

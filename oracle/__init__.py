@@ -51,8 +51,12 @@ def load():
             "oracle_compute_navier_stokes": [D, c_double, c_int, c_int, c_int, T, T],
             "oracle_max_dt": [D, c_double, c_double, c_int, c_int, T, T, P],
             "oracle_residual_norm": [D, P],
+            "oracle_set_art_visc_admis": [D, c_double],
             "oracle_update": [D, U, P],
             "oracle_compute_residual": [D, U],
+            "oracle_derivative": [c_int, P, P, P],
+            "oracle_perm_index": [c_int, c_int, c_int, c_int],
+            "oracle_characteristics": [c_int, P, P, P, P, P],
         }
         for name, args in sig.items():
             fn = getattr(lib, name)
@@ -60,6 +64,43 @@ def load():
             fn.restype = c_int
         _lib = lib
     return _lib
+
+
+def _dp(a):
+    import numpy as np
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def derivative(row_size, f, fb):
+    """Derivative::operator() on one row: diff.f + lift.(fb - B.f)."""
+    import numpy as np
+    lib = load()
+    f, pf = _dp(f)
+    fb, pb = _dp(fb)
+    out = np.zeros(row_size)
+    _, po = _dp(out)
+    po = out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    assert lib.oracle_derivative(row_size, pf, pb, po) == 0
+    return out
+
+
+def perm_index(n_dim, row_size, direction, q):
+    return load().oracle_perm_index(n_dim, row_size, direction, q)
+
+
+def characteristics(n_dim, state, normal, state1):
+    """(eigenvalues[3], decomposition[nv][3]) of Navier_stokes::Pde::Characteristics."""
+    import numpy as np
+    lib = load()
+    s, ps = _dp(state)
+    n, pn = _dp(normal)
+    s1, ps1 = _dp(state1)
+    ev = np.zeros(3)
+    dec = np.zeros((n_dim + 2) * 3)
+    assert lib.oracle_characteristics(n_dim, ps, pn, ps1, ev.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                      dec.ctypes.data_as(ctypes.POINTER(ctypes.c_double))) == 0
+    return ev, dec.reshape(n_dim + 2, 3)
 
 
 class Oracle:
@@ -113,6 +154,9 @@ class Oracle:
 
     def compute_residual(self, params):
         self._chk(self.lib.oracle_compute_residual(ctypes.byref(self.desc), ctypes.byref(params)))
+
+    def set_art_visc_admis(self, char_speed):
+        self._chk(self.lib.oracle_set_art_visc_admis(ctypes.byref(self.desc), char_speed))
 
     def residual_norm(self):
         out = (ctypes.c_double * 3)()

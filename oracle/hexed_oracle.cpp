@@ -23,6 +23,7 @@
 #include <algorithm>
 #include <limits>
 #include <vector>
+#include <type_traits>
 #include "../include/hexed_gpu.h"
 #include "../hexed_gb300/csrc/basis_tables.h"
 
@@ -1014,6 +1015,80 @@ struct K
     refine(true, false, false);
   }
 
+  // Stab_art_visc (src/stabilizing_art_visc.cpp:26-60) for one element: the uncertainty
+  double stab_uncert(int e, double char_speed) const
+  {
+    const double* state = elem(e);
+    double qw[nq], fw[nfq], proj[RS];
+    for (int q = 0; q < nq; ++q) {
+      double p = 1.;
+      for (int d = 0; d < ND; ++d) p *= t.weight[(q/ipow(RS, ND - 1 - d))%RS];
+      qw[q] = p;
+    }
+    for (int r = 0; r < nfq; ++r) {
+      double p = 1.;
+      for (int d = 0; d < ND - 1; ++d) p *= t.weight[(r/ipow(RS, ND - 2 - d))%RS];
+      fw[r] = p;
+    }
+    for (int i = 0; i < RS; ++i) proj[i] = t.ortho[(RS - 1)*RS + i]*t.weight[i];
+    double iv[nq];
+    double norm_sq = 0;
+    for (int q = 0; q < nq; ++q) {
+      iv[q] = 1./state[ND*nq + q];
+      norm_sq += iv[q]*iv[q]*qw[q];
+    }
+    double nonsmooth = 0;
+    for (int d = 0; d < ND; ++d) {
+      for (int r = 0; r < nfq; ++r) {
+        double dot = 0.;
+        for (int i = 0; i < RS; ++i) dot += iv[row_qpoint(d, r, i)]*proj[i];
+        nonsmooth += dot*dot*fw[r];
+      }
+    }
+    nonsmooth /= norm_sq*ND;
+    const double ramp_center = -4.25*std::log(RS - 1)/std::log(10);
+    const double half_width = 0.5;
+    double indicator = std::log(nonsmooth)/std::log(10);
+    if (indicator <= ramp_center - half_width) indicator = 0;
+    else if (indicator < ramp_center + half_width)
+      indicator = .5*(1 + std::sin(M_PI*(indicator - ramp_center)/2/half_width));
+    else indicator = 1;
+    return (RS - 1)*char_speed*m.nom_size[e]*indicator;
+  }
+
+  // Solver::set_art_visc_admis (src/Solver.cpp:636-658): uncertainty, vertex maximum
+  // (share_vertex_data with Vertex::vector_max), multilinear interpolation of the vertex
+  // values to the qpoints (Gauss_lobatto(2).interpolate + hypercube_matvec) into the
+  // Laplacian AV row.
+  void set_art_visc_admis(double char_speed) const
+  {
+    std::vector<double> unc(n_elem());
+    #pragma omp parallel for
+    for (int e = 0; e < n_elem(); ++e) unc[e] = stab_uncert(e, char_speed);
+    std::vector<double> vmax(m.n_vert, -std::numeric_limits<double>::infinity());
+    for (int e = 0; e < n_elem(); ++e)
+      for (int v = 0; v < nvert; ++v) {
+        double& x = vmax[m.vert_id[e*nvert + v]];
+        x = std::max(x, unc[e]);
+      }
+    #pragma omp parallel for
+    for (int e = 0; e < n_elem(); ++e) {
+      double* lap = elem(e) + (nv + 2)*nq;
+      for (int q = 0; q < nq; ++q) {
+        double vals[nvert];
+        for (int v = 0; v < nvert; ++v) vals[v] = vmax[m.vert_id[e*nvert + v]];
+        // contract the last reference dimension first, as hypercube_matvec does
+        int n = nvert;
+        for (int d = ND - 1; d >= 0; --d) {
+          const double x = t.node[(q/ipow(RS, ND - 1 - d))%RS];
+          for (int i = 0; i < n/2; ++i) vals[i] = (1. - x)*vals[2*i] + x*vals[2*i + 1];
+          n /= 2;
+        }
+        lap[q] = vals[0];
+      }
+    }
+  }
+
   // integral_field of Physical_residual^2 (src/Solver.cpp:1113-1131, src/Qpoint_func.cpp:37-45)
   void residual_norm(double* out) const
   {
@@ -1089,8 +1164,48 @@ int oracle_compute_navier_stokes(const hexed_mesh_desc* m, double dt, int stage,
 int oracle_max_dt(const hexed_mesh_desc* m, double msc, double msd, int local_time, int viscous,
                   const hexed_transport* visc, const hexed_transport* cond, double* out)
 { return dispatch(m, [&](auto& k) { *out = k.max_dt(viscous, msc, msd, local_time, *visc, *cond); }); }
+int oracle_set_art_visc_admis(const hexed_mesh_desc* m, double char_speed)
+{
+  if (!m || m->n_vert <= 0 || !m->vert_id) return HEXED_ERR_INVALID;
+  return dispatch(m, [&](auto& k) { k.set_art_visc_admis(char_speed); });
+}
 int oracle_residual_norm(const hexed_mesh_desc* m, double* out)
 { return dispatch(m, [&](auto& k) { k.residual_norm(out); }); }
+
+// Unit-level entry points for the restated reference tests.
+// Derivative::operator() on one row (include/Derivative.hpp:50-55)
+int oracle_derivative(int rs, const double* f, const double* fb, double* out)
+{
+  hexed_mesh_desc m{};
+  m.n_dim = 2; m.row_size = rs;
+  return dispatch(&m, [&](auto& k) { k.derivative(f, fb, out); });
+}
+
+// Face_permutation::match_faces index map (include/Spatial.hpp:85-129)
+int oracle_perm_index(int nd, int rs, int dir, int q)
+{
+  int r = -1;
+  hexed_mesh_desc m{};
+  m.n_dim = nd; m.row_size = rs;
+  dispatch(&m, [&](auto& k) { r = k.perm_index(dir, q); });
+  return r;
+}
+
+// Characteristics (include/pde.hpp:182-256): eigenvalues [3] and decomposition [nv][3]
+int oracle_characteristics(int nd, const double* state, const double* normal, const double* state1,
+                           double* eigvals, double* decomp)
+{
+  hexed_mesh_desc m{};
+  m.n_dim = nd; m.row_size = 2;
+  return dispatch(&m, [&](auto& k) {
+    using KT = std::remove_reference_t<decltype(k)>;
+    typename KT::Characteristics ch(state, normal);
+    for (int i = 0; i < 3; ++i) eigvals[i] = ch.vals[i];
+    double d[KT::nv][3];
+    ch.decomp(state1, d);
+    for (int r = 0; r < KT::nv; ++r) for (int c = 0; c < 3; ++c) decomp[r*3 + c] = d[r][c];
+  });
+}
 
 // Solver::update (src/Solver.cpp:834-886); returns the last dt through *out_dt
 int oracle_update(const hexed_mesh_desc* m, const hexed_update_params* p, double* out_dt)
@@ -1100,6 +1215,8 @@ int oracle_update(const hexed_mesh_desc* m, const hexed_update_params* p, double
     for (int i_flow = 0; i_flow < p->flow_iters; ++i_flow) {
       double max_cheby = chebyshev_step(p->n_cheby_flow, p->n_cheby_flow - 1);
       for (int i_cheby = 0; i_cheby < p->n_cheby_flow; ++i_cheby) {
+        // Case.cpp:432: set_art_visc_admis before each update when diffusive_admissibility is on
+        if (p->av_admis_char_speed > 0 && i_flow == 0 && i_cheby == 0) k.set_art_visc_admis(p->av_admis_char_speed);
         double nominal = std::min(k.max_dt(p->use_ldg, p->max_safety/max_cheby, p->max_safety, p->local_time,
                                            p->visc, p->cond), p->max_time_step);
         dt = nominal*chebyshev_step(p->n_cheby_flow, i_cheby);

@@ -99,3 +99,33 @@ def compare_arenas(a, b, tol=FP64_TOL, what=("elem", "rcache", "face", "bc_cache
 def _rel(x, y, axis):
     from conftest import rel_err
     return rel_err(x, y, axis)
+
+
+def all_directions(nd):
+    """Every Connection_direction a deformed connection can have (faces of equal sign along
+    the same dimension are forbidden, src/Accessible_mesh.cpp:181-185)."""
+    import itertools
+    from hexed_gb300.mesh import pack_dir
+    for i0, i1 in itertools.product(range(nd), repeat=2):
+        for s0, s1 in itertools.product(range(2), repeat=2):
+            if i0 == i1 and s0 == s1:
+                continue
+            yield pack_dir(i0, i1, s0, s1)
+
+
+def rotated_pair_case(nd, rs, direction, kind=abi.BC_RIEMANN, seed=0):
+    """Two deformed elements joined through a connection of the given direction (so the
+    second element's face data must be permuted), smoothly warped, all other faces on
+    boundary conditions."""
+    from hexed_gb300.mesh import general_mesh, oriented_neighbor
+    p0, p1 = oriented_neighbor(nd, direction)
+    verts = np.stack([p0, p1])
+    warp = 0.08 * np.sin(1.3 * verts[..., ::-1] + 0.4)
+    verts = verts + warp
+    i0, i1, s0, s1 = direction & 3, (direction >> 2) & 3, (direction >> 4) & 1, (direction >> 5) & 1
+    bounds = [(0, d, s, 0) for d in range(nd) for s in range(2) if (d, s) != (i0, s0)]
+    bounds += [(1, d, s, 0) for d in range(nd) for s in range(2) if (d, s) != (i1, s1)]
+    fs = problems.freestream_state(nd, 0.3, 7., 1.2, 1e5)
+    spec = bc_spec(kind, freestream=fs, pressure=0.9e5)
+    ar = general_mesh(nd, rs, verts, [1., 1.], [True, True], [(0, 1, i0, i1, s0, s1)], bounds, [spec])
+    return smooth_state(ar, seed)
