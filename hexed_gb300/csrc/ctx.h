@@ -37,11 +37,20 @@ struct OpsTable {
   void (*max_dt)(Ctx&, double msc, double msd, int local_time, int viscous, const hexed_transport& visc,
                  const hexed_transport& cond, double max_time_step, double cheby);
   void (*refine)(Ctx&, bool prolong, bool scale, bool offset);
-  void (*write_face)(Ctx&);
+  void (*write_face)(Ctx&, int e_begin, int n_elem);
   void (*bc_state)(Ctx&);
   void (*bc_flux)(Ctx&);
   void (*residual_norm)(Ctx&, double* d_out);
   void (*set_art_visc_admis)(Ctx&, double char_speed);
+  void (*segment_residual_norms)(Ctx&, int n_seg, const int* d_begin, const int* d_count, double* d_out);
+};
+
+// A captured multi-update sequence and the inputs it was captured for.
+struct GraphCache {
+  bool valid = false;
+  cudaGraphExec_t exec = nullptr;
+  hexed_update_params params;
+  int n = 0, n_car = 0, n_car_con = 0, n_bc_con = 0;
 };
 
 struct Ctx {
@@ -66,6 +75,20 @@ struct Ctx {
   double* d_norm;        // residual norm output [3]
   double* h_pinned;      // pinned host staging for scalars [8]
   Profiler* prof;
+  // sizes of the arena arrays (the n_* counts above are the active prefix the kernels see)
+  int cap_car, cap_car_con, cap_bc_con;
+  // per-call scratch of the segmented residual norms
+  int seg_capacity;
+  int* seg_table;        // device [2][seg_capacity]
+  double* seg_out;       // device [3*seg_capacity]
+  GraphCache* graph;
+  bool capturing;
+  // Jacobian determinant reciprocal [n_def][nq] (both forms)
+  double* inv_det;
+  // mixed form: FP32 face traces, residual cache and metric-normal copies, and the reference
+  // state the traces are stored against (rho0, ener0 = P0/(gamma-1), means of the initial state)
+  float* face_f; float* rcache_f; float* nrm_f; float* face_nrml_f; float* def_con_nrml_f; float* bc_nrml_f;
+  double rho0, ener0;
 };
 
 // Bracket one launch with timing events when profiling is enabled.

@@ -9,6 +9,7 @@
 #include <cstdarg>
 #include <string>
 #include <vector>
+#include <algorithm>
 #include "ctx.h"
 #include "kernels.cuh"
 #include "basis_tables.h"
@@ -138,12 +139,15 @@ int validate(const hexed_mesh_desc* d)
 
 size_t array_count(const Ctx* c, int which)
 {
-  const size_t n_elem = c->n_car + c->n_def;
+  const size_t n_elem = c->cap_car + c->n_def;
   switch (which) {
     case HEXED_ARRAY_ELEM: return n_elem*(c->nv + 3)*c->nq;
     case HEXED_ARRAY_RCACHE: return n_elem*c->nv*c->nq;
     case HEXED_ARRAY_FACE: return (size_t)c->n_slot*2*c->nv*c->nfq;
-    case HEXED_ARRAY_BC_CACHE: return (size_t)c->n_bc_con*2*c->nv*c->nfq;
+    case HEXED_ARRAY_BC_CACHE: return (size_t)c->cap_bc_con*2*c->nv*c->nfq;
+    case HEXED_ARRAY_NOM_SIZE: return n_elem;
+    case HEXED_ARRAY_VERT_TSS: return n_elem << c->nd;
+    case HEXED_ARRAY_BC_NRML: return (size_t)c->cap_bc_con*c->nd*c->nfq;
   }
   return 0;
 }
@@ -155,8 +159,87 @@ double* array_ptr(Ctx* c, int which)
     case HEXED_ARRAY_RCACHE: return c->rcache;
     case HEXED_ARRAY_FACE: return c->face;
     case HEXED_ARRAY_BC_CACHE: return c->bc_cache;
+    case HEXED_ARRAY_NOM_SIZE: return c->nom_size;
+    case HEXED_ARRAY_VERT_TSS: return c->vert_tss;
+    case HEXED_ARRAY_BC_NRML: return c->bc_nrml;
   }
   return nullptr;
+}
+
+// FP32 device storage of an arena array in the mixed form (face traces, residual cache).
+float* f32_array(Ctx* c, int which)
+{
+  if (c->precision != HEXED_MIXED) return nullptr;
+  if (which == HEXED_ARRAY_FACE) return c->face_f;
+  if (which == HEXED_ARRAY_RCACHE) return c->rcache_f;
+  return nullptr;
+}
+
+// Host <-> device copy of entries [offset, offset + count) of an arena array; FP32-stored
+// arrays go through a double staging buffer and a conversion kernel.
+int transfer(Ctx* c, int which, long offset, long count, double* host, bool to_device)
+{
+  const long n = (long)array_count(c, which);
+  double* d = array_ptr(c, which);
+  float* f = f32_array(c, which);
+  if (offset < 0 || count < 0 || offset + count > n || (count && !host))
+    return fail(HEXED_ERR_INVALID, "range [%ld, %ld) outside array %d of %ld entries", offset, offset + count, which, n);
+  if (count == 0) return HEXED_OK;
+  if (!d && !f) return fail(HEXED_ERR_INVALID, "array %d is not allocated", which);
+  if (f) {
+    double* tmp = nullptr;
+    HX_CUDA(cudaMalloc((void**)&tmp, count*sizeof(double)));
+    const int grid = int(std::min<long>((count + 255)/256, 152*16));
+    cudaError_t err;
+    if (to_device) {
+      cudaMemcpyAsync(tmp, host, count*sizeof(double), cudaMemcpyHostToDevice, c->stream);
+      hx::k_narrow<<<grid, 256, 0, c->stream>>>(tmp, f + offset, count);
+    } else {
+      hx::k_widen<<<grid, 256, 0, c->stream>>>(f + offset, tmp, count);
+      cudaMemcpyAsync(host, tmp, count*sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    }
+    err = cudaStreamSynchronize(c->stream);
+    cudaFree(tmp);
+    if (err != cudaSuccess) return fail(HEXED_ERR_CUDA, "transfer: %s", cudaGetErrorString(err));
+    return HEXED_OK;
+  }
+  if (to_device) HX_CUDA(cudaMemcpyAsync(d + offset, host, count*sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  else HX_CUDA(cudaMemcpyAsync(host, d + offset, count*sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (to_device && which == HEXED_ARRAY_BC_NRML && c->bc_nrml_f) {
+    // keep the mixed form's FP32 copy of the boundary normals in step
+    hx::k_narrow<<<int(std::min<long>((count + 255)/256, 152*16)), 256, 0, c->stream>>>(d + offset, c->bc_nrml_f + offset, count);
+  }
+  HX_CUDA(cudaStreamSynchronize(c->stream));
+  return HEXED_OK;
+}
+
+// FP32 copy of a device double array (mixed form).
+int narrow_copy(Ctx* c, const double* src, float** dst, long n)
+{
+  *dst = nullptr;
+  if (n == 0) return HEXED_OK;
+  HX_CUDA(cudaMalloc((void**)dst, n*sizeof(float)));
+  hx::k_narrow<<<int(std::min<long>((n + 255)/256, 152*16)), 256, 0, c->stream>>>(src, *dst, n);
+  HX_LAUNCHED();
+  return HEXED_OK;
+}
+
+// Rows of a connection array checked against the arena before upload.
+int validate_int_rows(const Ctx* c, int which, const int* rows, long count)
+{
+  auto slot_ok = [&](int s) { return s >= 0 && s < c->n_slot; };
+  for (long i = 0; i < count; ++i) {
+    if (which == HEXED_INT_CAR_CON) {
+      const int* r = rows + 3*i;
+      if (!slot_ok(r[0]) || !slot_ok(r[1]) || r[2] < 0 || r[2] >= c->nd)
+        return fail(HEXED_ERR_INVALID, "Cartesian connection row %ld out of range", i);
+    } else {
+      const int* r = rows + 4*i;
+      if (!slot_ok(r[0]) || !slot_ok(r[1]) || (r[2] & 3) >= c->nd || (r[2] >> 3) || r[3] < 0 || r[3] >= c->n_bc_spec)
+        return fail(HEXED_ERR_INVALID, "boundary connection row %ld out of range", i);
+    }
+  }
+  return HEXED_OK;
 }
 
 int check_ctx(hexed_gpu_ctx* ctx) { return ctx ? HEXED_OK : fail(HEXED_ERR_INVALID, "null context"); }
@@ -179,7 +262,7 @@ namespace hx {
 ProfScope::ProfScope(Ctx& ctx, const char* name) : c{ctx}, pair{-1}
 {
   Profiler* p = c.prof;
-  if (!p || !p->enabled || p->n_pairs >= Profiler::max_events/2) return;
+  if (!p || !p->enabled || c.capturing || p->n_pairs >= Profiler::max_events/2) return;
   int idx = -1;
   for (int i = 0; i < p->n_names; ++i) if (std::strcmp(p->names[i], name) == 0) { idx = i; break; }
   if (idx < 0) {
@@ -230,6 +313,7 @@ int hexed_gpu_create(const hexed_mesh_desc* d, int precision, hexed_gpu_ctx** ou
   c->n_car = d->n_car_elem; c->n_def = d->n_def_elem; c->n_slot = d->n_slot;
   c->n_car_con = d->n_car_con; c->n_def_con = d->n_def_con; c->n_bc_con = d->n_bc_con;
   c->n_ref = d->n_ref_face; c->n_bc_spec = d->n_bc_spec;
+  c->cap_car = c->n_car; c->cap_car_con = c->n_car_con; c->cap_bc_con = c->n_bc_con;
   int nq = 1; for (int i = 0; i < c->nd; ++i) nq *= c->rs;
   c->nq = nq; c->nfq = nq/c->rs; c->nv = c->nd + 2;
   c->tables = host_tables(c->rs);
@@ -243,8 +327,15 @@ int hexed_gpu_create(const hexed_mesh_desc* d, int precision, hexed_gpu_ctx** ou
   };
   HX_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   up(&c->elem, d->elem, n_elem*(c->nv + 3)*c->nq, "elem");
-  up(&c->rcache, d->rcache, n_elem*c->nv*c->nq, "rcache");
-  up(&c->face, d->face, (size_t)c->n_slot*2*c->nv*c->nfq, "face");
+  if (precision == HEXED_FP64) {
+    up(&c->rcache, d->rcache, n_elem*c->nv*c->nq, "rcache");
+    up(&c->face, d->face, (size_t)c->n_slot*2*c->nv*c->nfq, "face");
+  } else if (!d->rcache || !d->face) {
+    st = fail(HEXED_ERR_INVALID, "arena arrays `rcache` / `face` are null");
+  } else if (cudaMalloc((void**)&c->rcache_f, n_elem*c->nv*c->nq*sizeof(float)) != cudaSuccess ||
+             cudaMalloc((void**)&c->face_f, (size_t)c->n_slot*2*c->nv*c->nfq*sizeof(float)) != cudaSuccess) {
+    st = fail(HEXED_ERR_ALLOC, "trace allocation failed");
+  }
   up(&c->nom_size, d->nom_size, n_elem, "nom_size");
   up(&c->vert_tss, d->vert_tss, n_elem*nvert, "vert_tss");
   up(&c->jac, d->jac, (size_t)c->n_def*(nd*nd + 1)*c->nq, "jac");
@@ -263,6 +354,38 @@ int hexed_gpu_create(const hexed_mesh_desc* d, int precision, hexed_gpu_ctx** ou
     if (st == HEXED_OK && (cudaMalloc((void**)&c->uncert, n_elem*sizeof(double)) != cudaSuccess ||
                            cudaMalloc((void**)&c->vmax, c->n_vert*sizeof(double)) != cudaSuccess))
       st = fail(HEXED_ERR_ALLOC, "vertex scratch allocation failed");
+  }
+  if (st != HEXED_OK) { hexed_gpu_destroy(c); return st; }
+  if (precision == HEXED_MIXED) {
+    // staged FP32 traces and residual cache; FP32 copies of the metric normals
+    if (!st) st = transfer(c, HEXED_ARRAY_RCACHE, 0, (long)array_count(c, HEXED_ARRAY_RCACHE), d->rcache, true);
+    if (!st) st = transfer(c, HEXED_ARRAY_FACE, 0, (long)array_count(c, HEXED_ARRAY_FACE), d->face, true);
+    if (!st) st = narrow_copy(c, c->jac, &c->nrm_f, (long)c->n_def*(nd*nd + 1)*c->nq);
+    if (!st) st = narrow_copy(c, c->face_nrml, &c->face_nrml_f, (long)c->n_def*2*nd*nd*c->nfq);
+    if (!st) st = narrow_copy(c, c->def_con_nrml, &c->def_con_nrml_f, (long)c->n_def_con*nd*c->nfq);
+    if (!st) st = narrow_copy(c, c->bc_nrml, &c->bc_nrml_f, (long)c->n_bc_con*nd*c->nfq);
+    // reference state: mean density and mean pressure of the initial state
+    double rho_sum = 0., p_sum = 0.;
+    const size_t nq_ = c->nq, nv_ = c->nv;
+    for (size_t e = 0; e < n_elem; ++e) {
+      const double* st_e = d->elem + e*(nv_ + 3)*nq_;
+      for (size_t q = 0; q < nq_; ++q) {
+        double rho = st_e[nd*nq_ + q], kin = 0.;
+        for (size_t k = 0; k < nd; ++k) kin += st_e[k*nq_ + q]*st_e[k*nq_ + q];
+        rho_sum += rho;
+        p_sum += (1.4 - 1.)*(st_e[(nd + 1)*nq_ + q] - .5*kin/rho);
+      }
+    }
+    c->rho0 = rho_sum/double(n_elem*nq_);
+    c->ener0 = p_sum/double(n_elem*nq_)/(1.4 - 1.);
+  }
+  if (!st && c->n_def) {
+    if (cudaMalloc((void**)&c->inv_det, (size_t)c->n_def*c->nq*sizeof(double)) != cudaSuccess) {
+      st = fail(HEXED_ERR_ALLOC, "determinant allocation failed");
+    } else {
+      hx::k_inv_det<<<int(std::min<long>(((long)c->n_def*c->nq + 255)/256, 152*16)), 256, 0, c->stream>>>(
+          c->jac, c->inv_det, c->n_def, (int)c->nq, (int)(nd*nd));
+    }
   }
   if (st != HEXED_OK) { hexed_gpu_destroy(c); return st; }
   c->max_partials = 152*16*8;
@@ -287,8 +410,14 @@ int hexed_gpu_destroy(hexed_gpu_ctx* c)
   if (c->stream) cudaStreamSynchronize(c->stream);
   void* ptrs[] = {c->elem, c->rcache, c->face, c->nom_size, c->vert_tss, c->jac, c->face_nrml, c->car_con,
                   c->def_con, c->def_con_nrml, c->bc_con, c->bc_nrml, c->bc_cache, c->ref_face, c->bc_spec,
-                  c->scalars, c->partials, c->status, c->d_norm, c->vert_id, c->uncert, c->vmax};
+                  c->scalars, c->partials, c->status, c->d_norm, c->vert_id, c->uncert, c->vmax,
+                  c->seg_table, c->seg_out, c->inv_det, c->face_f, c->rcache_f, c->nrm_f, c->face_nrml_f,
+                  c->def_con_nrml_f, c->bc_nrml_f};
   for (void* p : ptrs) if (p) cudaFree(p);
+  if (c->graph) {
+    if (c->graph->exec) cudaGraphExecDestroy(c->graph->exec);
+    delete c->graph;
+  }
   if (c->h_pinned) cudaFreeHost(c->h_pinned);
   if (c->prof) {
     if (c->prof->created) for (auto& e : c->prof->events) cudaEventDestroy(e);
@@ -302,25 +431,13 @@ int hexed_gpu_destroy(hexed_gpu_ctx* c)
 int hexed_gpu_upload(hexed_gpu_ctx* c, int which, const double* host)
 {
   if (int st = check_ctx(c)) return st;
-  double* dst = array_ptr(c, which);
-  size_t n = array_count(c, which);
-  if (n == 0) return HEXED_OK;
-  if (!dst || !host) return fail(HEXED_ERR_INVALID, "bad array %d or null host pointer", which);
-  HX_CUDA(cudaMemcpyAsync(dst, host, n*sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  HX_CUDA(cudaStreamSynchronize(c->stream));
-  return HEXED_OK;
+  return transfer(c, which, 0, (long)array_count(c, which), const_cast<double*>(host), true);
 }
 
 int hexed_gpu_download(hexed_gpu_ctx* c, int which, double* host)
 {
   if (int st = check_ctx(c)) return st;
-  double* src = array_ptr(c, which);
-  size_t n = array_count(c, which);
-  if (n == 0) return HEXED_OK;
-  if (!src || !host) return fail(HEXED_ERR_INVALID, "bad array %d or null host pointer", which);
-  HX_CUDA(cudaMemcpyAsync(host, src, n*sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-  HX_CUDA(cudaStreamSynchronize(c->stream));
-  return HEXED_OK;
+  return transfer(c, which, 0, (long)array_count(c, which), host, false);
 }
 
 int hexed_gpu_synchronize(hexed_gpu_ctx* c)
@@ -389,7 +506,17 @@ int hexed_gpu_compute_restrict(hexed_gpu_ctx* c, int scale, int offset)
 int hexed_gpu_compute_write_face(hexed_gpu_ctx* c)
 {
   if (int st = check_ctx(c)) return st;
-  c->ops->write_face(*c);
+  c->ops->write_face(*c, 0, c->n_car + c->n_def);
+  HX_LAUNCHED();
+  return HEXED_OK;
+}
+
+int hexed_gpu_write_face_range(hexed_gpu_ctx* c, int elem_begin, int elem_count)
+{
+  if (int st = check_ctx(c)) return st;
+  if (elem_begin < 0 || elem_count < 0 || (long)elem_begin + elem_count > (long)c->cap_car + c->n_def)
+    return fail(HEXED_ERR_INVALID, "elements [%d, %ld) outside the arena", elem_begin, (long)elem_begin + elem_count);
+  c->ops->write_face(*c, elem_begin, elem_count);
   HX_LAUNCHED();
   return HEXED_OK;
 }
@@ -419,13 +546,14 @@ int hexed_gpu_apply_flux_bcs(hexed_gpu_ctx* c)
   return HEXED_OK;
 }
 
-int hexed_gpu_update(hexed_gpu_ctx* c, const hexed_update_params* p, double* out_dt)
+namespace {
+// Enqueues one Solver::update (src/Solver.cpp:834-886) on the context's stream.
+int enqueue_update(hexed_gpu_ctx* c, const hexed_update_params* p)
 {
-  if (int st = check_ctx(c)) return st;
-  if (!p || p->n_cheby_flow < 1 || p->flow_iters < 0) return fail(HEXED_ERR_INVALID, "bad update parameters");
   if (p->av_admis_char_speed > 0) {
     // Case.cpp:432: set_art_visc_admis before the update when diffusive_admissibility is on
-    if (int st = hexed_gpu_set_art_visc_admis(c, p->av_admis_char_speed)) return st;
+    if (c->n_vert <= 0) return fail(HEXED_ERR_INVALID, "artificial viscosity needs the arena's vertex table");
+    c->ops->set_art_visc_admis(*c, p->av_admis_char_speed);
   }
   const double max_cheby = chebyshev_step(p->n_cheby_flow, p->n_cheby_flow - 1);
   for (int i_flow = 0; i_flow < p->flow_iters; ++i_flow) {
@@ -438,6 +566,136 @@ int hexed_gpu_update(hexed_gpu_ctx* c, const hexed_update_params* p, double* out
       }
     }
   }
+  return HEXED_OK;
+}
+
+bool same_params(const hexed_update_params& a, const hexed_update_params& b)
+{
+  return std::memcmp(&a, &b, sizeof(a)) == 0;
+}
+} // namespace
+
+int hexed_gpu_update_n(hexed_gpu_ctx* c, const hexed_update_params* p, int n, int use_graph)
+{
+  if (int st = check_ctx(c)) return st;
+  if (!p || p->n_cheby_flow < 1 || p->flow_iters < 0 || n < 0) return fail(HEXED_ERR_INVALID, "bad update parameters");
+  if (!use_graph) {
+    for (int i = 0; i < n; ++i) if (int st = enqueue_update(c, p)) return st;
+    HX_LAUNCHED();
+    return HEXED_OK;
+  }
+  if (!c->graph) c->graph = new hx::GraphCache();
+  hx::GraphCache& g = *c->graph;
+  if (!(g.valid && g.n == n && same_params(g.params, *p) && g.n_car == c->n_car && g.n_car_con == c->n_car_con &&
+        g.n_bc_con == c->n_bc_con)) {
+    if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
+    g.valid = false;
+    // one eager update first so every kernel's attributes are set outside the capture
+    if (int st = enqueue_update(c, p)) return st;
+    HX_CUDA(cudaStreamSynchronize(c->stream));
+    cudaGraph_t graph = nullptr;
+    HX_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    c->capturing = true;
+    int st = HEXED_OK;
+    for (int i = 0; i < n && st == HEXED_OK; ++i) st = enqueue_update(c, p);
+    c->capturing = false;
+    cudaError_t err = cudaStreamEndCapture(c->stream, &graph);
+    if (st != HEXED_OK) { if (graph) cudaGraphDestroy(graph); return st; }
+    if (err != cudaSuccess) return fail(HEXED_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(err));
+    err = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (err != cudaSuccess) return fail(HEXED_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(err));
+    g.valid = true; g.n = n; g.params = *p; g.n_car = c->n_car; g.n_car_con = c->n_car_con; g.n_bc_con = c->n_bc_con;
+    n -= 1;   // the eager update above counts
+    if (n == 0) return HEXED_OK;
+    // replay the graph for the remaining updates in whole multiples, the rest eagerly
+    for (int i = 0; i < n % g.n; ++i) if (int s2 = enqueue_update(c, p)) return s2;
+    for (int i = 0; i < n/g.n; ++i) HX_CUDA(cudaGraphLaunch(g.exec, c->stream));
+    HX_LAUNCHED();
+    return HEXED_OK;
+  }
+  HX_CUDA(cudaGraphLaunch(g.exec, c->stream));
+  return HEXED_OK;
+}
+
+int hexed_gpu_write_range(hexed_gpu_ctx* c, int which, long offset, long count, const double* host)
+{
+  if (int st = check_ctx(c)) return st;
+  return transfer(c, which, offset, count, const_cast<double*>(host), true);
+}
+
+int hexed_gpu_read_range(hexed_gpu_ctx* c, int which, long offset, long count, double* host)
+{
+  if (int st = check_ctx(c)) return st;
+  return transfer(c, which, offset, count, host, false);
+}
+
+int hexed_gpu_write_int_range(hexed_gpu_ctx* c, int which, long offset, long count, const int* host)
+{
+  if (int st = check_ctx(c)) return st;
+  const int width = which == HEXED_INT_CAR_CON ? 3 : which == HEXED_INT_BC_CON ? 4 : 0;
+  const long rows = which == HEXED_INT_CAR_CON ? c->cap_car_con : c->cap_bc_con;
+  int* dst = which == HEXED_INT_CAR_CON ? c->car_con : c->bc_con;
+  if (!width || offset < 0 || count < 0 || offset + count > rows || (count && !host))
+    return fail(HEXED_ERR_INVALID, "rows [%ld, %ld) outside int array %d of %ld rows", offset, offset + count, which, rows);
+  if (int st = validate_int_rows(c, which, host, count)) return st;
+  if (count) HX_CUDA(cudaMemcpyAsync(dst + offset*width, host, count*width*sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  HX_CUDA(cudaStreamSynchronize(c->stream));
+  return HEXED_OK;
+}
+
+int hexed_gpu_write_bc_spec(hexed_gpu_ctx* c, int index, const hexed_bc_spec* spec)
+{
+  if (int st = check_ctx(c)) return st;
+  if (!spec || index < 0 || index >= c->n_bc_spec) return fail(HEXED_ERR_INVALID, "bad boundary-condition index %d", index);
+  if (spec->kind < 0 || spec->kind > HEXED_BC_NO_SLIP) return fail(HEXED_ERR_INVALID, "unknown BC kind %d", spec->kind);
+  HX_CUDA(cudaMemcpyAsync(c->bc_spec + index, spec, sizeof(*spec), cudaMemcpyHostToDevice, c->stream));
+  HX_CUDA(cudaStreamSynchronize(c->stream));
+  return HEXED_OK;
+}
+
+int hexed_gpu_set_active(hexed_gpu_ctx* c, int n_car_elem, int n_car_con, int n_bc_con)
+{
+  if (int st = check_ctx(c)) return st;
+  if (c->n_def) return fail(HEXED_ERR_INVALID, "set_active applies to Cartesian-only arenas");
+  if (n_car_elem < 0 || n_car_elem > c->cap_car || n_car_con < 0 || n_car_con > c->cap_car_con || n_bc_con < 0 ||
+      n_bc_con > c->cap_bc_con)
+    return fail(HEXED_ERR_INVALID, "active sizes exceed the arena");
+  c->n_car = n_car_elem; c->n_car_con = n_car_con; c->n_bc_con = n_bc_con;
+  return HEXED_OK;
+}
+
+int hexed_gpu_segment_residual_norms(hexed_gpu_ctx* c, int n_seg, const int* elem_begin, const int* elem_count,
+                                     double* out)
+{
+  if (int st = check_ctx(c)) return st;
+  if (n_seg < 0 || (n_seg && (!elem_begin || !elem_count || !out))) return fail(HEXED_ERR_INVALID, "bad segment table");
+  if (n_seg == 0) return HEXED_OK;
+  for (int i = 0; i < n_seg; ++i)
+    if (elem_begin[i] < 0 || elem_count[i] < 1 || (long)elem_begin[i] + elem_count[i] > (long)c->n_car + c->n_def)
+      return fail(HEXED_ERR_INVALID, "segment %d outside the active elements", i);
+  if (n_seg > c->seg_capacity) {
+    if (c->seg_table) cudaFree(c->seg_table);
+    if (c->seg_out) cudaFree(c->seg_out);
+    c->seg_table = nullptr; c->seg_out = nullptr; c->seg_capacity = 0;
+    HX_CUDA(cudaMalloc((void**)&c->seg_table, 2*n_seg*sizeof(int)));
+    HX_CUDA(cudaMalloc((void**)&c->seg_out, 3*n_seg*sizeof(double)));
+    c->seg_capacity = n_seg;
+  }
+  HX_CUDA(cudaMemcpyAsync(c->seg_table, elem_begin, n_seg*sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  HX_CUDA(cudaMemcpyAsync(c->seg_table + n_seg, elem_count, n_seg*sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  c->ops->segment_residual_norms(*c, n_seg, c->seg_table, c->seg_table + n_seg, c->seg_out);
+  HX_LAUNCHED();
+  HX_CUDA(cudaMemcpyAsync(out, c->seg_out, 3*n_seg*sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  HX_CUDA(cudaStreamSynchronize(c->stream));
+  return HEXED_OK;
+}
+
+int hexed_gpu_update(hexed_gpu_ctx* c, const hexed_update_params* p, double* out_dt)
+{
+  if (int st = check_ctx(c)) return st;
+  if (!p || p->n_cheby_flow < 1 || p->flow_iters < 0) return fail(HEXED_ERR_INVALID, "bad update parameters");
+  if (int st = enqueue_update(c, p)) return st;
   HX_LAUNCHED();
   if (out_dt) {
     HX_CUDA(cudaMemcpyAsync(c->h_pinned, c->scalars + hx::SC_DT, sizeof(double), cudaMemcpyDeviceToHost, c->stream));

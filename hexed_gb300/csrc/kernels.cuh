@@ -42,24 +42,34 @@ struct Tab {
 };
 
 // Device view of the arena (include/hexed_gpu.h). `face` is stored as FaceT.
+// Device view of the arena. FaceT is the storage type of the face traces, the residual cache
+// and the metric normals the flux kernels read: double in the FP64 form; float in the mixed
+// form, where those arrays are FP32 copies (the FP64 metrics stay in `jac`, and the Jacobian
+// determinant enters the stage update through the FP64 `inv_det`).
 template <typename FaceT>
 struct Dev {
   int n_car, n_def, n_elem, n_slot, n_car_con, n_def_con, n_bc_con, n_ref;
   double* elem;
-  double* rcache;
+  FaceT* rcache;
   FaceT* face;
   const double* nom_size;
   const double* vert_tss;
-  const double* jac;
-  const double* face_nrml;
+  const double* jac;          // FP64 [n_def][nd*nd + 1][nq]
+  const double* inv_det;      // FP64 [n_def][nq], 1/det
+  const FaceT* nrm;           // [n_def][nd*nd + 1][nq], reference-level normals in FaceT
+  const FaceT* face_nrml;
   const int* car_con;
   const int* def_con;
-  const double* def_con_nrml;
+  const FaceT* def_con_nrml;
   const int* bc_con;
-  const double* bc_nrml;
+  const double* bc_nrml;      // FP64 boundary normals (boundary conditions)
+  const FaceT* bc_nrml_t;     // the same in FaceT (face flux)
   double* bc_cache;
   const int* ref_face;
   const hexed_bc_spec* bc_spec;
+  // Reference state of the mixed form: face traces hold rho - rho0 and E - ener0, and the
+  // momentum flux carries p - (gamma-1)*ener0. Zero in the FP64 form.
+  double rho0, ener0;
   double* scalars;       // [0] dt of the current stage, [1] raw max_dt, ...
   double* partials;      // per-block reduction scratch
   int* status;           // device-side error flags
@@ -303,9 +313,19 @@ struct LocalSmem {
                                 + ND*S::nv*S::nq         // s_f
                                 + (VISC ? ND*S::nv*S::nq : 0)   // s_g
                                 + ND*2*S::nv*S::nfq;     // s_bf
-  static constexpr size_t bytes = sizeof(STab<RS, R>) + sizeof(R)*(size_t)per_elem*S::epb + 16
-                                  + sizeof(double)*S::epb + 16;
+  static constexpr size_t bytes = sizeof(STab<RS, R>) + sizeof(R)*(size_t)per_elem*S::epb + 16;
 };
+
+// Offset form of the state used for face traces and derivatives: the mixed form subtracts the
+// reference density and energy (in double, before narrowing), so the FP32 values carry the
+// variation and not the large mean; the FP64 form keeps the state as it is (references 0).
+template <int ND, typename R, typename FaceT>
+__device__ __forceinline__ R offset_var(const Dev<FaceT>& m, int v, double x)
+{
+  if (v == ND) return R(x - m.rho0);
+  if (v == ND + 1) return R(x - m.ener0);
+  return R(x);
+}
 
 template <int ND, int RS, typename R, bool DEF, bool VISC, typename FaceT>
 __global__ void __launch_bounds__(Shape<ND, RS>::threads)
@@ -314,20 +334,18 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
 {
   using S = Shape<ND, RS>;
   constexpr int nq = S::nq, nfq = S::nfq, nv = S::nv, EPB = S::epb;
+  // Mixed form: the momentum flux carries p - P0 with P0 = (gamma-1)*ener0, the face traces
+  // the offset state. The P0*n parts of interior and face fluxes cancel by the discrete metric
+  // identity sum_d [D.n_d + lift.(n_face - B.n_d)] = 0 (free-stream preservation), so this is
+  // the same scheme up to roundoff, without the cancellation of p ~ P0 in float.
+  constexpr bool split = !std::is_same<FaceT, double>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   STab<RS, R>& st = *reinterpret_cast<STab<RS, R>*>(smem_raw);
   R* s_u = reinterpret_cast<R*>(smem_raw + (sizeof(STab<RS, R>) + 15)/16*16);
   R* s_f = s_u + EPB*nv*nq;
   R* s_g = s_f + EPB*ND*nv*nq;
   R* s_bf = s_g + (VISC ? EPB*ND*nv*nq : 0);
-  double* s_pref = reinterpret_cast<double*>(
-      (reinterpret_cast<uintptr_t>(s_bf + EPB*ND*2*nv*nfq) + 15)/16*16);
   st.load(tab);
-  // Mixed form: the momentum flux carries p - p_ref, with p_ref the element's pressure at
-  // its first qpoint (in double); p_ref*n is taken out of the face fluxes in double as well.
-  // The identity sum_d [D.n_d + lift.(n_face - B.n_d)] = 0 (free-stream preservation) makes
-  // this exact up to roundoff while removing the cancellation of p ~ p_ref in float.
-  constexpr bool split = !std::is_same<R, double>::value;
   const int le = threadIdx.x/nq;
   const int q = threadIdx.x%nq;
   const int e0 = e_begin + blockIdx.x*EPB;
@@ -339,6 +357,7 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
   const double* state_g = m.elem + (size_t)e*(nv + 3)*nq;
 
   R u[nv + 2];   // state + bulk AV + Laplacian AV (include/pde.hpp:79-84)
+  R up[nv];      // offset form of the state
   R p_rel = 0;
   R nrm[ND][ND]; // nrm[j][i] = comp.normal(j, i)
   #pragma unroll
@@ -347,26 +366,22 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
     for (int j = 0; j < ND; ++j) nrm[j][i] = (i == j) ? R(1) : R(0);
   if (active) {
     #pragma unroll
-    for (int v = 0; v < nv; ++v) u[v] = R(state_g[v*nq + q]);
+    for (int v = 0; v < nv; ++v) {
+      const double x = state_g[v*nq + q];
+      up[v] = offset_var<ND, R>(m, v, x);
+      u[v] = split ? (v == ND ? R(m.rho0) + up[v] : v == ND + 1 ? R(m.ener0) + up[v] : up[v]) : R(x);
+    }
     u[nv] = R(state_g[(nv + 1)*nq + q]);
     u[nv + 1] = R(state_g[(nv + 2)*nq + q]);
     if constexpr (split) {
-      // reference kinetic energy in float: p_ref below is formed from the same value, so
-      // p_rel + p_ref is the pressure whatever its rounding (one FP64 op per thread)
-      R kin_ref = 0;
-      #pragma unroll
-      for (int d = 0; d < ND; ++d) { R m0 = R(state_g[d*nq]); kin_ref += m0*m0; }
-      kin_ref *= R(.5)/R(state_g[ND*nq]);
-      const double e_ref = state_g[(nv - 1)*nq];
       R kin = 0;
       #pragma unroll
       for (int d = 0; d < ND; ++d) kin += u[d]*u[d];
       kin *= R(.5)/u[ND];
-      p_rel = R(heat_rat - 1.)*(R(state_g[(nv - 1)*nq + q] - e_ref) - (kin - kin_ref));
-      if (q == 0) s_pref[le] = (heat_rat - 1.)*(e_ref - double(kin_ref));
+      p_rel = R(heat_rat - 1.)*(up[ND + 1] - kin);
     }
     if constexpr (DEF) {
-      const double* nr = m.jac + (size_t)ed*(ND*ND + 1)*nq;
+      const FaceT* nr = m.nrm + (size_t)ed*(ND*ND + 1)*nq;
       #pragma unroll
       for (int i = 0; i < ND; ++i)
         #pragma unroll
@@ -375,6 +390,8 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
   } else {
     #pragma unroll
     for (int v = 0; v < nv + 2; ++v) u[v] = R(1);
+    #pragma unroll
+    for (int v = 0; v < nv; ++v) up[v] = R(0);
   }
   R* my_u = s_u + le*nv*nq;
   R* my_f = s_f + le*ND*nv*nq;
@@ -400,7 +417,7 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
     if constexpr (!DEF) {
       if (threadIdx.x < EPB*nq) {
         #pragma unroll
-        for (int v = 0; v < nv; ++v) my_u[v*nq + q] = u[v];
+        for (int v = 0; v < nv; ++v) my_u[v*nq + q] = up[v];
       }
       __syncthreads();
       // per-row boundary corrections: bf_s = face_state_s - B_s . row
@@ -442,8 +459,7 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
         }
       }
     } else {
-      const double* nr = m.jac + (size_t)ed*(ND*ND + 1)*nq;
-      const double* fn = m.face_nrml + (size_t)ed*2*ND*ND*nfq;
+      const FaceT* nr = m.nrm + (size_t)ed*(ND*ND + 1)*nq;
       #pragma unroll 1
       for (int d = 0; d < ND; ++d) {
         __syncthreads(); // previous use of s_f / s_bf finished
@@ -452,7 +468,7 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
           for (int j = 0; j < ND; ++j) {
             R nd_ = R(nr[(d*ND + j)*nq + q]);
             #pragma unroll
-            for (int v = 0; v < nv; ++v) my_f[(j*nv + v)*nq + q] = nd_*u[v];
+            for (int v = 0; v < nv; ++v) my_f[(j*nv + v)*nq + q] = nd_*up[v];
           }
         }
         __syncthreads();
@@ -470,7 +486,7 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
           #pragma unroll
           for (int i = 0; i < RS; ++i) { R x = row[i*stride]; a0 += st.bound[i]*x; a1 += st.bound[RS + i]*x; }
           const FaceT* fl = m.face + (size_t)(ee*2*ND + 2*d)*S::slot_dof + nv*nfq + v*nfq + r;
-          const double* fnr = m.face_nrml + ((size_t)eed*2*ND + 2*d)*ND*nfq + j*nfq + r;
+          const FaceT* fnr = m.face_nrml + ((size_t)eed*2*ND + 2*d)*ND*nfq + j*nfq + r;
           R b0 = R(fnr[0])*R(fl[0]);
           R b1 = R(fnr[ND*nfq])*R(fl[S::slot_dof]);
           R* bf = s_bf + ((l*ND + j)*2*nv)*nfq;
@@ -497,7 +513,6 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
           }
         }
       }
-      (void)fn;
     }
     __syncthreads(); // s_f / s_bf are reused below
   }
@@ -517,7 +532,7 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
     }
     if constexpr (VISC) {
       R g[nv][ND];
-      const R inv_det = DEF ? R(1./m.jac[((size_t)ed*(ND*ND + 1) + ND*ND)*nq + q]) : R(1);
+      const R inv_det = DEF ? R(m.inv_det[(size_t)ed*nq + q]) : R(1);
       #pragma unroll
       for (int v = 0; v < nv; ++v)
         #pragma unroll
@@ -550,22 +565,8 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
       for (int i = 0; i < RS; ++i) { R x = row[i*stride]; a0 += st.bound[i]*x; a1 += st.bound[RS + i]*x; }
       FaceT* fl = m.face + (size_t)(ee*2*ND + 2*d)*S::slot_dof + v*nfq + r;
       R* bf = s_bf + ((l*ND + d)*2*nv)*nfq;
-      R fb0, fb1;
-      if (split && v < ND) {
-        double n0 = (v == d) ? 1. : 0., n1 = n0;
-        if constexpr (DEF) {
-          const double* fnr = m.face_nrml + ((size_t)(ee - m.n_car)*2*ND + 2*d)*ND*nfq + v*nfq + r;
-          n0 = fnr[0];
-          n1 = fnr[ND*nfq];
-        }
-        fb0 = R(double(fl[0]) - s_pref[l]*n0);
-        fb1 = R(double(fl[S::slot_dof]) - s_pref[l]*n1);
-      } else {
-        fb0 = R(fl[0]);
-        fb1 = R(fl[S::slot_dof]);
-      }
-      bf[v*nfq + r] = fb0 - a0;
-      bf[(nv + v)*nfq + r] = fb1 - a1;
+      bf[v*nfq + r] = R(fl[0]) - a0;
+      bf[(nv + v)*nfq + r] = R(fl[S::slot_dof]) - a1;
       if constexpr (VISC) {
         const R* rg = s_g + ((l*ND + d)*nv + v)*nq + off;
         R g0 = 0, g1 = 0;
@@ -634,29 +635,41 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
     }
   }
 
-  // ---- stage update (Spatial.hpp:484-503), in double
+  // ---- stage update (Spatial.hpp:484-503): the state accumulates in double
   if (active) {
     const double dt = m.scalars[SC_DT];
     const double update_coef = stage ? dt*tab.step_ratio : dt;
     double* st_w = m.elem + (size_t)e*(nv + 3)*nq;
-    double* rc = m.rcache + (size_t)e*nv*nq;
+    FaceT* rc = m.rcache + (size_t)e*nv*nq;
     double mult = update_coef*st_w[nv*nq + q]*inv_dpos;
-    if constexpr (DEF) mult *= 1./m.jac[((size_t)ed*(ND*ND + 1) + ND*ND)*nq + q];
+    if constexpr (DEF) mult *= m.inv_det[(size_t)ed*nq + q];
     #pragma unroll
     for (int v = 0; v < nv; ++v) {
-      double uu = double(rate[v]);
-      if (stage) {
-        uu -= rc[v*nq + q];
+      double uu;
+      if constexpr (!split) {
+        uu = double(rate[v]);
+        if (stage) {
+          uu -= rc[v*nq + q];
+        } else {
+          rc[v*nq + q] = uu;
+          if constexpr (VISC) uu += double(vrate[v]);
+        }
+        uu *= mult;
       } else {
-        rc[v*nq + q] = uu;
-        if constexpr (VISC) uu += double(vrate[v]);
+        R ur = rate[v];
+        if (stage) {
+          ur -= R(rc[v*nq + q]);
+        } else {
+          rc[v*nq + q] = FaceT(ur);
+          if constexpr (VISC) ur += vrate[v];
+        }
+        uu = double(ur)*mult;
       }
-      uu *= mult;
-      if (compute_residual) rc[v*nq + q] = uu;
+      if (compute_residual) rc[v*nq + q] = FaceT(uu);
       else {
         double nu = st_w[v*nq + q] + uu;
         st_w[v*nq + q] = nu;
-        u[v] = R(nu);
+        up[v] = offset_var<ND, R>(m, v, nu);
       }
     }
   }
@@ -665,7 +678,7 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
     __syncthreads();
     if (active) {
       #pragma unroll
-      for (int v = 0; v < nv; ++v) my_u[v*nq + q] = u[v];
+      for (int v = 0; v < nv; ++v) my_u[v*nq + q] = up[v];
     }
     __syncthreads();
     write_faces_from_smem<ND, RS, R, FaceT>(m, st, s_u, e0, e_end);
@@ -751,13 +764,17 @@ k_reconcile_ldg(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int compute_r
     const double dt = m.scalars[SC_DT];
     double* st_w = m.elem + (size_t)e*(nv + 3)*nq;
     double mult = dt*st_w[nv*nq + q]*(1./m.nom_size[e]);
-    if constexpr (DEF) mult *= 1./m.jac[((size_t)(e - m.n_car)*(ND*ND + 1) + ND*ND)*nq + q];
-    double* to_update = compute_residual ? m.rcache + (size_t)e*nv*nq : st_w;
-    const int ld = compute_residual ? nq : nq;
+    if constexpr (DEF) mult *= m.inv_det[(size_t)(e - m.n_car)*nq + q];
+    if (compute_residual) {
+      FaceT* rc = m.rcache + (size_t)e*nv*nq;
+      #pragma unroll
+      for (int v = 0; v < nv; ++v) rc[v*nq + q] = FaceT(double(rc[v*nq + q]) + double(tr[v])*mult);
+    } else {
+      #pragma unroll
+      for (int v = 0; v < nv; ++v) st_w[v*nq + q] += double(tr[v])*mult;
+    }
     #pragma unroll
-    for (int v = 0; v < nv; ++v) to_update[v*ld + q] += double(tr[v])*mult;
-    #pragma unroll
-    for (int v = 0; v < nv; ++v) my_u[v*nq + q] = R(st_w[v*nq + q]);
+    for (int v = 0; v < nv; ++v) my_u[v*nq + q] = offset_var<ND, R>(m, v, st_w[v*nq + q]);
   }
   __syncthreads();
   write_faces_from_smem<ND, RS, R, FaceT>(m, st, s_u, e0, e_end);
@@ -768,10 +785,13 @@ k_reconcile_ldg(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int compute_r
 // to both faces with sign; LDG face average for the viscous path. One thread per face qpoint.
 template <int ND, int RS, typename R, typename FaceT>
 __device__ __forceinline__ void neighbor_point(const Dev<FaceT>& m, int slot0, int slot1, int dir, int q,
-                                               const double* nrml, bool viscous, const double* ghost_override)
+                                               const FaceT* nrml, bool viscous, const double* ghost_override)
 {
   using S = Shape<ND, RS>;
   constexpr int nfq = S::nfq, nv = S::nv;
+  // mixed form: traces are stored in offset form (rho - rho0, E - ener0) and the momentum
+  // flux carries p - P0 (see k_local); nothing on the faces needs double
+  constexpr bool split = !std::is_same<FaceT, double>::value;
   const bool deformed = nrml != nullptr;
   int sign0 = 1, sign1 = 1;
   if (deformed) {
@@ -781,56 +801,56 @@ __device__ __forceinline__ void neighbor_point(const Dev<FaceT>& m, int slot0, i
   const int q1 = deformed ? perm_index<ND, RS>(dir, q) : q;
   FaceT* f0 = m.face + (size_t)slot0*S::slot_dof;
   FaceT* f1 = m.face + (size_t)slot1*S::slot_dof;
-  R u0[nv], u1[nv], jump[nv];
+  R o0[nv], o1[nv], jump[nv];   // offset-form traces and their jump
   #pragma unroll
   for (int v = 0; v < nv; ++v) {
-    const double a = double(f0[v*nfq + q]);
-    const double b = ghost_override ? double(ghost_override[v]) : double(f1[v*nfq + q1]);
-    u0[v] = R(a);
-    u1[v] = R(b);
-    jump[v] = R(a - b);   // state jump of nearly equal traces: formed in double, then narrowed
+    if constexpr (split) {
+      o0[v] = R(f0[v*nfq + q]);
+      o1[v] = ghost_override ? offset_var<ND, R>(m, v, ghost_override[v]) : R(f1[v*nfq + q1]);
+      jump[v] = o0[v] - o1[v];
+    } else {
+      const double a = double(f0[v*nfq + q]);
+      const double b = ghost_override ? double(ghost_override[v]) : double(f1[v*nfq + q1]);
+      o0[v] = R(a);
+      o1[v] = R(b);
+      jump[v] = R(a - b);
+    }
   }
   if (viscous) {
     #pragma unroll
     for (int v = 0; v < nv; ++v) {
-      R avg = R(.5)*(u0[v] + u1[v]);
+      R avg = R(.5)*(o0[v] + o1[v]);
       f0[nv*nfq + v*nfq + q] = FaceT(avg);
       f1[nv*nfq + v*nfq + q1] = FaceT(avg);
     }
   }
-  constexpr bool split = !std::is_same<R, double>::value;
-  double nd_[ND];
+  R u0[nv], u1[nv];
+  #pragma unroll
+  for (int v = 0; v < nv; ++v) {
+    const R ref = !split ? R(0) : v == ND ? R(m.rho0) : v == ND + 1 ? R(m.ener0) : R(0);
+    u0[v] = split ? o0[v] + ref : o0[v];
+    u1[v] = split ? o1[v] + ref : o1[v];
+  }
   R n[ND];
   const int i_dim0 = dir & 3;
   #pragma unroll
-  for (int d = 0; d < ND; ++d) {
-    nd_[d] = deformed ? sign0*nrml[d*nfq + q] : (d == i_dim0 ? 1. : 0.);
-    n[d] = R(nd_[d]);
-  }
+  for (int d = 0; d < ND; ++d) n[d] = deformed ? R(sign0)*R(nrml[d*nfq + q]) : (d == i_dim0 ? R(1) : R(0));
   R fl0[nv], fl1[nv];
   Conv<ND, R> c0(u0), c1(u1);
-  c0.flux(u0, n, fl0, split ? R(0) : c0.pressure);
-  c1.flux(u1, n, fl1, split ? R(0) : c1.pressure);
+  const R pm0 = split ? R(heat_rat - 1.)*(o0[ND + 1] - c0.kin_ener) : c0.pressure;
+  const R pm1 = split ? R(heat_rat - 1.)*(o1[ND + 1] - c1.kin_ener) : c1.pressure;
+  c0.flux(u0, n, fl0, pm0);
+  c1.flux(u1, n, fl1, pm1);
   const R cs0 = char_speed<ND, R>(u0, c0.inv_mass), cs1 = char_speed<ND, R>(u1, c1.inv_mass);
   R nn = 0;
   #pragma unroll
   for (int d = 0; d < ND; ++d) nn += n[d]*n[d];
   const R mult = fmax(cs0, cs1)*sqrt(nn);
-  // mixed form: the pressure term of the momentum flux is formed in double from the
-  // double energy, since p*n is large against its variation across the face
-  double p_sum = 0.;
-  if constexpr (split) {
-    double e0 = double(f0[(nv - 1)*nfq + q]);
-    double e1 = ghost_override ? ghost_override[nv - 1] : double(f1[(nv - 1)*nfq + q1]);
-    p_sum = (heat_rat - 1.)*(e0 - double(c0.kin_ener)) + (heat_rat - 1.)*(e1 - double(c1.kin_ener));
-  }
   #pragma unroll
   for (int v = 0; v < nv; ++v) {
-    double flux;
-    if (split && v < ND) flux = .5*(double(fl0[v] + fl1[v] + mult*jump[v]) + p_sum*nd_[v]);
-    else flux = double(R(.5)*(fl0[v] + fl1[v] + mult*jump[v]));
-    f0[v*nfq + q] = FaceT(sign0*flux);
-    f1[v*nfq + q1] = FaceT(sign1*flux);
+    R flux = R(.5)*(fl0[v] + fl1[v] + mult*jump[v]);
+    f0[v*nfq + q] = FaceT(R(sign0)*flux);
+    f1[v*nfq + q1] = FaceT(R(sign1)*flux);
   }
 }
 
@@ -981,8 +1001,11 @@ __device__ void bc_state_point(const Dev<FaceT>& m, int i_bc, int q, double* gh)
   FaceT* gf = m.face + (size_t)c[1]*S::slot_dof;
   const double* nrml = m.bc_nrml + (size_t)i_bc*ND*nfq;
   double* sc = m.bc_cache + (size_t)i_bc*2*nv*nfq;
+  constexpr bool split = !std::is_same<FaceT, double>::value;
+  double ref[nv];   // offset of the stored traces (mixed form), see offset_var
+  for (int v = 0; v < nv; ++v) ref[v] = !split ? 0. : v == ND ? m.rho0 : v == ND + 1 ? m.ener0 : 0.;
   double inside[nv], n[ND];
-  for (int v = 0; v < nv; ++v) inside[v] = double(in[v*nfq + q]);
+  for (int v = 0; v < nv; ++v) inside[v] = split ? double(in[v*nfq + q]) + ref[v] : double(in[v*nfq + q]);
   for (int d = 0; d < ND; ++d) n[d] = nrml[d*nfq + q];
   switch (b.kind) {
     case HEXED_BC_FREESTREAM:
@@ -1035,7 +1058,7 @@ __device__ void bc_state_point(const Dev<FaceT>& m, int i_bc, int q, double* gh)
       for (int v = 0; v < nv; ++v) gh[v] = inside[v];
       break;
   }
-  for (int v = 0; v < nv; ++v) gf[v*nfq + q] = FaceT(gh[v]);
+  for (int v = 0; v < nv; ++v) gf[v*nfq + q] = FaceT(split ? gh[v] - ref[v] : gh[v]);
 }
 
 template <int ND, int RS, typename FaceT>
@@ -1065,7 +1088,7 @@ __global__ void k_bc_neighbor(Dev<FaceT> m)
       bc_state_point<ND, RS, FaceT>(m, i, q, gh);
       ov = gh;
     }
-    neighbor_point<ND, RS, R, FaceT>(m, c[0], c[1], bc_dir(c[2]), q, m.bc_nrml + (size_t)i*ND*nfq, VISC, ov);
+    neighbor_point<ND, RS, R, FaceT>(m, c[0], c[1], bc_dir(c[2]), q, m.bc_nrml_t + (size_t)i*ND*nfq, VISC, ov);
   }
 }
 
@@ -1266,19 +1289,21 @@ __global__ void k_refine(Dev<FaceT> m, Tab<RS> tab, int scale, int offset)
 
 // ------------------------------------------------------------------- Write_face (standalone)
 template <int ND, int RS, typename FaceT>
-__global__ void k_write_face(Dev<FaceT> m, Tab<RS> tab)
+__global__ void k_write_face(Dev<FaceT> m, Tab<RS> tab, int e_begin, int n_elem)
 {
   using S = Shape<ND, RS>;
   constexpr int nq = S::nq, nfq = S::nfq, nv = S::nv;
-  const long total = (long)m.n_elem*ND*nv*nfq;
+  const long total = (long)n_elem*ND*nv*nfq;
   for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
     int r = int(t%nfq); long rest = t/nfq;
     int v = int(rest%nv); rest /= nv;
-    int d = int(rest%ND); int e = int(rest/ND);
+    int d = int(rest%ND); int e = e_begin + int(rest/ND);
     const int stride = S::stride(d);
     const double* row = m.elem + (size_t)e*(nv + 3)*nq + v*nq + (r/stride)*stride*RS + r%stride;
+    // traces in the offset form of the storage (see offset_var)
+    const double ref = std::is_same<FaceT, double>::value ? 0. : v == ND ? m.rho0 : v == ND + 1 ? m.ener0 : 0.;
     double a0 = 0., a1 = 0.;
-    for (int i = 0; i < RS; ++i) { double x = row[i*stride]; a0 += tab.bound[i]*x; a1 += tab.bound[RS + i]*x; }
+    for (int i = 0; i < RS; ++i) { double x = row[i*stride] - ref; a0 += tab.bound[i]*x; a1 += tab.bound[RS + i]*x; }
     FaceT* f0 = m.face + (size_t)(e*2*ND + 2*d)*S::slot_dof + v*nfq + r;
     f0[0] = FaceT(a0);
     f0[S::slot_dof] = FaceT(a1);
@@ -1367,6 +1392,24 @@ static __global__ void k_finalize_dt(double* scalars, const double* partials, in
 }
 
 static __global__ void k_set_scalar(double* scalars, int which, double value) { scalars[which] = value; }
+
+// Storage conversions of the mixed form and the determinant reciprocal.
+static __global__ void k_narrow(const double* src, float* dst, long n)
+{
+  for (long i = blockIdx.x*(long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x*blockDim.x) dst[i] = float(src[i]);
+}
+static __global__ void k_widen(const float* src, double* dst, long n)
+{
+  for (long i = blockIdx.x*(long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x*blockDim.x) dst[i] = double(src[i]);
+}
+static __global__ void k_inv_det(const double* jac, double* inv_det, long n_def, int nq, int n_metric)
+{
+  const long n = n_def*nq;
+  for (long i = blockIdx.x*(long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x*blockDim.x) {
+    const long e = i/nq, q = i%nq;
+    inv_det[i] = 1./jac[(e*(n_metric + 1) + n_metric)*nq + q];
+  }
+}
 
 // FP64 pipe probe: fp64_fma_chains independent dependent-FMA chains per thread.
 constexpr int fp64_fma_chains = 8;
@@ -1490,11 +1533,11 @@ __global__ void __launch_bounds__(256) k_residual_partial(Dev<FaceT> m, Tab<RS> 
     double vol = 1.;
     for (int d = 0; d < ND; ++d) vol *= m.nom_size[e];
     const double* st = m.elem + (size_t)e*(nv + 3)*nq;
-    const double* rc = m.rcache + (size_t)e*nv*nq;
+    const FaceT* rc = m.rcache + (size_t)e*nv*nq;
     const double jd = e >= m.n_car ? m.jac[((size_t)(e - m.n_car)*(ND*ND + 1) + ND*ND)*nq + q] : 1.;
     const double tss = st[nv*nq + q];
     for (int v = 0; v < nv; ++v) {
-      double r = rc[v*nq + q]/tss;
+      double r = double(rc[v*nq + q])/tss;
       acc[v] += w*vol*(r*r)*jd;
     }
   }
@@ -1506,6 +1549,49 @@ __global__ void __launch_bounds__(256) k_residual_partial(Dev<FaceT> m, Tab<RS> 
     __syncthreads();
   }
   if (threadIdx.x == 0) for (int v = 0; v < nv; ++v) partials[blockIdx.x*nv + v] = s_acc[0][v];
+}
+
+// Residual norms of independent element segments (one solve each): CTA i reduces segment i
+// alone, in a fixed order, so its result is the same whatever else the arena holds.
+template <int ND, int RS, typename FaceT>
+__global__ void __launch_bounds__(256) k_segment_residual(Dev<FaceT> m, Tab<RS> tab, const int* seg_begin,
+                                                          const int* seg_count, double* out)
+{
+  using S = Shape<ND, RS>;
+  constexpr int nq = S::nq, nv = S::nv;
+  const int e_first = seg_begin[blockIdx.x];
+  const long total = (long)seg_count[blockIdx.x]*nq;
+  double acc[nv];
+  for (int v = 0; v < nv; ++v) acc[v] = 0.;
+  for (long t = threadIdx.x; t < total; t += blockDim.x) {
+    const int e = e_first + int(t/nq), q = int(t%nq);
+    double w = 1.;
+    for (int d = 0; d < ND; ++d) w *= tab.weight[(q/ipow(RS, ND - 1 - d))%RS];
+    double vol = 1.;
+    for (int d = 0; d < ND; ++d) vol *= m.nom_size[e];
+    const double* st = m.elem + (size_t)e*(nv + 3)*nq;
+    const FaceT* rc = m.rcache + (size_t)e*nv*nq;
+    const double jd = e >= m.n_car ? m.jac[((size_t)(e - m.n_car)*(ND*ND + 1) + ND*ND)*nq + q] : 1.;
+    const double tss = st[nv*nq + q];
+    for (int v = 0; v < nv; ++v) {
+      double r = double(rc[v*nq + q])/tss;
+      acc[v] += w*vol*(r*r)*jd;
+    }
+  }
+  __shared__ double s_acc[256][nv];
+  for (int v = 0; v < nv; ++v) s_acc[threadIdx.x][v] = acc[v];
+  __syncthreads();
+  for (int half = blockDim.x/2; half > 0; half >>= 1) {
+    if ((int)threadIdx.x < half) for (int v = 0; v < nv; ++v) s_acc[threadIdx.x][v] += s_acc[threadIdx.x + half][v];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    double mom = 0.;
+    for (int d = 0; d < ND; ++d) mom += s_acc[0][d];
+    out[3*blockIdx.x] = sqrt(mom);
+    out[3*blockIdx.x + 1] = sqrt(s_acc[0][ND]);
+    out[3*blockIdx.x + 2] = sqrt(s_acc[0][ND + 1]);
+  }
 }
 
 template <int NV>

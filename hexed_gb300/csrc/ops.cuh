@@ -22,18 +22,27 @@ template <int ND, int RS, typename R>
 struct Runner
 {
   using S = Shape<ND, RS>;
-  using FaceT = double;
+  using FaceT = R;   // storage of traces, residual cache and metric normals (see Dev)
 
   static Dev<FaceT> dev(Ctx& c)
   {
     Dev<FaceT> m;
     m.n_car = c.n_car; m.n_def = c.n_def; m.n_elem = c.n_car + c.n_def; m.n_slot = c.n_slot;
     m.n_car_con = c.n_car_con; m.n_def_con = c.n_def_con; m.n_bc_con = c.n_bc_con; m.n_ref = c.n_ref;
-    m.elem = c.elem; m.rcache = c.rcache; m.face = c.face;
-    m.nom_size = c.nom_size; m.vert_tss = c.vert_tss; m.jac = c.jac; m.face_nrml = c.face_nrml;
-    m.car_con = c.car_con; m.def_con = c.def_con; m.def_con_nrml = c.def_con_nrml;
+    m.elem = c.elem;
+    m.nom_size = c.nom_size; m.vert_tss = c.vert_tss; m.jac = c.jac; m.inv_det = c.inv_det;
+    m.car_con = c.car_con; m.def_con = c.def_con;
     m.bc_con = c.bc_con; m.bc_nrml = c.bc_nrml; m.bc_cache = c.bc_cache; m.ref_face = c.ref_face;
     m.bc_spec = c.bc_spec; m.scalars = c.scalars; m.partials = c.partials; m.status = c.status;
+    if constexpr (std::is_same<R, double>::value) {
+      m.rcache = c.rcache; m.face = c.face; m.nrm = c.jac; m.face_nrml = c.face_nrml;
+      m.def_con_nrml = c.def_con_nrml; m.bc_nrml_t = c.bc_nrml;
+      m.rho0 = 0.; m.ener0 = 0.;
+    } else {
+      m.rcache = c.rcache_f; m.face = c.face_f; m.nrm = c.nrm_f; m.face_nrml = c.face_nrml_f;
+      m.def_con_nrml = c.def_con_nrml_f; m.bc_nrml_t = c.bc_nrml_f;
+      m.rho0 = c.rho0; m.ener0 = c.ener0;
+    }
     return m;
   }
 
@@ -195,11 +204,12 @@ struct Runner
     k_finalize_dt<<<1, 256, 0, c.stream>>>(c.scalars, c.partials, grid, local_time, max_time_step, cheby);
   }
 
-  static void write_face(Ctx& c)
+  static void write_face(Ctx& c, int e_begin, int n_elem)
   {
-    const long total = (long)(c.n_car + c.n_def)*ND*S::nv*S::nfq;
+    const long total = (long)n_elem*ND*S::nv*S::nfq;
+    if (total == 0) return;
     ProfScope ps(c, "write_face");
-    k_write_face<ND, RS, FaceT><<<grid_for(total, 256), 256, 0, c.stream>>>(dev(c), tab(c));
+    k_write_face<ND, RS, FaceT><<<grid_for(total, 256), 256, 0, c.stream>>>(dev(c), tab(c), e_begin, n_elem);
   }
 
   static void residual_norm(Ctx& c, double* d_out)
@@ -232,11 +242,17 @@ struct Runner
     k_av_interp<ND, RS><<<grid_for((long)n_elem*S::nq, 256), 256, 0, c.stream>>>(c.elem, c.vert_id, n_elem, tab(c), c.vmax);
   }
 
+  static void segment_residual_norms(Ctx& c, int n_seg, const int* d_begin, const int* d_count, double* d_out)
+  {
+    ProfScope ps(c, "segment_residual");
+    k_segment_residual<ND, RS, FaceT><<<n_seg, 256, 0, c.stream>>>(dev(c), tab(c), d_begin, d_count, d_out);
+  }
+
   static const OpsTable* table()
   {
     static const OpsTable t = {
       compute_euler, compute_navier_stokes, max_dt, refine, write_face, bc_state, bc_flux, residual_norm,
-      set_art_visc_admis,
+      set_art_visc_admis, segment_residual_norms,
     };
     return &t;
   }

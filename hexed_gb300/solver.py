@@ -121,6 +121,44 @@ class Context:
         abi.check(self.lib.hexed_gpu_residual_norm(self.handle, out))
         return list(out)
 
+    # -------------------------------------------------------------- pool (continuous batching)
+    def write_face_range(self, elem_begin, elem_count):
+        abi.check(self.lib.hexed_gpu_write_face_range(self.handle, elem_begin, elem_count))
+
+    def write_range(self, which, offset, values):
+        v = np.ascontiguousarray(values, dtype=np.float64).ravel()
+        abi.check(self.lib.hexed_gpu_write_range(self.handle, which, offset, v.size, v.ctypes.data_as(abi.P_double)))
+
+    def read_range(self, which, offset, count):
+        out = np.empty(count, dtype=np.float64)
+        abi.check(self.lib.hexed_gpu_read_range(self.handle, which, offset, count, out.ctypes.data_as(abi.P_double)))
+        return out
+
+    def write_int_range(self, which, offset_rows, rows):
+        r = np.ascontiguousarray(rows, dtype=np.int32)
+        abi.check(self.lib.hexed_gpu_write_int_range(self.handle, which, offset_rows, r.shape[0],
+                                                     r.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+
+    def write_bc_spec(self, index, spec):
+        abi.check(self.lib.hexed_gpu_write_bc_spec(self.handle, index, ctypes.byref(spec)))
+
+    def set_active(self, n_car_elem, n_car_con, n_bc_con):
+        abi.check(self.lib.hexed_gpu_set_active(self.handle, n_car_elem, n_car_con, n_bc_con))
+
+    def segment_residual_norms(self, elem_begin, elem_count):
+        """Residual norms (momentum, density, energy) of each element segment: [n_seg, 3]."""
+        b = np.ascontiguousarray(elem_begin, dtype=np.int32)
+        n = np.ascontiguousarray(elem_count, dtype=np.int32)
+        out = np.empty((b.size, 3), dtype=np.float64)
+        ip = ctypes.POINTER(ctypes.c_int)
+        abi.check(self.lib.hexed_gpu_segment_residual_norms(self.handle, b.size, b.ctypes.data_as(ip),
+                                                            n.ctypes.data_as(ip), out.ctypes.data_as(abi.P_double)))
+        return out
+
+    def update_n(self, params, n, use_graph=True):
+        """Enqueue n updates (as one CUDA graph when use_graph); returns without synchronising."""
+        abi.check(self.lib.hexed_gpu_update_n(self.handle, ctypes.byref(params), n, int(use_graph)))
+
     # -------------------------------------------------------------- instrumentation
     @property
     def stream_ptr(self):

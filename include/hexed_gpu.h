@@ -132,7 +132,10 @@ enum hexed_array {
   HEXED_ARRAY_ELEM = 0,
   HEXED_ARRAY_RCACHE = 1,
   HEXED_ARRAY_FACE = 2,
-  HEXED_ARRAY_BC_CACHE = 3
+  HEXED_ARRAY_BC_CACHE = 3,
+  HEXED_ARRAY_NOM_SIZE = 4,
+  HEXED_ARRAY_VERT_TSS = 5,
+  HEXED_ARRAY_BC_NRML = 6
 };
 
 /* Arithmetic of the volume and face kernels. */
@@ -201,6 +204,11 @@ int hexed_gpu_compute_prolong(hexed_gpu_ctx* ctx, int scale, int offset);
 int hexed_gpu_compute_restrict(hexed_gpu_ctx* ctx, int scale, int offset);
 int hexed_gpu_compute_write_face(hexed_gpu_ctx* ctx);
 
+/* Write_face for elements [elem_begin, elem_begin + elem_count) only: initialises the face
+ * traces of one newly admitted solve without touching the traces of solves already running.
+ * No counterpart in the reference (which writes the faces of a whole mesh at once). */
+int hexed_gpu_write_face_range(hexed_gpu_ctx* ctx, int elem_begin, int elem_count);
+
 /* Solver::set_art_visc_admis (src/Solver.cpp:636-658): per-element smoothness indicator of
  * the specific volume (Stab_art_visc, src/stabilizing_art_visc.cpp:8-66) scaled by
  * char_speed, maximum over the elements sharing each vertex, multilinear interpolation to
@@ -225,6 +233,48 @@ int hexed_gpu_compute_residual(hexed_gpu_ctx* ctx, const hexed_update_params* pa
  * src/Qpoint_func.cpp:37-45): sqrt of the integral of (rcache/tss)^2 over the domain,
  * summed over momentum components, density, energy -> out[3]. */
 int hexed_gpu_residual_norm(hexed_gpu_ctx* ctx, double out[3]);
+
+/* --- continuous batching: many independent solves in one arena ---
+ * A serving loop packs the meshes of many independent solves into one Cartesian arena of
+ * fixed capacity (connections never cross solves), lets the kernels run over an active
+ * prefix, and admits / retires solves by rewriting ranges of the arena. Per-solve residual
+ * norms are segmented reductions over each solve's element range, so a solve's arithmetic is
+ * the same alone and in the mix. No counterpart in the reference, which runs one solve per
+ * process. */
+
+/* Host <-> device copy of `count` entries of an arena array starting at entry `offset`
+ * (entries in units of the array's scalar type). `which` is a hexed_array. */
+int hexed_gpu_write_range(hexed_gpu_ctx* ctx, int which, long offset, long count, const double* host);
+int hexed_gpu_read_range(hexed_gpu_ctx* ctx, int which, long offset, long count, double* host);
+
+/* Int connection arrays for hexed_gpu_write_int_range. */
+enum hexed_int_array {
+  HEXED_INT_CAR_CON = 0,   /* [n][3] */
+  HEXED_INT_BC_CON = 1     /* [n][4] */
+};
+/* Rewrites rows of a connection array; every entry is range-checked against the arena
+ * (slots, dimensions, boundary-condition index) before it reaches the device. offset and
+ * count are in rows. */
+int hexed_gpu_write_int_range(hexed_gpu_ctx* ctx, int which, long offset, long count, const int* host);
+
+/* Replaces boundary-condition record `index` (< n_bc_spec of the arena). */
+int hexed_gpu_write_bc_spec(hexed_gpu_ctx* ctx, int index, const hexed_bc_spec* spec);
+
+/* Active prefix the kernels process in a Cartesian-only arena: elements [0, n_car_elem),
+ * Cartesian connections [0, n_car_con), boundary connections [0, n_bc_con); each at most the
+ * arena's size. */
+int hexed_gpu_set_active(hexed_gpu_ctx* ctx, int n_car_elem, int n_car_con, int n_bc_con);
+
+/* Residual norms (as hexed_gpu_residual_norm) of each of n_seg element segments
+ * [elem_begin[i], elem_begin[i] + elem_count[i]): out[3*i .. 3*i+2]. One CTA reduces one
+ * segment in a fixed order, so a segment's norms do not depend on the other segments. */
+int hexed_gpu_segment_residual_norms(hexed_gpu_ctx* ctx, int n_seg, const int* elem_begin,
+                                     const int* elem_count, double* out);
+
+/* n consecutive Solver::update steps. use_graph != 0 captures the n-step launch sequence into
+ * a CUDA graph on first use and replays it while the parameters and active sizes are
+ * unchanged (launch overhead of small solves). */
+int hexed_gpu_update_n(hexed_gpu_ctx* ctx, const hexed_update_params* params, int n, int use_graph);
 
 /* --- instrumentation --- */
 

@@ -1,0 +1,73 @@
+"""Mixed precision (FP32 fluxes, derivatives and traces; FP64 state, update, metrics, time
+step): error of the mixed state against the FP64 GPU state on every mesh kind."""
+import numpy as np
+import pytest
+
+import oracle
+from hexed_gb300 import abi, problems
+from hexed_gb300.solver import Context
+from helpers import all_directions, cartesian_case, deformed_case, rotated_pair_case
+
+pytestmark = pytest.mark.gpu
+
+
+def l2_by_quantity(a, b, nv):
+    out = {}
+    for name, sl in (("momentum", slice(0, nv - 2)), ("density", slice(nv - 2, nv - 1)), ("energy", slice(nv - 1, nv))):
+        out[name] = float(np.linalg.norm(a[:, sl] - b[:, sl]) / np.linalg.norm(b[:, sl]))
+    return out
+
+
+def run(ar, params, steps, precision, prolong=False):
+    ar = ar.copy()
+    with Context(ar, precision) as c:
+        c.write_face()
+        if prolong:
+            c.prolong()
+        for _ in range(steps):
+            c.update(params)
+        return c.download(abi.ARRAY_ELEM)[:, :ar.nv]
+
+
+def check(ar, params, steps, tol, prolong=False):
+    s64 = run(ar, params, steps, abi.FP64, prolong)
+    s32 = run(ar, params, steps, abi.MIXED, prolong)
+    assert np.isfinite(s32).all()
+    err = l2_by_quantity(s32, s64, ar.nv)
+    assert max(err.values()) <= tol, err
+    # the update really moved the state (the comparison is not vacuous)
+    assert np.abs(s64 - ar.elem[:, :ar.nv]).max() > 0
+    return err
+
+
+def test_mixed_vortex_2d():
+    ar = problems.vortex_2d(n_per_side=12, row_size=6)
+    check(ar, abi.update_params(max_safety=0.5), 50, 1e-6)
+
+
+def test_mixed_taylor_green():
+    ar = problems.taylor_green_3d(n_per_side=4, row_size=4)
+    check(ar, abi.update_params(max_safety=0.5, visc=ar.visc, cond=ar.cond), 50, 1e-6)
+
+
+@pytest.mark.parametrize("deformed", [False, True])
+def test_mixed_euler_and_bcs(deformed):
+    for kind in (abi.BC_RIEMANN, abi.BC_NONPENETRATION, abi.BC_FREESTREAM, abi.BC_PRESSURE_OUTFLOW):
+        ar = deformed_case(3, 4, 3, kind) if deformed else cartesian_case(2, 4, 5, kind)
+        check(ar, abi.update_params(max_safety=0.5), 20, 1e-6)
+
+
+def test_mixed_rotated_connections():
+    for d in list(all_directions(3))[::5]:
+        ar = rotated_pair_case(3, 3, d)
+        check(ar, abi.update_params(max_safety=0.5), 10, 1e-6)
+
+
+def test_mixed_hanging_faces():
+    ar = problems.pulse_tree_3d(n_base=2, row_size=4, levels=1)
+    check(ar, abi.update_params(max_safety=0.5), 20, 1e-6, prolong=True)
+
+
+def test_mixed_artificial_viscosity():
+    ar = problems.mach2_jump_3d(n_per_side=3, row_size=4)
+    check(ar, abi.update_params(max_safety=0.5, av_admis_char_speed=ar.av_char_speed), 10, 1e-5)
