@@ -140,6 +140,8 @@ def load_library(path=LIB_PATH):
         "hexed_gpu_segment_residual_norms": ([vp, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int), P_double],
                                              c_int),
         "hexed_gpu_update_n": ([vp, ctypes.POINTER(UpdateParams), c_int, c_int], c_int),
+        "hexed_gpu_segment_residual_norms_static": ([vp, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int),
+                                                     P_double], c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -10,6 +10,7 @@
 #include <string>
 #include <vector>
 #include <algorithm>
+#include <mutex>
 #include "ctx.h"
 #include "kernels.cuh"
 #include "basis_tables.h"
@@ -800,3 +801,66 @@ int hexed_gpu_profile_read(hexed_gpu_ctx* c, hexed_kernel_time* out, int capacit
 }
 
 } // extern "C"
+
+// ------------------------------------------------------------------ no-allocation variant
+namespace {
+
+// Scratch of hexed_gpu_segment_residual_norms_static, in module memory that exists from load
+// time: the norms of up to HEXED_STATIC_MAX_SEGMENTS segments (3 doubles each), then the
+// segment table (begins, then counts, as ints packed two to a double slot). Nothing in it has
+// to start at zero: every call copies its table in and the kernel writes every norm it returns.
+constexpr int static_max_seg = HEXED_STATIC_MAX_SEGMENTS;
+static __device__ __align__(256) double g_seg_scratch[3*static_max_seg + static_max_seg];
+
+constexpr int max_devices = 64;
+std::mutex g_seg_scratch_lock;
+double* g_seg_scratch_addr[max_devices] = {};
+
+// Device address of g_seg_scratch on `device`, looked up once per device with that device
+// current (the host-side symbol is not a device address).
+int seg_scratch_on(int device, double** out)
+{
+  if (device < 0 || device >= max_devices) return fail(HEXED_ERR_INVALID, "device %d out of range", device);
+  std::lock_guard<std::mutex> guard(g_seg_scratch_lock);
+  if (!g_seg_scratch_addr[device]) {
+    int current = -1;
+    HX_CUDA(cudaGetDevice(&current));
+    if (current != device) HX_CUDA(cudaSetDevice(device));
+    void* addr = nullptr;
+    const cudaError_t err = cudaGetSymbolAddress(&addr, g_seg_scratch);
+    if (current != device) HX_CUDA(cudaSetDevice(current));
+    if (err != cudaSuccess || !addr)
+      return fail(HEXED_ERR_CUDA, "cudaGetSymbolAddress of the segment-norm scratch: %s", cudaGetErrorString(err));
+    g_seg_scratch_addr[device] = static_cast<double*>(addr);
+  }
+  *out = g_seg_scratch_addr[device];
+  return HEXED_OK;
+}
+
+} // namespace
+
+extern "C" int hexed_gpu_segment_residual_norms_static(hexed_gpu_ctx* c, int n_seg, const int* elem_begin,
+                                                       const int* elem_count, double* out)
+{
+  if (int st = check_ctx(c)) return st;
+  if (n_seg < 0 || (n_seg && (!elem_begin || !elem_count || !out))) return fail(HEXED_ERR_INVALID, "bad segment table");
+  if (n_seg > static_max_seg)
+    return fail(HEXED_ERR_INVALID, "%d segments exceed the fixed scratch of this entry point (at most %d)", n_seg,
+                static_max_seg);
+  for (int i = 0; i < n_seg; ++i)
+    if (elem_begin[i] < 0 || elem_count[i] < 1 || (long)elem_begin[i] + elem_count[i] > (long)c->n_car + c->n_def)
+      return fail(HEXED_ERR_INVALID, "segment %d outside the active elements", i);
+  double* scratch = nullptr;
+  if (int st = seg_scratch_on(c->device, &scratch)) return st;
+  if (n_seg == 0) return HEXED_OK;
+  double* d_out = scratch;
+  int* d_table = reinterpret_cast<int*>(scratch + 3*static_max_seg);
+  HX_CUDA(cudaMemcpyAsync(d_table, elem_begin, n_seg*sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  HX_CUDA(cudaMemcpyAsync(d_table + static_max_seg, elem_count, n_seg*sizeof(int), cudaMemcpyHostToDevice,
+                          c->stream));
+  c->ops->segment_residual_norms(*c, n_seg, d_table, d_table + static_max_seg, d_out);
+  HX_LAUNCHED();
+  HX_CUDA(cudaMemcpyAsync(out, d_out, 3*n_seg*sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  HX_CUDA(cudaStreamSynchronize(c->stream));
+  return HEXED_OK;
+}

@@ -145,14 +145,17 @@ class Context:
     def set_active(self, n_car_elem, n_car_con, n_bc_con):
         abi.check(self.lib.hexed_gpu_set_active(self.handle, n_car_elem, n_car_con, n_bc_con))
 
-    def segment_residual_norms(self, elem_begin, elem_count):
-        """Residual norms (momentum, density, energy) of each element segment: [n_seg, 3]."""
+    def segment_residual_norms(self, elem_begin, elem_count, static_scratch=False):
+        """Residual norms (momentum, density, energy) of each element segment: [n_seg, 3].
+        static_scratch selects the entry point that allocates no device memory."""
         b = np.ascontiguousarray(elem_begin, dtype=np.int32)
         n = np.ascontiguousarray(elem_count, dtype=np.int32)
         out = np.empty((b.size, 3), dtype=np.float64)
         ip = ctypes.POINTER(ctypes.c_int)
-        abi.check(self.lib.hexed_gpu_segment_residual_norms(self.handle, b.size, b.ctypes.data_as(ip),
-                                                            n.ctypes.data_as(ip), out.ctypes.data_as(abi.P_double)))
+        fn = (self.lib.hexed_gpu_segment_residual_norms_static if static_scratch
+              else self.lib.hexed_gpu_segment_residual_norms)
+        abi.check(fn(self.handle, b.size, b.ctypes.data_as(ip), n.ctypes.data_as(ip),
+                     out.ctypes.data_as(abi.P_double)))
         return out
 
     def update_n(self, params, n, use_graph=True):

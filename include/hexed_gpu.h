@@ -271,6 +271,24 @@ int hexed_gpu_set_active(hexed_gpu_ctx* ctx, int n_car_elem, int n_car_con, int 
 int hexed_gpu_segment_residual_norms(hexed_gpu_ctx* ctx, int n_seg, const int* elem_begin,
                                      const int* elem_count, double* out);
 
+/* Largest n_seg hexed_gpu_segment_residual_norms_static accepts. */
+#define HEXED_STATIC_MAX_SEGMENTS 4096
+
+/* hexed_gpu_segment_residual_norms without any device allocation: same arguments, same
+ * results. hexed_gpu_segment_residual_norms grows its per-context table and output buffers
+ * with cudaMalloc when n_seg exceeds what it has seen; this variant instead uses one
+ * fixed array of module memory (128 KiB per device, up to HEXED_STATIC_MAX_SEGMENTS
+ * segments; more are rejected with HEXED_ERR_INVALID). It is for callers that cannot let
+ * the library allocate: a serving loop that has handed out the device's free memory to
+ * admitted solves, or one that keeps a fixed memory budget, would otherwise see a failed or
+ * device-synchronising allocation in the middle of its loop. The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress); make that first call before
+ * any stream capture. The array is shared by every context on the device and keeps the last
+ * call's contents, so overlapping calls (from two threads, or on two streams) race: callers
+ * serialise them. No counterpart in the reference. */
+int hexed_gpu_segment_residual_norms_static(hexed_gpu_ctx* ctx, int n_seg, const int* elem_begin,
+                                            const int* elem_count, double* out);
+
 /* n consecutive Solver::update steps. use_graph != 0 captures the n-step launch sequence into
  * a CUDA graph on first use and replays it while the parameters and active sizes are
  * unchanged (launch overhead of small solves). */
