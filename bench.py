@@ -6,6 +6,12 @@ A step is one Solver::update: max_dt, the viscous LDG stage 0 and the inviscid s
 (src/Solver.cpp:834-886). value = element DOFs x 2 stages x steps / device time.
 
   python bench.py [--gpus N --steps K --warmup W --precision fp64|mixed --impl gb300|reference]
+                  [--workload tgv|vortex|mach2|tree --n N --rs RS]
+  python bench.py --serving [--solves S --rate R --max-side M --tol T --precision fp64|mixed]
+
+The default line reports the FP64 form (the headline) and, under "mixed", the mixed form of
+the same workload with its error against the FP64 state. --workload selects the other
+configurations (see Workload); --serving measures the serving loop (see run_serving).
 
 Multi-GPU: the path runs one independent replica per GPU (no data-path collective);
 value aggregates all replicas (weak scaling).
@@ -28,9 +34,8 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-from hexed_gb300 import abi, problems  # noqa: E402
+from hexed_gb300 import abi, problems, replicas  # noqa: E402
 
-WORKLOAD = "taylor_green_3d_ns_32cube_deformed_rs6"
 METRIC = "GDOF-updates/s per RK stage"
 
 
@@ -39,8 +44,55 @@ def dist_env():
         int(os.environ.get("LOCAL_RANK", "0"))
 
 
-def make_case(n, rs, seed=0):
-    return problems.taylor_green_3d(n_per_side=n, row_size=rs, seed=seed)
+class Workload:
+    """One benchmark configuration: the mesh and initial state, and the update parameters.
+
+    tgv    compressible Navier-Stokes Taylor-Green vortex, n^3 deformed hexes (default 32),
+           row size 6, Mach 0.1, Re 1600, Pr 0.71, Sutherland transport (the headline)
+    vortex 2D isentropic vortex, n x n Cartesian quads (default 32) on [-5, 5]^2, row size 6,
+           Mach 0.5, Riemann-invariant freestream boundaries
+    mach2  the deformed n^3 mesh (default 32) with an inviscid Mach 2 flow and a density jump
+           of ratio 2.5 at x = pi, with stabilising artificial viscosity
+    tree   16^3 base tree refined 2 levels inside a sphere of radius 0.25 (27,224 hexes with
+           hanging faces), row size 4 (or 6), Euler Mach 0.3 with a Gaussian pressure pulse
+    """
+    DEFAULT_N = {"tgv": 32, "vortex": 32, "mach2": 32, "tree": 16}
+    DEFAULT_RS = {"tgv": 6, "vortex": 6, "mach2": 6, "tree": 4}
+
+    def __init__(self, kind, n=None, rs=None):
+        self.kind = kind
+        self.n = n or self.DEFAULT_N[kind]
+        self.rs = rs or self.DEFAULT_RS[kind]
+
+    def arena(self):
+        k, n, rs = self.kind, self.n, self.rs
+        if k == "tgv":
+            return problems.taylor_green_3d(n_per_side=n, row_size=rs)
+        if k == "vortex":
+            return problems.vortex_2d(n_per_side=n, row_size=rs)
+        if k == "mach2":
+            return problems.mach2_jump_3d(n_per_side=n, row_size=rs)
+        return problems.pulse_tree_3d(n_base=n, row_size=rs, levels=2)
+
+    def params(self, ar):
+        if self.kind == "tgv":
+            return abi.update_params(max_safety=0.5, visc=ar.visc, cond=ar.cond)
+        if self.kind == "mach2":
+            return abi.update_params(max_safety=0.5, av_admis_char_speed=ar.av_char_speed)
+        return abi.update_params(max_safety=0.5)
+
+    @property
+    def name(self):
+        return {"tgv": f"taylor_green_3d_ns_{self.n}cube_deformed_rs{self.rs}",
+                "vortex": f"isentropic_vortex_2d_{self.n}sq_rs{self.rs}",
+                "mach2": f"mach2_density_jump_3d_euler_av_{self.n}cube_deformed_rs{self.rs}",
+                "tree": f"pulse_tree_3d_{self.n}base_2levels_rs{self.rs}"}[self.kind]
+
+
+def initialize(c):
+    """Solver::initialize on a context or oracle: traces, then hanging-face mortars."""
+    c.write_face()
+    c.prolong()
 
 
 def dofs_per_update(ar):
@@ -48,33 +100,50 @@ def dofs_per_update(ar):
 
 
 # ------------------------------------------------------------------ algorithmic bytes
-def kernel_bytes(name, ar):
+def kernel_bytes(name, ar, precision="fp64"):
     """Compulsory bytes per launch of each kernel: every array the kernel must read or
-    write, counted once (FP64 arena; face traces stored in double)."""
+    write, counted once. The state, time-step scale, AV rows and determinant reciprocals are
+    double in both forms; traces, residual cache and metric normals are float in the mixed
+    form."""
     nd, nq, nfq, nv = ar.n_dim, ar.nq, ar.nfq, ar.nv
     F = 2 * nd
-    met = (nd * nd + 1) * nq
+    d, w = 8, (4 if precision == "mixed" else 8)
+    metric = w * nd * nd * nq + d * nq
     per_elem = {
-        "local_car_euler": (3 * nv + 1) * nq + 2 * F * nv * nfq,
-        "local_def_euler": (3 * nv + 1) * nq + 2 * F * nv * nfq + met,
-        "local_car_ns": (3 * nv + 3) * nq + 3 * F * nv * nfq,
-        "local_def_ns": (3 * nv + 3) * nq + 3 * F * nv * nfq + met + F * nd * nfq,
-        "reconcile_ldg_car": (2 * nv + 1) * nq + 2 * F * nv * nfq,
-        "reconcile_ldg_def": (2 * nv + 2) * nq + 2 * F * nv * nfq,
-        "max_dt": (nv + 3) * nq + 2 ** nd,
+        "local_car_euler": d * (2 * nv + 1) * nq + w * nv * nq + w * 2 * F * nv * nfq,
+        "local_def_euler": d * (2 * nv + 1) * nq + w * nv * nq + w * 2 * F * nv * nfq + metric,
+        "local_car_ns": d * (2 * nv + 3) * nq + w * nv * nq + w * 3 * F * nv * nfq,
+        "local_def_ns": d * (2 * nv + 3) * nq + w * nv * nq + w * 3 * F * nv * nfq + metric + w * F * nd * nfq,
+        "reconcile_ldg_car": d * (2 * nv + 1) * nq + w * 2 * F * nv * nfq,
+        "reconcile_ldg_def": d * (2 * nv + 2) * nq + w * 2 * F * nv * nfq,
+        "max_dt": d * (nv + 3) * nq + d * 2 ** nd,
     }
     if name in per_elem:
         n = ar.n_def if "def" in name else ar.n_car if "car" in name else ar.n_elem
-        return 8 * per_elem[name] * n
+        return per_elem[name] * n
     per_con = {
-        "neighbor_car": 4 * nv * nfq,
-        "neighbor_def": 4 * nv * nfq + nd * nfq,
-        "neighbor_bc_fused": 4 * nv * nfq + nd * nfq,
+        "neighbor_car": w * 4 * nv * nfq,
+        "neighbor_def": w * (4 * nv * nfq + nd * nfq),
+        "neighbor_bc_fused": w * (4 * nv * nfq + nd * nfq),
     }
     if name in per_con:
         n = {"neighbor_car": len(ar.car_con), "neighbor_def": len(ar.def_con)}.get(name, len(ar.bc_con))
-        return 8 * per_con[name] * n
+        return per_con[name] * n
     return None
+
+
+# DRAM bytes per element and launch measured by ncu on smaller cases of the same kernels
+# (read + write; profiles/k_local_tgv_rs6.md): FP64 at 16^3, mixed at 24^3 elements.
+NCU_DRAM_BYTES_PER_ELEM = {
+    ("local_def_ns", "fp64", 6): (219.576320e6 + 71.881728e6) / 4096,
+    ("local_def_ns", "mixed", 6): (479.313152e6 + 204.372480e6) / 13824,
+}
+
+
+# Busiest pipe of the same kernels in those captures (% of peak sustained, active cycles).
+NCU_PIPE_FRAC = {
+    ("local_def_ns", "fp64", 6): ("fp64", 0.919),
+}
 
 
 # ------------------------------------------------------------------ clocks
@@ -129,13 +198,13 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ CPU oracle timing
-def cpu_baseline(n, rs, steps=None, target_s=12.):
+def cpu_baseline(wl, steps=None, target_s=12.):
     """Time the oracle port (OpenMP, all host threads) on the same workload."""
     import oracle
-    ar = make_case(n, rs)
+    ar = wl.arena()
     o = oracle.Oracle(ar)
-    o.write_face()
-    p = abi.update_params(max_safety=0.5, visc=ar.visc, cond=ar.cond)
+    initialize(o)
+    p = wl.params(ar)
     t0 = time.perf_counter()
     o.update(p)
     one = time.perf_counter() - t0
@@ -147,7 +216,7 @@ def cpu_baseline(n, rs, steps=None, target_s=12.):
     t = time.perf_counter() - t0
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     return {"value": dofs_per_update(ar) * steps / t / 1e9, "unit": "GDOF/s", "cores": cores, "kind": "port",
-            "sample": f"{steps} Solver::update steps of the full {n}^3 row-size-{rs} workload on the CPU oracle "
+            "sample": f"{steps} Solver::update steps of the full {wl.name} workload on the CPU oracle "
                       f"({t:.2f} s)", "seconds": t}
 
 
@@ -157,11 +226,12 @@ def run_reference(args):
         return 0
     import oracle
     oracle.build()
-    ar = make_case(args.n, args.rs)
+    wl = Workload(args.workload, args.n, args.rs)
+    ar = wl.arena()
     o = oracle.Oracle(ar)
-    o.write_face()
-    p = abi.update_params(max_safety=0.5, visc=ar.visc, cond=ar.cond)
-    # one update is several seconds of CPU work at full size: keep each step one update
+    initialize(o)
+    p = wl.params(ar)
+    # one update is a fraction of a second of CPU work at full size: each step is one update
     for _ in range(args.warmup):
         o.update(p)
     t0 = time.perf_counter()
@@ -173,7 +243,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "GDOF/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": WORKLOAD, "n_elem": ar.n_elem, "row_size": args.rs,
+            "data": "synthetic", "config": {"workload": wl.name, "n_elem": ar.n_elem, "row_size": wl.rs,
                                             "precision": "fp64"},
             "cpu_baseline": {"value": value, "unit": "GDOF/s", "cores": cores, "kind": "port",
                              "sample": f"{args.steps} Solver::update steps of the full workload on the CPU oracle"},
@@ -196,17 +266,17 @@ def state_errors(a, b, nv):
     return out
 
 
-def mixed_vs_fp64(n, rs, steps):
+def mixed_vs_fp64(wl, steps):
     """Run the same case `steps` updates in FP64 and in mixed precision on the GPU and
     report the mixed state's error against the FP64 state."""
     from hexed_gb300.solver import Context
     states = {}
-    base = make_case(n, rs)
+    base = wl.arena()
     for prec in (abi.FP64, abi.MIXED):
         ar = base.copy()
         with Context(ar, prec) as c:
-            c.write_face()
-            p = abi.update_params(max_safety=0.5, visc=ar.visc, cond=ar.cond)
+            initialize(c)
+            p = wl.params(ar)
             for _ in range(steps):
                 c.update(p, read_dt=False)
             states[prec] = c.download(abi.ARRAY_ELEM)[:, :ar.nv]
@@ -214,6 +284,45 @@ def mixed_vs_fp64(n, rs, steps):
     err["steps"] = steps
     err["reference"] = "FP64 GPU path, same mesh and initial state"
     return err
+
+
+# ------------------------------------------------------------------ serving stream
+def run_serving(args):
+    """Continuous-batching serving of a stream of steady 2D Euler solves against the same
+    stream served one solve at a time (FP64), both on this GPU, same tolerance.
+
+    The stream: Cartesian meshes of [0, 1]^2 with sides uniform in [8, max_side], row size 4
+    or 6, Mach U(0.2, 0.8), angle U(-10, 10) degrees, freestream plus a 5-mode 2% Fourier
+    perturbation, local time stepping until the normalized residual reaches `tol`; Poisson
+    arrivals at `rate` per second."""
+    from hexed_gb300 import serving
+    precision = abi.MIXED if args.precision == "mixed" else abi.FP64
+    params = abi.update_params(max_safety=0.5, local_time=True)
+    reqs = serving.request_stream(args.solves, args.rate, seed=args.seed, sides=(8, args.max_side))
+    k = {4: args.batch, 6: args.batch}
+    with serving.Server(precision, tol=args.tol, updates_per_batch=k, params=params,
+                        max_updates=args.max_updates) as srv:
+        srv.run(reqs[:2])   # warm-up: kernels loaded, graphs of the first shapes
+        batched = srv.run(reqs).summary()
+    base = None
+    if not args.no_one_at_a_time:
+        with serving.Server(abi.FP64, tol=args.tol, updates_per_batch=k, params=params, max_live=1,
+                            max_updates=args.max_updates) as srv:
+            srv.run(reqs[:2])
+            base = srv.run(reqs).summary()
+    line = {
+        "metric": "steady solves/s (continuous batching)", "value": batched["solves_per_s"], "unit": "solves/s",
+        "n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if precision == abi.FP64 else "f32/f64", "data": "synthetic",
+        "config": {"workload": "serving_2d_euler_stream", "solves": args.solves, "rate_per_s": args.rate,
+                   "sides": [8, args.max_side], "row_sizes": [4, 6], "tol": args.tol, "seed": args.seed,
+                   "updates_per_batch": args.batch, "precision": args.precision},
+        "p50_latency_s": batched["p50_latency_s"], "p99_latency_s": batched["p99_latency_s"],
+        "batched": batched, "one_at_a_time_fp64": base,
+        "speedup_vs_one_at_a_time": (batched["solves_per_s"] / base["solves_per_s"]) if base else None,
+    }
+    print(json.dumps(line))
+    return 0
 
 
 # ------------------------------------------------------------------ GPU arm
@@ -224,14 +333,27 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
-    ap.add_argument("--n", type=int, default=32, help="elements per side")
-    ap.add_argument("--rs", type=int, default=6, help="row size")
+    ap.add_argument("--workload", default="tgv", choices=["tgv", "vortex", "mach2", "tree"])
+    ap.add_argument("--n", type=int, default=None, help="elements per side (tree: base elements per side)")
+    ap.add_argument("--rs", type=int, default=None, help="row size")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=None)
     ap.add_argument("--err-steps", type=int, default=200, help="updates for the mixed-vs-FP64 error report")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-form measurement beside FP64")
+    ap.add_argument("--serving", action="store_true", help="serve a stream of steady 2D solves instead")
+    ap.add_argument("--solves", type=int, default=64)
+    ap.add_argument("--rate", type=float, default=200.)
+    ap.add_argument("--max-side", type=int, default=16)
+    ap.add_argument("--tol", type=float, default=1e-8)
+    ap.add_argument("--batch", type=int, default=20, help="updates per batch (one graph replay)")
+    ap.add_argument("--max-updates", type=int, default=400_000)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-one-at-a-time", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.serving:
+        return run_serving(args)
 
     import torch
     rank, world, local_rank = dist_env()
@@ -248,10 +370,11 @@ def main():
 
     from hexed_gb300.solver import Context, fp64_peak_tflops
     precision = abi.MIXED if args.precision == "mixed" else abi.FP64
-    ar = make_case(args.n, args.rs)
+    wl = Workload(args.workload, args.n, args.rs)
+    ar = wl.arena()
     ctx = Context(ar, precision)
-    ctx.write_face()
-    p = abi.update_params(max_safety=0.5, visc=ar.visc, cond=ar.cond)
+    initialize(ctx)
+    p = wl.params(ar)
     stream = torch.cuda.ExternalStream(ctx.stream_ptr)
     for _ in range(args.warmup):
         ctx.update(p, read_dt=False)
@@ -271,11 +394,8 @@ def main():
     barrier()
     ms = e0.elapsed_time(e1)
     prof = ctx.profile_read()
-    ms_t = torch.tensor([ms], device="cuda")
-    if pg:
-        pg.all_reduce(ms_t, op=pg.ReduceOp.MAX)
-    ms = float(ms_t.item())
-    value = dofs_per_update(ar) * args.steps * world / (ms / 1e3) / 1e9
+    ms = replicas.max_over_ranks(ms, device="cuda")
+    value = replicas.job_rate(dofs_per_update(ar) * args.steps, world, ms) / 1e9
     launches = sum(v[0] for v in prof.values())
 
     # ---- end to end through the C ABI with pinned host buffers: upload the state, one
@@ -299,8 +419,8 @@ def main():
     f1.record(stream)
     torch.cuda.synchronize()
     wall_e2e = time.perf_counter() - t0
-    ms_e2e = max(f0.elapsed_time(f1), wall_e2e * 1e3)
-    e2e_value = dofs_per_update(ar) * args.steps * world / (ms_e2e / 1e3) / 1e9
+    ms_e2e = replicas.max_over_ranks(max(f0.elapsed_time(f1), wall_e2e * 1e3), device="cuda")
+    e2e_value = replicas.job_rate(dofs_per_update(ar) * args.steps, world, ms_e2e) / 1e9
 
     # ---- roofline of the dominant kernel
     peaks = {}
@@ -314,27 +434,64 @@ def main():
     top = max(prof.items(), key=lambda kv: kv[1][1])
     top_name, (top_launches, top_ms) = top
     per_launch_ms = top_ms / max(top_launches, 1)
-    nbytes = kernel_bytes(top_name, ar)
+    nbytes = kernel_bytes(top_name, ar, args.precision)
     achieved = nbytes / (per_launch_ms * 1e-3) / 1e9 if nbytes else None
     fp64_peak = fp64_peak_tflops()
+    traffic = None
+    per_elem = NCU_DRAM_BYTES_PER_ELEM.get((top_name, args.precision, wl.rs)) if wl.kind == "tgv" else None
+    if per_elem is not None:
+        traffic = per_elem * (ar.n_def if "def" in top_name else ar.n_car if "car" in top_name else ar.n_elem)
     roofline = {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved / hbm_peak if achieved else None, "traffic": None,
+                "frac": achieved / hbm_peak if achieved else None, "traffic": traffic,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a smaller case of the same "
+                                  "kernel, scaled by elements (profiles/k_local_tgv_rs6.md)" if traffic else None,
                 "algorithmic_bytes_per_launch": nbytes, "launch_ms": per_launch_ms,
                 "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
                 "fp64_peak_tflops_measured": fp64_peak}
+    pipe = NCU_PIPE_FRAC.get((top_name, args.precision, wl.rs)) if wl.kind == "tgv" else None
+    if pipe is not None:
+        # what bounds this kernel instead of HBM: the busiest pipe in ncu (profiles/k_local_tgv_rs6.md)
+        roofline["compute_bound"] = {"pipe": pipe[0], "frac_of_peak_ncu": pipe[1]}
     kernels = {k: {"launches": v[0], "total_ms": round(v[1], 4), "share": round(v[1] / sum(x[1] for x in prof.values()), 4)}
                for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])}
 
     mixed_err = None
-    if precision == abi.MIXED and rank == 0:
+    if precision == abi.MIXED and rank == 0 and args.err_steps > 0:
         ctx.close()
-        mixed_err = mixed_vs_fp64(args.n, args.rs, args.err_steps)
+        mixed_err = mixed_vs_fp64(wl, args.err_steps)
+
+    # the mixed form of the same workload beside the FP64 headline
+    mixed = None
+    if precision == abi.FP64 and rank == 0 and not args.no_mixed:
+        ctx.close()
+        mctx = Context(wl.arena(), abi.MIXED)
+        initialize(mctx)
+        mstream = torch.cuda.ExternalStream(mctx.stream_ptr)
+        for _ in range(args.warmup):
+            mctx.update(p, read_dt=False)
+        mctx.profile_enable(True)
+        torch.cuda.synchronize()
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        g0.record(mstream)
+        for _ in range(args.steps):
+            mctx.update(p, read_dt=False)
+        g1.record(mstream)
+        torch.cuda.synchronize()
+        mms = g0.elapsed_time(g1)
+        mprof = mctx.profile_read()
+        mctx.close()
+        mvalue = dofs_per_update(ar) * args.steps / (mms / 1e3) / 1e9
+        mixed = {"value": mvalue, "unit": "GDOF/s", "ms_per_step": mms / args.steps, "speedup_vs_fp64": mvalue / value,
+                 "dtype": "f32/f64",
+                 "kernels": {k: {"launches": v[0], "total_ms": round(v[1], 4)}
+                             for k, v in sorted(mprof.items(), key=lambda kv: -kv[1][1])},
+                 "error_vs_fp64": mixed_vs_fp64(wl, args.err_steps) if args.err_steps > 0 else None}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         ctx.close()
         try:
-            cpu = cpu_baseline(args.n, args.rs, args.cpu_steps)
+            cpu = cpu_baseline(wl, args.cpu_steps)
         except Exception as exc:  # noqa: BLE001
             cpu = {"error": str(exc)}
 
@@ -343,9 +500,9 @@ def main():
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64" if precision == abi.FP64 else "f32/f64",
                 "data": "synthetic",
-                "config": {"workload": WORKLOAD, "n_elem": ar.n_elem, "row_size": args.rs,
+                "config": {"workload": wl.name, "n_elem": ar.n_elem, "row_size": wl.rs,
                            "precision": args.precision, "parallelism": f"replicas{world}",
-                           "l2": "inputs larger than L2 (arena ~2 GB)"},
+                           "l2": f"inputs larger than L2 (state alone {ar.elem.nbytes / 1e6:.0f} MB; L2 129 MB)"},
                 "e2e": {"value": e2e_value, "unit": "GDOF/s", "h2d_bytes_per_step": n_bytes,
                         "d2h_bytes_per_step": n_bytes},
                 "gpu_launches": launches,
@@ -355,6 +512,8 @@ def main():
                 "cpu_baseline": cpu}
         if mixed_err is not None:
             line["mixed_vs_fp64"] = mixed_err
+        if mixed is not None:
+            line["mixed"] = mixed
         print(json.dumps(line))
     if pg:
         pg.destroy_process_group()

@@ -21,7 +21,8 @@ STATUS_NAMES = {0: "HEXED_OK", -1: "HEXED_ERR_INVALID", -2: "HEXED_ERR_CUDA", -3
 
 BC_FREESTREAM, BC_RIEMANN, BC_NONPENETRATION, BC_COPY, BC_OUTFLOW, BC_PRESSURE_OUTFLOW, BC_NO_SLIP = range(7)
 THERMAL_HEAT_FLUX, THERMAL_ENERGY, THERMAL_EQUILIBRIUM = range(3)
-ARRAY_ELEM, ARRAY_RCACHE, ARRAY_FACE, ARRAY_BC_CACHE, ARRAY_NOM_SIZE, ARRAY_VERT_TSS, ARRAY_BC_NRML = range(7)
+ARRAY_ELEM, ARRAY_RCACHE, ARRAY_FACE, ARRAY_BC_CACHE, ARRAY_NOM_SIZE, ARRAY_VERT_TSS, ARRAY_BC_NRML, \
+    ARRAY_REF_STATE = range(8)
 INT_CAR_CON, INT_BC_CON = 0, 1
 FP64, MIXED = 0, 1
 
@@ -132,6 +133,11 @@ def load_library(path=LIB_PATH):
         "hexed_gpu_stream": ([vp], vp),
         "hexed_gpu_fp64_peak": ([P_double], c_int),
         "hexed_gpu_write_face_range": ([vp, c_int, c_int], c_int),
+        "hexed_gpu_set_reference_state": ([vp, P_double], c_int),
+        "hexed_gpu_set_launch_shape": ([vp, c_int, c_int], c_int),
+        "hexed_gpu_check_conversions": ([P_double, ctypes.c_long, ctypes.POINTER(ctypes.c_long)], c_int),
+        "hexed_gpu_is_admissible": ([vp, P_int, P_int], c_int),
+        "hexed_gpu_launch_shape": ([vp, P_int, P_int], c_int),
         "hexed_gpu_write_range": ([vp, c_int, ctypes.c_long, ctypes.c_long, P_double], c_int),
         "hexed_gpu_read_range": ([vp, c_int, ctypes.c_long, ctypes.c_long, P_double], c_int),
         "hexed_gpu_write_int_range": ([vp, c_int, ctypes.c_long, ctypes.c_long, ctypes.POINTER(c_int)], c_int),

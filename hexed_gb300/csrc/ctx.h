@@ -12,6 +12,7 @@ struct HostTables {
 };
 
 struct Ctx;
+struct LocalDt;   // kernels.cuh
 
 // Per-kernel CUDA-event timing, the device analogue of the reference's per-kernel
 // Stopwatch_tree hooks (include/kernel_factory.hpp:32-45). Off unless enabled.
@@ -31,7 +32,7 @@ struct Profiler {
 
 // Launch sequences of one (n_dim, row_size, precision); all enqueue on Ctx::stream.
 struct OpsTable {
-  void (*compute_euler)(Ctx&, int stage, int compute_residual, int use_filter, bool fuse_bc);
+  void (*compute_euler)(Ctx&, int stage, int compute_residual, int use_filter, bool fuse_bc, const LocalDt& ldt);
   void (*compute_navier_stokes)(Ctx&, int stage, int compute_residual, int use_filter,
                                 const hexed_transport& visc, const hexed_transport& cond, bool fuse_bc);
   void (*max_dt)(Ctx&, double msc, double msd, int local_time, int viscous, const hexed_transport& visc,
@@ -43,6 +44,8 @@ struct OpsTable {
   void (*residual_norm)(Ctx&, double* d_out);
   void (*set_art_visc_admis)(Ctx&, double char_speed);
   void (*segment_residual_norms)(Ctx&, int n_seg, const int* d_begin, const int* d_count, double* d_out);
+  int (*local_elems_per_cta)(int variant);
+  void (*admissible)(Ctx&, int* d_record);
 };
 
 // A captured multi-update sequence and the inputs it was captured for.
@@ -86,9 +89,15 @@ struct Ctx {
   // Jacobian determinant reciprocal [n_def][nq] (both forms)
   double* inv_det;
   // mixed form: FP32 face traces, residual cache and metric-normal copies, and the reference
-  // state the traces are stored against (rho0, ener0 = P0/(gamma-1), means of the initial state)
+  // state of each element [n_elem][nv] the traces and fluxes are offsets from (by default the
+  // mean conserved state of the initial state)
   float* face_f; float* rcache_f; float* nrm_f; float* face_nrml_f; float* def_con_nrml_f; float* bc_nrml_f;
-  double rho0, ener0;
+  double* ref_state;
+  int* record;           // per-element admissibility records [cap elements] (allocated at creation)
+  // launch shape: volume-kernel variant (elements per CTA, see Runner::epb_of) and threads
+  // per CTA of the face kernels
+  int local_variant;
+  int face_threads;
 };
 
 // Bracket one launch with timing events when profiling is enabled.

@@ -88,6 +88,17 @@ int upload_array(T** dst, const T* src, size_t count, const char* name)
   return HEXED_OK;
 }
 
+// Scratch-like arena arrays (state, residual cache, traces, BC caches) may be passed as null:
+// the device copy then starts at zero.
+template <typename T>
+int upload_or_zero(T** dst, const T* src, size_t count, const char* name)
+{
+  if (src || count == 0) return upload_array(dst, src, count, name);
+  HX_CUDA(cudaMalloc((void**)dst, count*sizeof(T)));
+  HX_CUDA(cudaMemset(*dst, 0, count*sizeof(T)));
+  return HEXED_OK;
+}
+
 int validate(const hexed_mesh_desc* d)
 {
   if (!d) return fail(HEXED_ERR_INVALID, "null mesh descriptor");
@@ -149,6 +160,7 @@ size_t array_count(const Ctx* c, int which)
     case HEXED_ARRAY_NOM_SIZE: return n_elem;
     case HEXED_ARRAY_VERT_TSS: return n_elem << c->nd;
     case HEXED_ARRAY_BC_NRML: return (size_t)c->cap_bc_con*c->nd*c->nfq;
+    case HEXED_ARRAY_REF_STATE: return c->ref_state ? n_elem*c->nv : 0;
   }
   return 0;
 }
@@ -163,6 +175,7 @@ double* array_ptr(Ctx* c, int which)
     case HEXED_ARRAY_NOM_SIZE: return c->nom_size;
     case HEXED_ARRAY_VERT_TSS: return c->vert_tss;
     case HEXED_ARRAY_BC_NRML: return c->bc_nrml;
+    case HEXED_ARRAY_REF_STATE: return c->ref_state;
   }
   return nullptr;
 }
@@ -326,16 +339,20 @@ int hexed_gpu_create(const hexed_mesh_desc* d, int precision, hexed_gpu_ctx** ou
   auto up = [&](auto** dst, const auto* src, size_t n, const char* name) {
     if (st == HEXED_OK) st = upload_array(dst, src, n, name);
   };
+  auto up0 = [&](auto** dst, const auto* src, size_t n, const char* name) {
+    if (st == HEXED_OK) st = upload_or_zero(dst, src, n, name);
+  };
   HX_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
-  up(&c->elem, d->elem, n_elem*(c->nv + 3)*c->nq, "elem");
+  up0(&c->elem, d->elem, n_elem*(c->nv + 3)*c->nq, "elem");
   if (precision == HEXED_FP64) {
-    up(&c->rcache, d->rcache, n_elem*c->nv*c->nq, "rcache");
-    up(&c->face, d->face, (size_t)c->n_slot*2*c->nv*c->nfq, "face");
-  } else if (!d->rcache || !d->face) {
-    st = fail(HEXED_ERR_INVALID, "arena arrays `rcache` / `face` are null");
+    up0(&c->rcache, d->rcache, n_elem*c->nv*c->nq, "rcache");
+    up0(&c->face, d->face, (size_t)c->n_slot*2*c->nv*c->nfq, "face");
   } else if (cudaMalloc((void**)&c->rcache_f, n_elem*c->nv*c->nq*sizeof(float)) != cudaSuccess ||
              cudaMalloc((void**)&c->face_f, (size_t)c->n_slot*2*c->nv*c->nfq*sizeof(float)) != cudaSuccess) {
     st = fail(HEXED_ERR_ALLOC, "trace allocation failed");
+  } else {
+    if (!d->rcache) cudaMemset(c->rcache_f, 0, n_elem*c->nv*c->nq*sizeof(float));
+    if (!d->face) cudaMemset(c->face_f, 0, (size_t)c->n_slot*2*c->nv*c->nfq*sizeof(float));
   }
   up(&c->nom_size, d->nom_size, n_elem, "nom_size");
   up(&c->vert_tss, d->vert_tss, n_elem*nvert, "vert_tss");
@@ -346,7 +363,7 @@ int hexed_gpu_create(const hexed_mesh_desc* d, int precision, hexed_gpu_ctx** ou
   up(&c->def_con_nrml, d->def_con_nrml, (size_t)c->n_def_con*nd*c->nfq, "def_con_nrml");
   up(&c->bc_con, d->bc_con, (size_t)c->n_bc_con*4, "bc_con");
   up(&c->bc_nrml, d->bc_nrml, (size_t)c->n_bc_con*nd*c->nfq, "bc_nrml");
-  up(&c->bc_cache, d->bc_cache, (size_t)c->n_bc_con*2*c->nv*c->nfq, "bc_cache");
+  up0(&c->bc_cache, d->bc_cache, (size_t)c->n_bc_con*2*c->nv*c->nfq, "bc_cache");
   up(&c->ref_face, d->ref_face, (size_t)c->n_ref*7, "ref_face");
   up(&c->bc_spec, d->bc_spec, (size_t)c->n_bc_spec, "bc_spec");
   c->n_vert = d->n_vert;
@@ -359,26 +376,24 @@ int hexed_gpu_create(const hexed_mesh_desc* d, int precision, hexed_gpu_ctx** ou
   if (st != HEXED_OK) { hexed_gpu_destroy(c); return st; }
   if (precision == HEXED_MIXED) {
     // staged FP32 traces and residual cache; FP32 copies of the metric normals
-    if (!st) st = transfer(c, HEXED_ARRAY_RCACHE, 0, (long)array_count(c, HEXED_ARRAY_RCACHE), d->rcache, true);
-    if (!st) st = transfer(c, HEXED_ARRAY_FACE, 0, (long)array_count(c, HEXED_ARRAY_FACE), d->face, true);
+    if (!st && d->rcache) st = transfer(c, HEXED_ARRAY_RCACHE, 0, (long)array_count(c, HEXED_ARRAY_RCACHE), d->rcache, true);
+    if (!st && d->face) st = transfer(c, HEXED_ARRAY_FACE, 0, (long)array_count(c, HEXED_ARRAY_FACE), d->face, true);
     if (!st) st = narrow_copy(c, c->jac, &c->nrm_f, (long)c->n_def*(nd*nd + 1)*c->nq);
     if (!st) st = narrow_copy(c, c->face_nrml, &c->face_nrml_f, (long)c->n_def*2*nd*nd*c->nfq);
     if (!st) st = narrow_copy(c, c->def_con_nrml, &c->def_con_nrml_f, (long)c->n_def_con*nd*c->nfq);
     if (!st) st = narrow_copy(c, c->bc_nrml, &c->bc_nrml_f, (long)c->n_bc_con*nd*c->nfq);
-    // reference state: mean density and mean pressure of the initial state
-    double rho_sum = 0., p_sum = 0.;
+    // reference state of every element: the mean conserved state of the initial state (zero
+    // without one; hexed_gpu_set_reference_state or HEXED_ARRAY_REF_STATE set it then)
+    std::vector<double> mean(c->nv, 0.), refs;
     const size_t nq_ = c->nq, nv_ = c->nv;
-    for (size_t e = 0; e < n_elem; ++e) {
-      const double* st_e = d->elem + e*(nv_ + 3)*nq_;
-      for (size_t q = 0; q < nq_; ++q) {
-        double rho = st_e[nd*nq_ + q], kin = 0.;
-        for (size_t k = 0; k < nd; ++k) kin += st_e[k*nq_ + q]*st_e[k*nq_ + q];
-        rho_sum += rho;
-        p_sum += (1.4 - 1.)*(st_e[(nd + 1)*nq_ + q] - .5*kin/rho);
-      }
-    }
-    c->rho0 = rho_sum/double(n_elem*nq_);
-    c->ener0 = p_sum/double(n_elem*nq_)/(1.4 - 1.);
+    for (size_t e = 0; d->elem && e < n_elem; ++e)
+      for (size_t v = 0; v < nv_; ++v)
+        for (size_t q = 0; q < nq_; ++q) mean[v] += d->elem[(e*(nv_ + 3) + v)*nq_ + q];
+    for (size_t v = 0; v < nv_; ++v) mean[v] /= double(n_elem*nq_);
+    refs.resize(n_elem*nv_);
+    for (size_t e = 0; e < n_elem; ++e)
+      for (size_t v = 0; v < nv_; ++v) refs[e*nv_ + v] = mean[v];
+    if (!st) st = upload_array(&c->ref_state, refs.data(), refs.size(), "reference state");
   }
   if (!st && c->n_def) {
     if (cudaMalloc((void**)&c->inv_det, (size_t)c->n_def*c->nq*sizeof(double)) != cudaSuccess) {
@@ -389,8 +404,11 @@ int hexed_gpu_create(const hexed_mesh_desc* d, int precision, hexed_gpu_ctx** ou
     }
   }
   if (st != HEXED_OK) { hexed_gpu_destroy(c); return st; }
+  c->local_variant = 0;
+  c->face_threads = 256;
   c->max_partials = 152*16*8;
   if (cudaMalloc((void**)&c->partials, c->max_partials*sizeof(double)) != cudaSuccess ||
+      cudaMalloc((void**)&c->record, n_elem*sizeof(int)) != cudaSuccess ||
       cudaMalloc((void**)&c->scalars, hx::SC_N*sizeof(double)) != cudaSuccess ||
       cudaMalloc((void**)&c->status, 4*sizeof(int)) != cudaSuccess ||
       cudaMalloc((void**)&c->d_norm, 4*sizeof(double)) != cudaSuccess ||
@@ -413,7 +431,7 @@ int hexed_gpu_destroy(hexed_gpu_ctx* c)
                   c->def_con, c->def_con_nrml, c->bc_con, c->bc_nrml, c->bc_cache, c->ref_face, c->bc_spec,
                   c->scalars, c->partials, c->status, c->d_norm, c->vert_id, c->uncert, c->vmax,
                   c->seg_table, c->seg_out, c->inv_det, c->face_f, c->rcache_f, c->nrm_f, c->face_nrml_f,
-                  c->def_con_nrml_f, c->bc_nrml_f};
+                  c->def_con_nrml_f, c->bc_nrml_f, c->ref_state, c->record};
   for (void* p : ptrs) if (p) cudaFree(p);
   if (c->graph) {
     if (c->graph->exec) cudaGraphExecDestroy(c->graph->exec);
@@ -454,7 +472,7 @@ int hexed_gpu_compute_euler(hexed_gpu_ctx* c, double dt, int i_stage, int comput
   if (i_stage && compute_residual)
     return fail(HEXED_ERR_PRECONDITION, "residual calculation is a single-stage operation");
   if (int st = set_dt(c, dt)) return st;
-  c->ops->compute_euler(*c, i_stage ? 1 : 0, compute_residual, use_filter, false);
+  c->ops->compute_euler(*c, i_stage ? 1 : 0, compute_residual, use_filter, false, hx::LocalDt{0, 0., 0., 0.});
   HX_LAUNCHED();
   return HEXED_OK;
 }
@@ -512,6 +530,90 @@ int hexed_gpu_compute_write_face(hexed_gpu_ctx* c)
   return HEXED_OK;
 }
 
+int hexed_gpu_is_admissible(hexed_gpu_ctx* c, int* admissible, int* record)
+{
+  if (int st = check_ctx(c)) return st;
+  if (!admissible) return fail(HEXED_ERR_INVALID, "null output");
+  c->ops->admissible(*c, c->record);
+  HX_LAUNCHED();
+  HX_CUDA(cudaMemcpyAsync(c->h_pinned, c->status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  if (record)
+    HX_CUDA(cudaMemcpyAsync(record, c->record, (size_t)(c->n_car + c->n_def)*sizeof(int), cudaMemcpyDeviceToHost,
+                            c->stream));
+  HX_CUDA(cudaStreamSynchronize(c->stream));
+  int flags;
+  std::memcpy(&flags, c->h_pinned, sizeof(int));
+  *admissible = !(flags & 1);
+  if (flags & 2) return fail(HEXED_ERR_NUMERICAL, "state is not finite");
+  return HEXED_OK;
+}
+
+int hexed_gpu_check_conversions(const double* host, long n, long* mismatches)
+{
+  if (!mismatches || n < 0 || (n && !host)) return fail(HEXED_ERR_INVALID, "bad arguments");
+  *mismatches = 0;
+  if (n == 0) return HEXED_OK;
+  double* d_in = nullptr;
+  unsigned long long* d_count = nullptr;
+  HX_CUDA(cudaMalloc((void**)&d_in, n*sizeof(double)));
+  if (cudaMalloc((void**)&d_count, sizeof(unsigned long long)) != cudaSuccess) {
+    cudaFree(d_in);
+    return fail(HEXED_ERR_ALLOC, "allocation failed");
+  }
+  unsigned long long count = 0;
+  cudaError_t err = cudaMemcpy(d_in, host, n*sizeof(double), cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) err = cudaMemset(d_count, 0, sizeof(unsigned long long));
+  if (err == cudaSuccess) {
+    hx::k_check_conversions<<<int(std::min<long>((n + 255)/256, 152*16)), 256>>>(d_in, n, d_count);
+    err = cudaGetLastError();
+  }
+  if (err == cudaSuccess) err = cudaMemcpy(&count, d_count, sizeof(count), cudaMemcpyDeviceToHost);
+  cudaFree(d_in);
+  cudaFree(d_count);
+  if (err != cudaSuccess) return fail(HEXED_ERR_CUDA, "conversion check: %s", cudaGetErrorString(err));
+  *mismatches = (long)count;
+  return HEXED_OK;
+}
+
+int hexed_gpu_set_launch_shape(hexed_gpu_ctx* c, int local_variant, int face_threads)
+{
+  if (int st = check_ctx(c)) return st;
+  if (local_variant < 0 || local_variant > 2) return fail(HEXED_ERR_INVALID, "launch-shape variant %d not in 0..2", local_variant);
+  if (local_variant && c->nd == 3) return fail(HEXED_ERR_INVALID, "3D volume kernels have one launch shape");
+  if (face_threads != 64 && face_threads != 128 && face_threads != 256)
+    return fail(HEXED_ERR_INVALID, "face kernels take 64, 128 or 256 threads per CTA, not %d", face_threads);
+  HX_CUDA(cudaStreamSynchronize(c->stream));
+  c->local_variant = local_variant;
+  c->face_threads = face_threads;
+  if (c->graph) c->graph->valid = false;   // the captured launches used the previous shape
+  return HEXED_OK;
+}
+
+int hexed_gpu_launch_shape(hexed_gpu_ctx* c, int* local_elems_per_cta, int* face_threads)
+{
+  if (int st = check_ctx(c)) return st;
+  if (local_elems_per_cta) *local_elems_per_cta = c->ops->local_elems_per_cta(c->local_variant);
+  if (face_threads) *face_threads = c->face_threads;
+  return HEXED_OK;
+}
+
+int hexed_gpu_set_reference_state(hexed_gpu_ctx* c, const double* state)
+{
+  if (int st = check_ctx(c)) return st;
+  if (!state) return fail(HEXED_ERR_INVALID, "null reference state");
+  for (size_t v = 0; v < c->nv; ++v)
+    if (!std::isfinite(state[v])) return fail(HEXED_ERR_INVALID, "non-finite reference state");
+  if (!(state[c->nd] > 0)) return fail(HEXED_ERR_INVALID, "reference density must be positive");
+  if (c->precision != HEXED_MIXED) return HEXED_OK;
+  const size_t n = (size_t)c->cap_car + c->n_def;
+  std::vector<double> refs(n*c->nv);
+  for (size_t e = 0; e < n; ++e)
+    for (size_t v = 0; v < c->nv; ++v) refs[e*c->nv + v] = state[v];
+  HX_CUDA(cudaMemcpyAsync(c->ref_state, refs.data(), refs.size()*sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  HX_CUDA(cudaStreamSynchronize(c->stream));
+  return HEXED_OK;
+}
+
 int hexed_gpu_write_face_range(hexed_gpu_ctx* c, int elem_begin, int elem_count)
 {
   if (int st = check_ctx(c)) return st;
@@ -548,22 +650,37 @@ int hexed_gpu_apply_flux_bcs(hexed_gpu_ctx* c)
 }
 
 namespace {
-// Enqueues one Solver::update (src/Solver.cpp:834-886) on the context's stream.
-int enqueue_update(hexed_gpu_ctx* c, const hexed_update_params* p)
+// Enqueues one Solver::update (src/Solver.cpp:834-886) on the context's stream. With local
+// time stepping and no diffusion the step is known on the host (the global part is 1, times
+// max_time_step and the Chebyshev factor, as k_finalize_dt would give): the first stage's
+// volume kernel then computes each point's time-step scale itself (LocalDt mode 1) instead
+// of a separate Max_dt pass, with the same arithmetic, and *host_dt receives the step.
+// Otherwise *host_dt is NaN and the step stays on the device.
+int enqueue_update(hexed_gpu_ctx* c, const hexed_update_params* p, double* host_dt = nullptr)
 {
+  if (host_dt) *host_dt = std::nan("");
   if (p->av_admis_char_speed > 0) {
     // Case.cpp:432: set_art_visc_admis before the update when diffusive_admissibility is on
     if (c->n_vert <= 0) return fail(HEXED_ERR_INVALID, "artificial viscosity needs the arena's vertex table");
     c->ops->set_art_visc_admis(*c, p->av_admis_char_speed);
   }
+  const bool fuse_dt = p->local_time && !p->use_ldg;
   const double max_cheby = chebyshev_step(p->n_cheby_flow, p->n_cheby_flow - 1);
   for (int i_flow = 0; i_flow < p->flow_iters; ++i_flow) {
     for (int i_cheby = 0; i_cheby < p->n_cheby_flow; ++i_cheby) {
-      c->ops->max_dt(*c, p->max_safety/max_cheby, p->max_safety, p->local_time, p->use_ldg, p->visc, p->cond,
-                     p->max_time_step, chebyshev_step(p->n_cheby_flow, i_cheby));
+      const double msc = p->max_safety/max_cheby, msd = p->max_safety;
+      const double cheby = chebyshev_step(p->n_cheby_flow, i_cheby);
+      if (fuse_dt) {
+        const double dt = std::fmin(1., p->max_time_step)*cheby;
+        c->ops->compute_euler(*c, 0, 0, p->use_filter, true, hx::LocalDt{1, msc, msd, dt});
+        c->ops->compute_euler(*c, 1, 0, p->use_filter, true, hx::LocalDt{2, msc, msd, dt});
+        if (host_dt) *host_dt = dt;
+        continue;
+      }
+      c->ops->max_dt(*c, msc, msd, p->local_time, p->use_ldg, p->visc, p->cond, p->max_time_step, cheby);
       for (int i = 0; i < 2; ++i) {
         if (p->use_ldg && !i) c->ops->compute_navier_stokes(*c, 0, 0, p->use_filter, p->visc, p->cond, true);
-        else c->ops->compute_euler(*c, i, 0, p->use_filter, true);
+        else c->ops->compute_euler(*c, i, 0, p->use_filter, true, hx::LocalDt{0, 0., 0., 0.});
       }
     }
   }
@@ -696,12 +813,17 @@ int hexed_gpu_update(hexed_gpu_ctx* c, const hexed_update_params* p, double* out
 {
   if (int st = check_ctx(c)) return st;
   if (!p || p->n_cheby_flow < 1 || p->flow_iters < 0) return fail(HEXED_ERR_INVALID, "bad update parameters");
-  if (int st = enqueue_update(c, p)) return st;
+  double host_dt;
+  if (int st = enqueue_update(c, p, &host_dt)) return st;
   HX_LAUNCHED();
   if (out_dt) {
-    HX_CUDA(cudaMemcpyAsync(c->h_pinned, c->scalars + hx::SC_DT, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    HX_CUDA(cudaStreamSynchronize(c->stream));
-    *out_dt = c->h_pinned[0];
+    if (!std::isnan(host_dt)) {
+      *out_dt = host_dt;
+    } else {
+      HX_CUDA(cudaMemcpyAsync(c->h_pinned, c->scalars + hx::SC_DT, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+      HX_CUDA(cudaStreamSynchronize(c->stream));
+      *out_dt = c->h_pinned[0];
+    }
   }
   return HEXED_OK;
 }
@@ -712,7 +834,7 @@ int hexed_gpu_compute_residual(hexed_gpu_ctx* c, const hexed_update_params* p)
   if (!p) return fail(HEXED_ERR_INVALID, "null parameters");
   if (int st = set_dt(c, 1.)) return st;
   if (p->use_ldg) c->ops->compute_navier_stokes(*c, 0, 1, p->use_filter, p->visc, p->cond, true);
-  else c->ops->compute_euler(*c, 0, 1, p->use_filter, true);
+  else c->ops->compute_euler(*c, 0, 1, p->use_filter, true, hx::LocalDt{0, 0., 0., 0.});
   HX_LAUNCHED();
   return HEXED_OK;
 }

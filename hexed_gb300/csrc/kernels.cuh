@@ -67,9 +67,9 @@ struct Dev {
   double* bc_cache;
   const int* ref_face;
   const hexed_bc_spec* bc_spec;
-  // Reference state of the mixed form: face traces hold rho - rho0 and E - ener0, and the
-  // momentum flux carries p - (gamma-1)*ener0. Zero in the FP64 form.
-  double rho0, ener0;
+  // Mixed form: reference state of each element [n_elem][nv]; its face traces, and the
+  // fluxes its kernels form, are differences from it (see RefState). Null in the FP64 form.
+  const double* ref;
   double* scalars;       // [0] dt of the current stage, [1] raw max_dt, ...
   double* partials;      // per-block reduction scratch
   int* status;           // device-side error flags
@@ -91,6 +91,68 @@ struct Shape {
 };
 
 template <typename T> __device__ __forceinline__ T load(const T* p) { return __ldg(p); }
+
+// ------------------------------------------------------------------- conversions (mixed form)
+// IEEE 754 binary64 <-> binary32 conversions written with integer operations, from the
+// format definitions. The hardware conversions between double and float issue on the FP64
+// pipe, which on this GPU runs at a small fraction of the FP32 rate and was the busiest unit
+// of the mixed-form kernels; these run on the integer pipes. f32_of rounds to nearest even
+// (as __double2float_rn does) where the result is a normal float, and gives signed zero
+// below the normal range (no float subnormals), +-inf above it and NaN for NaN. f64_of is
+// exact for normal floats, gives signed zero for float zeros and subnormals and keeps inf
+// and NaN.
+__device__ __forceinline__ float f32_of(double x)
+{
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned sign = hi & 0x80000000u;
+  const unsigned ex = (hi >> 20) & 0x7ffu;
+  const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);   // leading 23 mantissa bits
+  const unsigned rest = lo & 0x1fffffffu;                    // the 29 bits rounded away
+  const int e = int(ex) - (1023 - 127);                      // biased float exponent
+  unsigned bits = (unsigned(e) << 23) + m;
+  bits += (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ? 1u : 0u;  // a carry may
+  bits = e >= 255 ? 0x7f800000u : bits;                      // reach the exponent (inf)
+  bits = (ex == 0x7ffu && (m | rest)) ? 0x7fc00000u : bits;
+  bits = e <= 0 ? 0u : bits;
+  return __uint_as_float(sign | bits);
+}
+
+__device__ __forceinline__ double f64_of(float f)
+{
+  const unsigned b = __float_as_uint(f);
+  const unsigned sign = b & 0x80000000u, ex = (b >> 23) & 0xffu, m = b & 0x7fffffu;
+  unsigned hi = sign | ((ex + (1023u - 127u)) << 20) | (m >> 3);
+  unsigned lo = m << 29;
+  if (ex == 0u) { hi = sign; lo = 0u; }
+  if (ex == 0xffu) hi = sign | 0x7ff00000u | (m >> 3) | (m ? 0x80000u : 0u);
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+// Self-check of f32_of / f64_of against the hardware conversions (__double2float_rn and
+// the float-to-double widening): counts inputs whose results differ in any bit, skipping
+// inputs whose float result is subnormal (f32_of flushes those to zero by design).
+static __global__ void k_check_conversions(const double* in, long n, unsigned long long* mismatches)
+{
+  for (long i = blockIdx.x*(long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x*blockDim.x) {
+    const double x = in[i];
+    const float hw = __double2float_rn(x);
+    const float sw = f32_of(x);
+    const float ahw = fabsf(hw);
+    if (ahw > 0.f && ahw < 1.17549435e-38f) continue;
+    bool bad = isnan(hw) ? !isnan(sw) : __float_as_uint(hw) != __float_as_uint(sw);
+    const double wide_hw = double(hw), wide_sw = f64_of(hw);
+    bad = bad || (isnan(wide_hw) ? !isnan(wide_sw) : __double_as_longlong(wide_hw) != __double_as_longlong(wide_sw));
+    if (bad) atomicAdd(mismatches, 1ull);
+  }
+}
+
+// double -> compute type R (identity for double)
+template <typename R>
+__device__ __forceinline__ R to_R(double x)
+{
+  if constexpr (std::is_same<R, float>::value) return f32_of(x);
+  else return x;
+}
 
 // ------------------------------------------------------------------- PDE pieces
 // Navier_stokes<visc>::Pde::Computation (include/pde.hpp:72-175), one qpoint.
@@ -137,17 +199,69 @@ __device__ __forceinline__ R char_speed(const R* s, R inv_mass) // pde.hpp:161-1
   return sound_speed + sqrt(sq)*inv_mass;
 }
 
-// Transport_model with its constants folded on the host (include/Transport_model.hpp:21-44)
-struct Tm {
-  double const_val, ref_val, inv_sqrt_ref_temp, ref_temp_plus_offset, temp_offset;
+// Reference state of the mixed form and the parts of its flux the offset flux needs.
+template <int ND, typename R>
+struct RefState {
+  R s[ND + 2];   // conserved reference state
+  R v[ND];       // its velocity
+  R v_sq;        // |v|^2
+  R h;           // E + p
+  __device__ __forceinline__ void set(const double* ref)
+  {
+    #pragma unroll
+    for (int i = 0; i < ND + 2; ++i) s[i] = to_R<R>(ref[i]);
+    const R inv = R(1)/s[ND];
+    v_sq = 0;
+    #pragma unroll
+    for (int j = 0; j < ND; ++j) { v[j] = s[j]*inv; v_sq += v[j]*v[j]; }
+    h = s[ND + 1] + R(heat_rat - 1.)*(s[ND + 1] - R(.5)*s[ND]*v_sq);
+  }
 };
-inline Tm make_tm(const hexed_transport& t)
+
+// f(u).n - f(u_ref).n of the convective flux (pde.hpp:108-122) from the offset state
+// d = u - u_ref, with c the Conv of the full state u. Every term is an offset times a bounded
+// factor, so in float the result carries the relative accuracy of the offsets and not of the
+// full fluxes (no difference of nearly equal fluxes is formed):
+//   dv = (dm - v_ref drho)/rho, dp = (gamma-1)(dE - (drho |v_ref|^2 + rho (v + v_ref).dv)/2),
+//   mass dm.n, momentum dm (v.n) + m_ref (dv.n) + dp n, energy (dE + dp)(v.n) + h_ref (dv.n).
+// The reference flux itself drops out of the scheme: its volume derivative and its face
+// terms cancel by the discrete metric identity (free-stream preservation).
+template <int ND, typename R>
+__device__ __forceinline__ void flux_delta(const R* u, const R* d, const RefState<ND, R>& r, const Conv<ND, R>& c,
+                                           const R* n, R* f)
 {
-  return {t.const_val, t.ref_val, 1./sqrt(t.ref_temp), t.ref_temp + t.temp_offset, t.temp_offset};
+  R v[ND], dv[ND];
+  R dkin2 = d[ND]*r.v_sq;
+  #pragma unroll
+  for (int j = 0; j < ND; ++j) {
+    v[j] = u[j]*c.inv_mass;
+    dv[j] = (d[j] - r.v[j]*d[ND])*c.inv_mass;
+    dkin2 += u[ND]*(v[j] + r.v[j])*dv[j];
+  }
+  const R dp = R(heat_rat - 1.)*(d[ND + 1] - R(.5)*dkin2);
+  R vn = 0, dvn = 0, dmn = 0;
+  #pragma unroll
+  for (int j = 0; j < ND; ++j) { vn += v[j]*n[j]; dvn += dv[j]*n[j]; dmn += d[j]*n[j]; }
+  #pragma unroll
+  for (int i = 0; i < ND; ++i) f[i] = d[i]*vn + r.s[i]*dvn + dp*n[i];
+  f[ND] = dmn;
+  f[ND + 1] = (d[ND + 1] + dp)*vn + r.h*dvn;
+}
+
+// Transport_model constants folded on the host, in the compute type of the kernel
+// (include/Transport_model.hpp:21-44).
+template <typename R>
+struct TmT {
+  R const_val, ref_val, inv_sqrt_ref_temp, ref_temp_plus_offset, temp_offset;
+};
+template <typename R>
+inline TmT<R> make_tm(const hexed_transport& t)
+{
+  return {R(t.const_val), R(t.ref_val), R(1./sqrt(t.ref_temp)), R(t.ref_temp + t.temp_offset), R(t.temp_offset)};
 }
 
 template <typename R>
-__device__ __forceinline__ R transport_coef(const Tm& t, R sqrt_temp) // Transport_model.hpp:35-38
+__device__ __forceinline__ R transport_coef(const TmT<R>& t, R sqrt_temp) // Transport_model.hpp:35-38
 {
   R r = sqrt_temp*R(t.inv_sqrt_ref_temp);
   R p3 = r*r*r;
@@ -158,7 +272,7 @@ template <int ND, typename R>
 struct DiffScalars { // compute_scalars_diff (pde.hpp:130-138)
   R bulk_av, laplacian_av, mu, energy_cond;
   __device__ __forceinline__ DiffScalars(const R* s, const Conv<ND, R>& c, R bulk, R lap,
-                                         const Tm& visc, const Tm& cond)
+                                         const TmT<R>& visc, const TmT<R>& cond)
   {
     bulk_av = fabs(bulk);
     laplacian_av = fabs(lap);
@@ -273,13 +387,13 @@ struct STab {
 // ------------------------------------------------------------------- Write_face helper
 // Extrapolate an element's state (shared memory, [nv][nq]) to its 2nd face slots
 // (Spatial::Write_face, include/Spatial.hpp:41-57). Called by all threads of the CTA.
-template <int ND, int RS, typename R, typename FaceT>
+template <int ND, int RS, typename R, typename FaceT, int EPB = Shape<ND, RS>::epb>
 __device__ __forceinline__ void write_faces_from_smem(const Dev<FaceT>& m, const STab<RS, R>& st,
                                                       const R* s_u, int e0, int e_end)
 {
   using S = Shape<ND, RS>;
   constexpr int nq = S::nq, nfq = S::nfq, nv = S::nv;
-  constexpr int n_task = S::epb*ND*nv*nfq;
+  constexpr int n_task = EPB*ND*nv*nfq;
   for (int task = threadIdx.x; task < n_task; task += blockDim.x) {
     int r = task%nfq;
     int rest = task/nfq;
@@ -306,38 +420,88 @@ __device__ __forceinline__ void write_faces_from_smem(const Dev<FaceT>& m, const
 
 // ------------------------------------------------------------------- Local
 // Spatial::Local (include/Spatial.hpp:326-509) fused with the stage update and Write_face.
-template <int ND, int RS, typename R, bool DEF, bool VISC>
+template <int ND, int RS, typename R, bool DEF, bool VISC, int EPB = Shape<ND, RS>::epb>
 struct LocalSmem {
   using S = Shape<ND, RS>;
   static constexpr int per_elem = S::nv*S::nq            // s_u
                                 + ND*S::nv*S::nq         // s_f
                                 + (VISC ? ND*S::nv*S::nq : 0)   // s_g
                                 + ND*2*S::nv*S::nfq;     // s_bf
-  static constexpr size_t bytes = sizeof(STab<RS, R>) + sizeof(R)*(size_t)per_elem*S::epb + 16;
+  static constexpr size_t bytes = sizeof(STab<RS, R>) + sizeof(R)*(size_t)per_elem*EPB + 16;
 };
 
-// Offset form of the state used for face traces and derivatives: the mixed form subtracts the
-// reference density and energy (in double, before narrowing), so the FP32 values carry the
-// variation and not the large mean; the FP64 form keeps the state as it is (references 0).
-template <int ND, typename R, typename FaceT>
-__device__ __forceinline__ R offset_var(const Dev<FaceT>& m, int v, double x)
-{
-  if (v == ND) return R(x - m.rho0);
-  if (v == ND + 1) return R(x - m.ener0);
-  return R(x);
-}
-
-template <int ND, int RS, typename R, bool DEF, bool VISC, typename FaceT>
-__global__ void __launch_bounds__(Shape<ND, RS>::threads)
-k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int compute_residual, int use_filter,
-        Tm visc, Tm cond)
+// Max_dt of one quadrature point (include/Spatial.hpp:793-826): the local time step from the
+// vertex time-step scales interpolated to the point, the characteristic speed and, for
+// diffusion, the diffusivity. Shared by k_max_dt and the fused local-time path of k_local.
+template <int ND, int RS, typename R, bool VISC, typename FaceT>
+__device__ __forceinline__ R point_step(const Dev<FaceT>& m, const Tab<RS>& tab, int e, int q, R inv_cfl_c,
+                                        R inv_cfl_d, const TmT<R>& visc, const TmT<R>& cond)
 {
   using S = Shape<ND, RS>;
-  constexpr int nq = S::nq, nfq = S::nfq, nv = S::nv, EPB = S::epb;
-  // Mixed form: the momentum flux carries p - P0 with P0 = (gamma-1)*ener0, the face traces
-  // the offset state. The P0*n parts of interior and face fluxes cancel by the discrete metric
-  // identity sum_d [D.n_d + lift.(n_face - B.n_d)] = 0 (free-stream preservation), so this is
-  // the same scheme up to roundoff, without the cancellation of p ~ P0 in float.
+  constexpr int nq = S::nq, nv = S::nv, nvert = S::nvert;
+  const double* state = m.elem + (size_t)e*(nv + 3)*nq;
+  R vals[nvert];
+  #pragma unroll
+  for (int i = 0; i < nvert; ++i) vals[i] = to_R<R>(m.vert_tss[(size_t)e*nvert + i]);
+  int stride = nvert;
+  #pragma unroll
+  for (int d = 0; d < ND; ++d) {
+    const R coord = to_R<R>(tab.node[(q/ipow(RS, ND - 1 - d))%RS]);
+    stride /= 2;
+    #pragma unroll
+    for (int i = 0; i < (nvert >> (d + 1)); ++i) vals[i] += coord*(vals[i + stride] - vals[i]);
+  }
+  const R spacing = vals[0];
+  R s[nv];
+  #pragma unroll
+  for (int v = 0; v < nv; ++v) s[v] = to_R<R>(state[v*nq + q]);
+  const R inv_spacing = R(1)/spacing;
+  Conv<ND, R> c(s);
+  R scale = 0;
+  scale += char_speed<ND, R>(s, c.inv_mass)*inv_cfl_c*inv_spacing;
+  if constexpr (VISC) {
+    DiffScalars<ND, R> df(s, c, to_R<R>(state[(nv + 1)*nq + q]), to_R<R>(state[(nv + 2)*nq + q]), visc, cond);
+    R diffusivity = fabs(df.laplacian_av) + fmax(fabs(df.bulk_av) + df.mu*c.inv_mass, df.energy_cond*c.inv_mass);
+    scale += diffusivity*inv_cfl_d*inv_spacing*inv_spacing;
+  }
+  return R(1)/scale;
+}
+
+// Time step of a k_local launch. mode 0: the step is scalars[SC_DT] and the time-step scale
+// row of the state holds each point's scale (written by k_max_dt). mode 1 (first stage of an
+// update with local time stepping): the step is `dt` and the kernel computes each point's
+// scale itself (point_step, as k_max_dt would) and stores it. mode 2: the step is `dt`, the
+// scale row is read.
+struct LocalDt {
+  int mode;
+  double msc, msd, dt;
+};
+
+// Threads of a volume-kernel CTA holding EPB elements (whole warps).
+template <int ND, int RS, int EPB>
+struct Tile { static constexpr int threads = (EPB*ipow(RS, ND) + 31)/32*32; };
+
+// Offset form of the state used for face traces and derivatives: the mixed form subtracts the
+// element's reference state (in double, before narrowing), so the FP32 values carry the
+// variation and not the large mean; the FP64 form keeps the state as it is.
+template <int ND, typename R, typename FaceT>
+__device__ __forceinline__ R offset_var(const Dev<FaceT>& m, int e, int v, double x)
+{
+  if constexpr (std::is_same<FaceT, double>::value) return R(x);
+  else return to_R<R>(x - m.ref[(size_t)e*(ND + 2) + v]);
+}
+
+template <int ND, int RS, typename R, bool DEF, bool VISC, typename FaceT, int EPB>
+__device__ __forceinline__ void local_body(Dev<FaceT> m, const Tab<RS>& tab, int e_begin, int e_end, int stage,
+                                           int compute_residual, int use_filter, const TmT<R>& visc,
+                                           const TmT<R>& cond, const LocalDt& ldt)
+{
+  using S = Shape<ND, RS>;
+  constexpr int nq = S::nq, nfq = S::nfq, nv = S::nv;
+  // Mixed form: traces and convective fluxes are offsets from the element's reference state
+  // (flux_delta). The reference flux's parts of interior and face fluxes cancel by the discrete
+  // metric identity sum_d [D.n_d + lift.(n_face - B.n_d)] = 0 (free-stream preservation), so
+  // this is the same scheme up to roundoff, without differences of nearly equal floats.
   constexpr bool split = !std::is_same<FaceT, double>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   STab<RS, R>& st = *reinterpret_cast<STab<RS, R>*>(smem_raw);
@@ -354,11 +518,12 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
   const int ed = e - m.n_car;
   const double d_pos = active ? m.nom_size[e] : 1.;
   const double inv_dpos = 1./d_pos;
+  const R inv_dpos_r = split ? R(1)/to_R<R>(d_pos) : R(inv_dpos);
   const double* state_g = m.elem + (size_t)e*(nv + 3)*nq;
 
   R u[nv + 2];   // state + bulk AV + Laplacian AV (include/pde.hpp:79-84)
   R up[nv];      // offset form of the state
-  R p_rel = 0;
+  const double* ref_e = split ? m.ref + (size_t)(active ? e : 0)*nv : nullptr;
   R nrm[ND][ND]; // nrm[j][i] = comp.normal(j, i)
   #pragma unroll
   for (int i = 0; i < ND; ++i)
@@ -368,18 +533,12 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
     #pragma unroll
     for (int v = 0; v < nv; ++v) {
       const double x = state_g[v*nq + q];
-      up[v] = offset_var<ND, R>(m, v, x);
-      u[v] = split ? (v == ND ? R(m.rho0) + up[v] : v == ND + 1 ? R(m.ener0) + up[v] : up[v]) : R(x);
+      up[v] = offset_var<ND, R>(m, e, v, x);
+      if constexpr (split) u[v] = to_R<R>(ref_e[v]) + up[v];
+      else u[v] = R(x);
     }
-    u[nv] = R(state_g[(nv + 1)*nq + q]);
-    u[nv + 1] = R(state_g[(nv + 2)*nq + q]);
-    if constexpr (split) {
-      R kin = 0;
-      #pragma unroll
-      for (int d = 0; d < ND; ++d) kin += u[d]*u[d];
-      kin *= R(.5)/u[ND];
-      p_rel = R(heat_rat - 1.)*(up[ND + 1] - kin);
-    }
+    u[nv] = to_R<R>(state_g[(nv + 1)*nq + q]);
+    u[nv + 1] = to_R<R>(state_g[(nv + 2)*nq + q]);
     if constexpr (DEF) {
       const FaceT* nr = m.nrm + (size_t)ed*(ND*ND + 1)*nq;
       #pragma unroll
@@ -454,7 +613,7 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
             R l = 0;
             l += st.lift[i*2]*bf[v*nfq + row_of[d]];
             l += st.lift[i*2 + 1]*bf[(nv + v)*nfq + row_of[d]];
-            grad[v][d] = (acc + l)*R(inv_dpos);
+            grad[v][d] = (acc + l)*inv_dpos_r;
           }
         }
       }
@@ -508,7 +667,7 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
               R l = 0;
               l += st.lift[i*2]*bf[v*nfq + row_of[d]];
               l += st.lift[i*2 + 1]*bf[(nv + v)*nfq + row_of[d]];
-              grad[v][j] = grad[v][j] + (acc + l)*R(inv_dpos);
+              grad[v][j] = grad[v][j] + (acc + l)*inv_dpos_r;
             }
           }
         }
@@ -520,19 +679,21 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
   // ---- fluxes (Spatial.hpp:405-442)
   if (active) {
     Conv<ND, R> c(u);
-    const R p_mom = split ? p_rel : c.pressure;
+    RefState<ND, R> rs;   // formed here, not kept live through the gradient part
+    if constexpr (split) rs.set(ref_e);
     #pragma unroll
     for (int i = 0; i < ND; ++i) {
       R col[ND], f[nv];
       #pragma unroll
       for (int j = 0; j < ND; ++j) col[j] = nrm[j][i];
-      c.flux(u, col, f, p_mom);
+      if constexpr (split) flux_delta<ND, R>(u, up, rs, c, col, f);
+      else c.flux(u, col, f);
       #pragma unroll
       for (int v = 0; v < nv; ++v) my_f[(i*nv + v)*nq + q] = f[v];
     }
     if constexpr (VISC) {
       R g[nv][ND];
-      const R inv_det = DEF ? R(m.inv_det[(size_t)ed*nq + q]) : R(1);
+      const R inv_det = DEF ? to_R<R>(m.inv_det[(size_t)ed*nq + q]) : R(1);
       #pragma unroll
       for (int v = 0; v < nv; ++v)
         #pragma unroll
@@ -637,17 +798,27 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
 
   // ---- stage update (Spatial.hpp:484-503): the state accumulates in double
   if (active) {
-    const double dt = m.scalars[SC_DT];
+    const double dt = ldt.mode ? ldt.dt : m.scalars[SC_DT];
     const double update_coef = stage ? dt*tab.step_ratio : dt;
     double* st_w = m.elem + (size_t)e*(nv + 3)*nq;
     FaceT* rc = m.rcache + (size_t)e*nv*nq;
-    double mult = update_coef*st_w[nv*nq + q]*inv_dpos;
-    if constexpr (DEF) mult *= m.inv_det[(size_t)ed*nq + q];
-    #pragma unroll
-    for (int v = 0; v < nv; ++v) {
-      double uu;
-      if constexpr (!split) {
-        uu = double(rate[v]);
+    double tss;
+    if (ldt.mode == 1) {
+      const R inv_cfl_c = R(1./(tab.max_cfl*ldt.msc));
+      const R inv_cfl_d = R(1./(-2/tab.min_eig_diffusion*ldt.msd));
+      const R step = point_step<ND, RS, R, VISC>(m, tab, e, q, inv_cfl_c, inv_cfl_d, visc, cond);
+      if constexpr (split) tss = f64_of(step);
+      else tss = step;
+      st_w[nv*nq + q] = tss;
+    } else {
+      tss = st_w[nv*nq + q];
+    }
+    if constexpr (!split) {
+      double mult = update_coef*tss*inv_dpos;
+      if constexpr (DEF) mult *= m.inv_det[(size_t)ed*nq + q];
+      #pragma unroll
+      for (int v = 0; v < nv; ++v) {
+        double uu = double(rate[v]);
         if (stage) {
           uu -= rc[v*nq + q];
         } else {
@@ -655,7 +826,21 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
           if constexpr (VISC) uu += double(vrate[v]);
         }
         uu *= mult;
-      } else {
+        if (compute_residual) rc[v*nq + q] = FaceT(uu);
+        else {
+          double nu = st_w[v*nq + q] + uu;
+          st_w[v*nq + q] = nu;
+          up[v] = offset_var<ND, R>(m, e, v, nu);
+        }
+      }
+    } else {
+      // Mixed form: the increment is formed in float; only its accumulation into the state
+      // is a double add. The offset-form trace of the new state is the old one plus the
+      // increment.
+      R mult = to_R<R>(update_coef)*to_R<R>(tss)*inv_dpos_r;
+      if constexpr (DEF) mult *= to_R<R>(m.inv_det[(size_t)ed*nq + q]);
+      #pragma unroll
+      for (int v = 0; v < nv; ++v) {
         R ur = rate[v];
         if (stage) {
           ur -= R(rc[v*nq + q]);
@@ -663,13 +848,12 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
           rc[v*nq + q] = FaceT(ur);
           if constexpr (VISC) ur += vrate[v];
         }
-        uu = double(ur)*mult;
-      }
-      if (compute_residual) rc[v*nq + q] = FaceT(uu);
-      else {
-        double nu = st_w[v*nq + q] + uu;
-        st_w[v*nq + q] = nu;
-        up[v] = offset_var<ND, R>(m, v, nu);
+        const R inc = ur*mult;
+        if (compute_residual) rc[v*nq + q] = FaceT(inc);
+        else {
+          st_w[v*nq + q] = st_w[v*nq + q] + f64_of(inc);
+          up[v] += inc;
+        }
       }
     }
   }
@@ -681,8 +865,31 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
       for (int v = 0; v < nv; ++v) my_u[v*nq + q] = up[v];
     }
     __syncthreads();
-    write_faces_from_smem<ND, RS, R, FaceT>(m, st, s_u, e0, e_end);
+    write_faces_from_smem<ND, RS, R, FaceT, EPB>(m, st, s_u, e0, e_end);
   }
+}
+
+// Spatial::Local (include/Spatial.hpp:293-510), one thread per quadrature point, EPB
+// elements per CTA (see local_body).
+template <int ND, int RS, typename R, bool DEF, bool VISC, typename FaceT, int EPB = Shape<ND, RS>::epb>
+__global__ void __launch_bounds__(Tile<ND, RS, EPB>::threads)
+k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int compute_residual, int use_filter,
+        TmT<R> visc, TmT<R> cond, LocalDt ldt)
+{
+  local_body<ND, RS, R, DEF, VISC, FaceT, EPB>(m, tab, e_begin, e_end, stage, compute_residual, use_filter, visc, cond,
+                                              ldt);
+}
+
+// The float viscous volume kernel with its registers capped for three resident CTAs per SM:
+// it holds the offset state, its gradient and the reference state at once, and its default
+// allocation drops it to two.
+template <int ND, int RS, typename R, bool DEF, bool VISC, typename FaceT, int EPB = Shape<ND, RS>::epb>
+__global__ void __launch_bounds__(Tile<ND, RS, EPB>::threads, 3)
+k_local_3cta(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int compute_residual, int use_filter,
+             TmT<R> visc, TmT<R> cond, LocalDt ldt)
+{
+  local_body<ND, RS, R, DEF, VISC, FaceT, EPB>(m, tab, e_begin, e_end, stage, compute_residual, use_filter, visc, cond,
+                                              ldt);
 }
 
 // ------------------------------------------------------------------- Reconcile_ldg_flux
@@ -763,18 +970,32 @@ k_reconcile_ldg(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int compute_r
   if (active) {
     const double dt = m.scalars[SC_DT];
     double* st_w = m.elem + (size_t)e*(nv + 3)*nq;
-    double mult = dt*st_w[nv*nq + q]*(1./m.nom_size[e]);
-    if constexpr (DEF) mult *= m.inv_det[(size_t)(e - m.n_car)*nq + q];
-    if (compute_residual) {
-      FaceT* rc = m.rcache + (size_t)e*nv*nq;
-      #pragma unroll
-      for (int v = 0; v < nv; ++v) rc[v*nq + q] = FaceT(double(rc[v*nq + q]) + double(tr[v])*mult);
+    if constexpr (std::is_same<FaceT, double>::value) {
+      double mult = dt*st_w[nv*nq + q]*(1./m.nom_size[e]);
+      if constexpr (DEF) mult *= m.inv_det[(size_t)(e - m.n_car)*nq + q];
+      if (compute_residual) {
+        FaceT* rc = m.rcache + (size_t)e*nv*nq;
+        #pragma unroll
+        for (int v = 0; v < nv; ++v) rc[v*nq + q] = FaceT(double(rc[v*nq + q]) + double(tr[v])*mult);
+      } else {
+        #pragma unroll
+        for (int v = 0; v < nv; ++v) st_w[v*nq + q] += double(tr[v])*mult;
+      }
     } else {
-      #pragma unroll
-      for (int v = 0; v < nv; ++v) st_w[v*nq + q] += double(tr[v])*mult;
+      // mixed form: increment in float, accumulated into the double state (see k_local)
+      R mult = to_R<R>(dt)*to_R<R>(st_w[nv*nq + q])*(R(1)/to_R<R>(m.nom_size[e]));
+      if constexpr (DEF) mult *= to_R<R>(m.inv_det[(size_t)(e - m.n_car)*nq + q]);
+      if (compute_residual) {
+        FaceT* rc = m.rcache + (size_t)e*nv*nq;
+        #pragma unroll
+        for (int v = 0; v < nv; ++v) rc[v*nq + q] = rc[v*nq + q] + tr[v]*mult;
+      } else {
+        #pragma unroll
+        for (int v = 0; v < nv; ++v) st_w[v*nq + q] += f64_of(tr[v]*mult);
+      }
     }
     #pragma unroll
-    for (int v = 0; v < nv; ++v) my_u[v*nq + q] = offset_var<ND, R>(m, v, st_w[v*nq + q]);
+    for (int v = 0; v < nv; ++v) my_u[v*nq + q] = offset_var<ND, R>(m, e, v, st_w[v*nq + q]);
   }
   __syncthreads();
   write_faces_from_smem<ND, RS, R, FaceT>(m, st, s_u, e0, e_end);
@@ -789,9 +1010,16 @@ __device__ __forceinline__ void neighbor_point(const Dev<FaceT>& m, int slot0, i
 {
   using S = Shape<ND, RS>;
   constexpr int nfq = S::nfq, nv = S::nv;
-  // mixed form: traces are stored in offset form (rho - rho0, E - ener0) and the momentum
-  // flux carries p - P0 (see k_local); nothing on the faces needs double
+  // mixed form: traces are offsets from the reference state of the connection's elements
+  // (one solve, one reference) and so are the fluxes (flux_delta); nothing here needs double
   constexpr bool split = !std::is_same<FaceT, double>::value;
+  RefState<ND, R> rs;
+  int e_ref = 0;
+  if constexpr (split) {
+    const int n_elem_slots = m.n_elem*2*ND;
+    e_ref = slot0 < n_elem_slots ? slot0/(2*ND) : slot1 < n_elem_slots ? slot1/(2*ND) : 0;
+    rs.set(m.ref + (size_t)e_ref*nv);
+  }
   const bool deformed = nrml != nullptr;
   int sign0 = 1, sign1 = 1;
   if (deformed) {
@@ -806,7 +1034,7 @@ __device__ __forceinline__ void neighbor_point(const Dev<FaceT>& m, int slot0, i
   for (int v = 0; v < nv; ++v) {
     if constexpr (split) {
       o0[v] = R(f0[v*nfq + q]);
-      o1[v] = ghost_override ? offset_var<ND, R>(m, v, ghost_override[v]) : R(f1[v*nfq + q1]);
+      o1[v] = ghost_override ? offset_var<ND, R>(m, e_ref, v, ghost_override[v]) : R(f1[v*nfq + q1]);
       jump[v] = o0[v] - o1[v];
     } else {
       const double a = double(f0[v*nfq + q]);
@@ -827,9 +1055,8 @@ __device__ __forceinline__ void neighbor_point(const Dev<FaceT>& m, int slot0, i
   R u0[nv], u1[nv];
   #pragma unroll
   for (int v = 0; v < nv; ++v) {
-    const R ref = !split ? R(0) : v == ND ? R(m.rho0) : v == ND + 1 ? R(m.ener0) : R(0);
-    u0[v] = split ? o0[v] + ref : o0[v];
-    u1[v] = split ? o1[v] + ref : o1[v];
+    u0[v] = split ? rs.s[v] + o0[v] : o0[v];
+    u1[v] = split ? rs.s[v] + o1[v] : o1[v];
   }
   R n[ND];
   const int i_dim0 = dir & 3;
@@ -837,10 +1064,13 @@ __device__ __forceinline__ void neighbor_point(const Dev<FaceT>& m, int slot0, i
   for (int d = 0; d < ND; ++d) n[d] = deformed ? R(sign0)*R(nrml[d*nfq + q]) : (d == i_dim0 ? R(1) : R(0));
   R fl0[nv], fl1[nv];
   Conv<ND, R> c0(u0), c1(u1);
-  const R pm0 = split ? R(heat_rat - 1.)*(o0[ND + 1] - c0.kin_ener) : c0.pressure;
-  const R pm1 = split ? R(heat_rat - 1.)*(o1[ND + 1] - c1.kin_ener) : c1.pressure;
-  c0.flux(u0, n, fl0, pm0);
-  c1.flux(u1, n, fl1, pm1);
+  if constexpr (split) {
+    flux_delta<ND, R>(u0, o0, rs, c0, n, fl0);
+    flux_delta<ND, R>(u1, o1, rs, c1, n, fl1);
+  } else {
+    c0.flux(u0, n, fl0);
+    c1.flux(u1, n, fl1);
+  }
   const R cs0 = char_speed<ND, R>(u0, c0.inv_mass), cs1 = char_speed<ND, R>(u1, c1.inv_mass);
   R nn = 0;
   #pragma unroll
@@ -1003,7 +1233,7 @@ __device__ void bc_state_point(const Dev<FaceT>& m, int i_bc, int q, double* gh)
   double* sc = m.bc_cache + (size_t)i_bc*2*nv*nfq;
   constexpr bool split = !std::is_same<FaceT, double>::value;
   double ref[nv];   // offset of the stored traces (mixed form), see offset_var
-  for (int v = 0; v < nv; ++v) ref[v] = !split ? 0. : v == ND ? m.rho0 : v == ND + 1 ? m.ener0 : 0.;
+  for (int v = 0; v < nv; ++v) ref[v] = !split ? 0. : m.ref[(size_t)(c[0]/(2*ND))*nv + v];
   double inside[nv], n[ND];
   for (int v = 0; v < nv; ++v) inside[v] = split ? double(in[v*nfq + q]) + ref[v] : double(in[v*nfq + q]);
   for (int d = 0; d < ND; ++d) n[d] = nrml[d*nfq + q];
@@ -1089,6 +1319,37 @@ __global__ void k_bc_neighbor(Dev<FaceT> m)
       ov = gh;
     }
     neighbor_point<ND, RS, R, FaceT>(m, c[0], c[1], bc_dir(c[2]), q, m.bc_nrml_t + (size_t)i*ND*nfq, VISC, ov);
+  }
+}
+
+// Neighbor of a Cartesian-only mesh in one launch: blocks [0, car_blocks) take the Cartesian
+// connections (as k_neighbor), the remaining blocks the boundary connections (as
+// k_bc_neighbor). Same per-point arithmetic, one launch fewer per stage.
+template <int ND, int RS, typename R, bool VISC, bool FUSE, typename FaceT>
+__global__ void k_neighbor_car_bc(Dev<FaceT> m, int car_blocks)
+{
+  constexpr int nfq = Shape<ND, RS>::nfq;
+  if ((int)blockIdx.x < car_blocks) {
+    const long total = (long)m.n_car_con*nfq;
+    for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)car_blocks*blockDim.x) {
+      const int i = int(t/nfq), q = int(t%nfq);
+      const int* c = m.car_con + 3*i;
+      neighbor_point<ND, RS, R, FaceT>(m, c[0], c[1], c[2] | (c[2] << 2) | (1 << 4), q, nullptr, VISC, nullptr);
+    }
+  } else {
+    const long total = (long)m.n_bc_con*nfq;
+    const long stride = (long)(gridDim.x - car_blocks)*blockDim.x;
+    for (long t = (blockIdx.x - car_blocks)*(long)blockDim.x + threadIdx.x; t < total; t += stride) {
+      const int i = int(t/nfq), q = int(t%nfq);
+      const int* c = m.bc_con + 4*i;
+      double gh[ND + 2];
+      const double* ov = nullptr;
+      if (FUSE) {
+        bc_state_point<ND, RS, FaceT>(m, i, q, gh);
+        ov = gh;
+      }
+      neighbor_point<ND, RS, R, FaceT>(m, c[0], c[1], bc_dir(c[2]), q, m.bc_nrml_t + (size_t)i*ND*nfq, VISC, ov);
+    }
   }
 }
 
@@ -1301,7 +1562,7 @@ __global__ void k_write_face(Dev<FaceT> m, Tab<RS> tab, int e_begin, int n_elem)
     const int stride = S::stride(d);
     const double* row = m.elem + (size_t)e*(nv + 3)*nq + v*nq + (r/stride)*stride*RS + r%stride;
     // traces in the offset form of the storage (see offset_var)
-    const double ref = std::is_same<FaceT, double>::value ? 0. : v == ND ? m.rho0 : v == ND + 1 ? m.ener0 : 0.;
+    const double ref = std::is_same<FaceT, double>::value ? 0. : m.ref[(size_t)e*nv + v];
     double a0 = 0., a1 = 0.;
     for (int i = 0; i < RS; ++i) { double x = row[i*stride] - ref; a0 += tab.bound[i]*x; a1 += tab.bound[RS + i]*x; }
     FaceT* f0 = m.face + (size_t)(e*2*ND + 2*d)*S::slot_dof + v*nfq + r;
@@ -1316,49 +1577,36 @@ __global__ void k_write_face(Dev<FaceT> m, Tab<RS> tab, int e_begin, int n_elem)
 // step is a CFL limit with a safety factor and needs no more than float accuracy.
 template <int ND, int RS, typename R, bool VISC, typename FaceT>
 __global__ void __launch_bounds__(256)
-k_max_dt(Dev<FaceT> m, Tab<RS> tab, double msc, double msd, int local_time, Tm visc,
-         Tm cond, double* partials)
+k_max_dt(Dev<FaceT> m, Tab<RS> tab, double msc, double msd, int local_time, TmT<R> visc,
+         TmT<R> cond, double* partials)
 {
   using S = Shape<ND, RS>;
   constexpr int nq = S::nq, nv = S::nv, nvert = S::nvert;
   const R inv_cfl_c = R(1./(tab.max_cfl*msc));
   const R inv_cfl_d = R(1./(-2/tab.min_eig_diffusion*msd));
   double dt = 1.7976931348623157e308;
+  R dt_r = R(3.4e38);   // running minimum in the compute type (float form)
   const long total = (long)m.n_elem*nq;
   for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
     const int e = int(t/nq), q = int(t%nq);
     double* state = m.elem + (size_t)e*(nv + 3)*nq;
-    R vals[nvert];
-    #pragma unroll
-    for (int i = 0; i < nvert; ++i) vals[i] = R(m.vert_tss[(size_t)e*nvert + i]);
-    int stride = nvert;
-    #pragma unroll
-    for (int d = 0; d < ND; ++d) {
-      const R coord = R(tab.node[(q/ipow(RS, ND - 1 - d))%RS]);
-      stride /= 2;
-      #pragma unroll
-      for (int i = 0; i < (nvert >> (d + 1)); ++i) vals[i] += coord*(vals[i + stride] - vals[i]);
-    }
-    const R spacing = vals[0];
-    R s[nv];
-    #pragma unroll
-    for (int v = 0; v < nv; ++v) s[v] = R(state[v*nq + q]);
-    const R inv_spacing = R(1)/spacing;
-    Conv<ND, R> c(s);
-    R scale = 0;
-    scale += char_speed<ND, R>(s, c.inv_mass)*inv_cfl_c*inv_spacing;
-    if constexpr (VISC) {
-      DiffScalars<ND, R> df(s, c, R(state[(nv + 1)*nq + q]), R(state[(nv + 2)*nq + q]), visc, cond);
-      R diffusivity = fabs(df.laplacian_av) + fmax(fabs(df.bulk_av) + df.mu*c.inv_mass, df.energy_cond*c.inv_mass);
-      scale += diffusivity*inv_cfl_d*inv_spacing*inv_spacing;
-    }
-    const double step = double(R(1)/scale);
-    if (local_time) state[nv*nq + q] = step;
-    else {
-      state[nv*nq + q] = 1.;
-      dt = fmin(dt, step);
+    if constexpr (std::is_same<R, double>::value) {
+      const double step = point_step<ND, RS, R, VISC>(m, tab, e, q, inv_cfl_c, inv_cfl_d, visc, cond);
+      if (local_time) state[nv*nq + q] = step;
+      else {
+        state[nv*nq + q] = 1.;
+        dt = fmin(dt, step);
+      }
+    } else {
+      const R step = point_step<ND, RS, R, VISC>(m, tab, e, q, inv_cfl_c, inv_cfl_d, visc, cond);
+      if (local_time) state[nv*nq + q] = f64_of(step);
+      else {
+        state[nv*nq + q] = 1.;
+        dt_r = fmin(dt_r, step);
+      }
     }
   }
+  if constexpr (!std::is_same<R, double>::value) dt = dt_r < R(3.4e38) ? f64_of(dt_r) : dt;
   // CTA minimum
   __shared__ double s_min[32];
   for (int o = 16; o > 0; o >>= 1) dt = fmin(dt, __shfl_xor_sync(0xffffffffu, dt, o));
@@ -1392,6 +1640,67 @@ static __global__ void k_finalize_dt(double* scalars, const double* partials, in
 }
 
 static __global__ void k_set_scalar(double* scalars, int which, double value) { scalars[which] = value; }
+
+// thermo::admissible (src/thermo.cpp:6-18) over every element state, every element face trace
+// and every fine mortar face, as Solver::is_admissible does (src/Solver.cpp:921-959): density
+// and total energy positive at every point. record[e] = 1 marks an inadmissible element (its
+// state or one of its faces); status bit 0 is set if any point is inadmissible, bit 1 if any
+// value is not finite (the reference asserts there). Traces of the mixed form are offsets:
+// the element's reference state is added back.
+template <int ND, int RS, typename FaceT>
+__global__ void k_admissible(Dev<FaceT> m, int* record, int* status)
+{
+  using S = Shape<ND, RS>;
+  constexpr int nq = S::nq, nfq = S::nfq, nv = S::nv;
+  constexpr bool split = !std::is_same<FaceT, double>::value;
+  const long n_state = (long)m.n_elem*nq;
+  const long n_face = (long)m.n_elem*2*ND*nfq;
+  const long n_mortar = (long)m.n_ref*4*nfq;
+  const long total = n_state + n_face + n_mortar;
+  for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
+    double val[nv];
+    int e;
+    if (t < n_state) {
+      e = int(t/nq);
+      const int q = int(t%nq);
+      const double* st = m.elem + (size_t)e*(nv + 3)*nq;
+      for (int v = 0; v < nv; ++v) val[v] = st[v*nq + q];
+    } else {
+      int slot, r;
+      if (t < n_state + n_face) {
+        const long u = t - n_state;
+        slot = int(u/nfq);
+        r = int(u%nfq);
+        e = slot/(2*ND);
+      } else {
+        const long u = t - n_state - n_face;
+        const int i = int(u/(4*nfq)), k = int((u/nfq)%4);
+        r = int(u%nfq);
+        const int* rf = m.ref_face + 7*i;
+        int n_fine = 1 << (ND - 1);
+        for (int d = 0; d < ND - 1; ++d) n_fine /= 1 + (rf[5 + d] != 0);
+        if (k >= n_fine || rf[1 + k] < 0) continue;
+        slot = rf[1 + k];
+        e = -1;   // a mortar belongs to no element; its reference is the coarse element's
+        if constexpr (split) e = rf[0]/(2*ND);
+      }
+      const FaceT* f = m.face + (size_t)slot*S::slot_dof;
+      for (int v = 0; v < nv; ++v) {
+        val[v] = double(f[v*nfq + r]);
+        if constexpr (split) val[v] += m.ref[(size_t)e*nv + v];
+      }
+      if (t >= n_state + n_face) e = -1;
+    }
+    bool finite = true;
+    for (int v = 0; v < nv; ++v) finite = finite && isfinite(val[v]);
+    const bool admissible = val[ND] > 0. && val[ND + 1] > 0.;
+    if (!finite) atomicOr(status, 2);
+    if (!admissible) {
+      atomicOr(status, 1);
+      if (e >= 0) record[e] = 1;
+    }
+  }
+}
 
 // Storage conversions of the mixed form and the determinant reciprocal.
 static __global__ void k_narrow(const double* src, float* dst, long n)

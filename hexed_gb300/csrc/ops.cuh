@@ -37,11 +37,11 @@ struct Runner
     if constexpr (std::is_same<R, double>::value) {
       m.rcache = c.rcache; m.face = c.face; m.nrm = c.jac; m.face_nrml = c.face_nrml;
       m.def_con_nrml = c.def_con_nrml; m.bc_nrml_t = c.bc_nrml;
-      m.rho0 = 0.; m.ener0 = 0.;
+      m.ref = nullptr;
     } else {
       m.rcache = c.rcache_f; m.face = c.face_f; m.nrm = c.nrm_f; m.face_nrml = c.face_nrml_f;
       m.def_con_nrml = c.def_con_nrml_f; m.bc_nrml_t = c.bc_nrml_f;
-      m.rho0 = c.rho0; m.ener0 = c.ener0;
+      m.ref = c.ref_state;
     }
     return m;
   }
@@ -65,22 +65,65 @@ struct Runner
     return t;
   }
 
-  template <bool DEF, bool VISC>
-  static void local(Ctx& c, int stage, int cr, int uf, const hexed_transport& visc, const hexed_transport& cond)
+  // Elements per CTA of the volume kernel for launch-shape variant v: 0 the default
+  // (256/nq), 1 half of it, 2 twice it. The 2D Cartesian kernels (the serving path) are
+  // compiled in all three shapes; other kernels only in the default.
+  static constexpr int epb_of(int v) { return v == 1 ? (S::epb > 1 ? S::epb/2 : 1) : v == 2 ? 2*S::epb : S::epb; }
+  static constexpr bool has_variants(bool def) { return ND == 2 && !def; }
+
+  template <bool DEF, bool VISC, int EPB, bool CAPPED>
+  static auto pick_local()
   {
-    const int e_begin = DEF ? c.n_car : 0;
-    const int e_end = DEF ? c.n_car + c.n_def : c.n_car;
-    if (e_end <= e_begin) return;
-    const int blocks = (e_end - e_begin + S::epb - 1)/S::epb;
-    constexpr size_t smem = LocalSmem<ND, RS, R, DEF, VISC>::bytes;
-    auto kern = k_local<ND, RS, R, DEF, VISC, FaceT>;
+    if constexpr (CAPPED) return k_local_3cta<ND, RS, R, DEF, VISC, FaceT, EPB>;
+    else return k_local<ND, RS, R, DEF, VISC, FaceT, EPB>;
+  }
+
+  template <bool DEF, bool VISC, int EPB>
+  static void local_shape(Ctx& c, int stage, int cr, int uf, const hexed_transport& visc, const hexed_transport& cond,
+                          int e_begin, int e_end, const LocalDt& ldt)
+  {
+    const int blocks = (e_end - e_begin + EPB - 1)/EPB;
+    constexpr size_t smem = LocalSmem<ND, RS, R, DEF, VISC, EPB>::bytes;
+    // the float viscous 3D kernel is the register-capped variant (k_local_3cta)
+    constexpr bool capped = std::is_same<R, float>::value && VISC && ND == 3;
+    auto kern = pick_local<DEF, VISC, EPB, capped>();
     static bool configured = false;
     if (!configured) {
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       configured = true;
     }
     ProfScope ps(c, DEF ? (VISC ? "local_def_ns" : "local_def_euler") : (VISC ? "local_car_ns" : "local_car_euler"));
-    kern<<<blocks, S::threads, smem, c.stream>>>(dev(c), tab(c), e_begin, e_end, stage, cr, uf, make_tm(visc), make_tm(cond));
+    kern<<<blocks, Tile<ND, RS, EPB>::threads, smem, c.stream>>>(dev(c), tab(c), e_begin, e_end, stage, cr, uf,
+                                                                 make_tm<R>(visc), make_tm<R>(cond), ldt);
+  }
+
+  template <bool DEF, bool VISC>
+  static void local(Ctx& c, int stage, int cr, int uf, const hexed_transport& visc, const hexed_transport& cond,
+                    const LocalDt& ldt = LocalDt{0, 0., 0., 0.})
+  {
+    const int e_begin = DEF ? c.n_car : 0;
+    const int e_end = DEF ? c.n_car + c.n_def : c.n_car;
+    if (e_end <= e_begin) return;
+    if constexpr (has_variants(DEF)) {
+      if (c.local_variant == 1)
+        return local_shape<DEF, VISC, epb_of(1)>(c, stage, cr, uf, visc, cond, e_begin, e_end, ldt);
+      if (c.local_variant == 2)
+        return local_shape<DEF, VISC, epb_of(2)>(c, stage, cr, uf, visc, cond, e_begin, e_end, ldt);
+    }
+    local_shape<DEF, VISC, S::epb>(c, stage, cr, uf, visc, cond, e_begin, e_end, ldt);
+  }
+
+  static int local_elems_per_cta(int v) { return has_variants(false) ? epb_of(v) : S::epb; }
+
+  // Solver::is_admissible (src/Solver.cpp:921-959); record [n_elem] and status[0] cleared first
+  static void admissible(Ctx& c, int* record)
+  {
+    const int n_elem = c.n_car + c.n_def;
+    cudaMemsetAsync(record, 0, (size_t)n_elem*sizeof(int), c.stream);
+    cudaMemsetAsync(c.status, 0, sizeof(int), c.stream);
+    const long total = (long)n_elem*(S::nq + 2*ND*S::nfq) + (long)c.n_ref*4*S::nfq;
+    ProfScope ps(c, "admissible");
+    k_admissible<ND, RS, FaceT><<<grid_for(total, 256), 256, 0, c.stream>>>(dev(c), record, c.status);
   }
 
   template <bool DEF>
@@ -104,7 +147,17 @@ struct Runner
   template <bool VISC>
   static void neighbor(Ctx& c, bool fuse_bc)
   {
-    const int block = 256;
+    const int block = c.face_threads;
+    // one launch for small Cartesian meshes, where launch latency dominates; large ones keep
+    // the leaner Cartesian kernel (the fused one carries the boundary code's registers)
+    if (c.n_car_con && c.n_bc_con && !c.n_def_con && (long)c.n_car_con*S::nfq <= 2L*152*block) {
+      const int car_blocks = grid_for((long)c.n_car_con*S::nfq, block);
+      const int blocks = car_blocks + grid_for((long)c.n_bc_con*S::nfq, block);
+      ProfScope ps(c, "neighbor_car_bc");
+      if (fuse_bc) k_neighbor_car_bc<ND, RS, R, VISC, true, FaceT><<<blocks, block, 0, c.stream>>>(dev(c), car_blocks);
+      else k_neighbor_car_bc<ND, RS, R, VISC, false, FaceT><<<blocks, block, 0, c.stream>>>(dev(c), car_blocks);
+      return;
+    }
     if (c.n_car_con) {
       ProfScope ps(c, "neighbor_car");
       k_neighbor<ND, RS, R, false, VISC, FaceT><<<grid_for((long)c.n_car_con*S::nfq, block), block, 0, c.stream>>>(dev(c));
@@ -142,7 +195,7 @@ struct Runner
 
   static void neighbor_reconcile(Ctx& c, bool fuse_bc)
   {
-    const int block = 256;
+    const int block = c.face_threads;
     if (c.n_car_con) {
       ProfScope ps(c, "neighbor_reconcile_car");
       k_neighbor_reconcile<ND, RS, R, 0, false, FaceT><<<grid_for((long)c.n_car_con*S::nfq, block), block, 0, c.stream>>>(dev(c));
@@ -161,13 +214,13 @@ struct Runner
   // compute_euler (src/kernels_convective.cpp:8-19). fuse_bc: apply the state BCs inside
   // the boundary part of Neighbor (used by the solver layer, which would otherwise run
   // Solver::apply_state_bcs immediately before).
-  static void compute_euler(Ctx& c, int stage, int cr, int uf, bool fuse_bc)
+  static void compute_euler(Ctx& c, int stage, int cr, int uf, bool fuse_bc, const LocalDt& ldt)
   {
     hexed_transport inv{0., 0., 1., 1., 0};
     neighbor<false>(c, fuse_bc);
     refine(c, false, true, false);
-    local<false, false>(c, stage, cr, uf, inv, inv);
-    local<true, false>(c, stage, cr, uf, inv, inv);
+    local<false, false>(c, stage, cr, uf, inv, inv, ldt);
+    local<true, false>(c, stage, cr, uf, inv, inv, ldt);
     refine(c, true, false, false);
   }
 
@@ -197,8 +250,8 @@ struct Runner
     const int grid = grid_for(total, 256, c.max_partials);
     {
       ProfScope ps(c, "max_dt");
-      if (viscous) k_max_dt<ND, RS, R, true, FaceT><<<grid, 256, 0, c.stream>>>(dev(c), tab(c), msc, msd, local_time, make_tm(visc), make_tm(cond), c.partials);
-      else k_max_dt<ND, RS, R, false, FaceT><<<grid, 256, 0, c.stream>>>(dev(c), tab(c), msc, msd, local_time, make_tm(visc), make_tm(cond), c.partials);
+      if (viscous) k_max_dt<ND, RS, R, true, FaceT><<<grid, 256, 0, c.stream>>>(dev(c), tab(c), msc, msd, local_time, make_tm<R>(visc), make_tm<R>(cond), c.partials);
+      else k_max_dt<ND, RS, R, false, FaceT><<<grid, 256, 0, c.stream>>>(dev(c), tab(c), msc, msd, local_time, make_tm<R>(visc), make_tm<R>(cond), c.partials);
     }
     ProfScope ps(c, "finalize_dt");
     k_finalize_dt<<<1, 256, 0, c.stream>>>(c.scalars, c.partials, grid, local_time, max_time_step, cheby);
@@ -252,7 +305,7 @@ struct Runner
   {
     static const OpsTable t = {
       compute_euler, compute_navier_stokes, max_dt, refine, write_face, bc_state, bc_flux, residual_norm,
-      set_art_visc_admis, segment_residual_norms,
+      set_art_visc_admis, segment_residual_norms, local_elems_per_cta, admissible,
     };
     return &t;
   }

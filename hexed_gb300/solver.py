@@ -106,6 +106,16 @@ class Context:
     def apply_flux_bcs(self):
         abi.check(self.lib.hexed_gpu_apply_flux_bcs(self.handle))
 
+    def is_admissible(self, records=False):
+        """Solver::is_admissible: True if density and energy are positive everywhere
+        (raises HexedError HEXED_ERR_NUMERICAL for a non-finite state); with records=True
+        also the per-element flags."""
+        ok = ctypes.c_int()
+        rec = np.zeros(self.arena.n_elem, dtype=np.int32) if records else None
+        abi.check(self.lib.hexed_gpu_is_admissible(self.handle, ctypes.byref(ok),
+                                                   rec.ctypes.data_as(abi.P_int) if records else None))
+        return (bool(ok.value), rec) if records else bool(ok.value)
+
     # -------------------------------------------------------------- solver layer
     def update(self, params, read_dt=True):
         out = ctypes.c_double()
@@ -122,6 +132,20 @@ class Context:
         return list(out)
 
     # -------------------------------------------------------------- pool (continuous batching)
+    def set_launch_shape(self, local_variant=0, face_threads=256):
+        abi.check(self.lib.hexed_gpu_set_launch_shape(self.handle, local_variant, face_threads))
+
+    def launch_shape(self):
+        """(elements per volume-kernel CTA, face-kernel threads per CTA)."""
+        e, f = ctypes.c_int(), ctypes.c_int()
+        abi.check(self.lib.hexed_gpu_launch_shape(self.handle, ctypes.byref(e), ctypes.byref(f)))
+        return e.value, f.value
+
+    def set_reference_state(self, state):
+        """Reference state of every element (mixed form; ignored by the FP64 form)."""
+        st = np.ascontiguousarray(state, dtype=np.float64)
+        abi.check(self.lib.hexed_gpu_set_reference_state(self.handle, st.ctypes.data_as(abi.P_double)))
+
     def write_face_range(self, elem_begin, elem_count):
         abi.check(self.lib.hexed_gpu_write_face_range(self.handle, elem_begin, elem_count))
 

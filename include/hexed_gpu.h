@@ -135,7 +135,9 @@ enum hexed_array {
   HEXED_ARRAY_BC_CACHE = 3,
   HEXED_ARRAY_NOM_SIZE = 4,
   HEXED_ARRAY_VERT_TSS = 5,
-  HEXED_ARRAY_BC_NRML = 6
+  HEXED_ARRAY_BC_NRML = 6,
+  HEXED_ARRAY_REF_STATE = 7   /* mixed form only: [n_elem][nv] reference state of each element
+                                 (write it before the element's state and traces) */
 };
 
 /* Arithmetic of the volume and face kernels. */
@@ -170,7 +172,9 @@ const char* hexed_gpu_version(void);
 
 /* Creates a context on the current CUDA device and uploads the whole arena.
  * Replaces the setup the reference performs once per mesh (Solver::calc_jacobian +
- * initialize, src/Solver.cpp:273-408) as far as the kernels see it. */
+ * initialize, src/Solver.cpp:273-408) as far as the kernels see it. `elem`, `rcache`,
+ * `face` and `bc_cache` may be null: their device copies then start at zero (an arena whose
+ * states are written later with hexed_gpu_write_range). */
 int hexed_gpu_create(const hexed_mesh_desc* desc, int precision, hexed_gpu_ctx** out);
 int hexed_gpu_destroy(hexed_gpu_ctx* ctx);
 
@@ -203,6 +207,37 @@ int hexed_gpu_max_dt(hexed_gpu_ctx* ctx, double convective_safety, double diffus
 int hexed_gpu_compute_prolong(hexed_gpu_ctx* ctx, int scale, int offset);
 int hexed_gpu_compute_restrict(hexed_gpu_ctx* ctx, int scale, int offset);
 int hexed_gpu_compute_write_face(hexed_gpu_ctx* ctx);
+
+/* Solver::is_admissible (src/Solver.cpp:921-959, thermo::admissible src/thermo.cpp:6-18):
+ * *admissible = 1 if density and total energy are positive at every point of every element
+ * state, element face trace and fine mortar face, else 0. record (optional, [n_elem] of the
+ * active elements) receives 1 for each inadmissible element. Returns HEXED_ERR_NUMERICAL
+ * ("state is not finite") if any of these values is not finite, where the reference asserts. */
+int hexed_gpu_is_admissible(hexed_gpu_ctx* ctx, int* admissible, int* record);
+
+/* Checks the double <-> float conversions the mixed form does with integer operations against
+ * the hardware conversions on n host values; *mismatches = values whose results differ in
+ * any bit (values whose float result is subnormal are skipped: the mixed form flushes them
+ * to zero). A diagnostic; no counterpart in the reference. */
+int hexed_gpu_check_conversions(const double* values, long n, long* mismatches);
+
+/* Launch shape of the volume and face kernels. local_variant selects the elements per CTA of
+ * the 2D Cartesian volume kernels: 0 = 256/nq (the default), 1 = half, 2 = twice that (3D
+ * kernels have only 0). face_threads (64, 128 or 256 = default) is the CTA size of the
+ * face kernels. Chosen per row size by the autotuner of the serving loop; results do not
+ * depend on it. No counterpart in the reference. */
+int hexed_gpu_set_launch_shape(hexed_gpu_ctx* ctx, int local_variant, int face_threads);
+/* The launch shape in use: elements per volume-kernel CTA and face-kernel threads per CTA. */
+int hexed_gpu_launch_shape(hexed_gpu_ctx* ctx, int* local_elems_per_cta, int* face_threads);
+
+/* Reference state (nv conserved values) of every element in the mixed form. The mixed form
+ * stores face traces, and forms convective fluxes, as differences from the element's
+ * reference state, so that float arithmetic resolves small variations of a nearly uniform
+ * flow. By default this is the mean conserved state of the state given to hexed_gpu_create.
+ * HEXED_ARRAY_REF_STATE sets it per element: one solve's elements share one reference state.
+ * Call this before the states and traces it applies to are written. No effect in the FP64
+ * form. No counterpart in the reference. */
+int hexed_gpu_set_reference_state(hexed_gpu_ctx* ctx, const double* state);
 
 /* Write_face for elements [elem_begin, elem_begin + elem_count) only: initialises the face
  * traces of one newly admitted solve without touching the traces of solves already running.

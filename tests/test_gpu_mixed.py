@@ -71,3 +71,23 @@ def test_mixed_hanging_faces():
 def test_mixed_artificial_viscosity():
     ar = problems.mach2_jump_3d(n_per_side=3, row_size=4)
     check(ar, abi.update_params(max_safety=0.5, av_admis_char_speed=ar.av_char_speed), 10, 1e-5)
+
+
+def test_integer_conversions_match_hardware():
+    """The mixed form converts between double and float with integer operations; they must
+    give the bits of the hardware conversions."""
+    import ctypes
+    rng = np.random.default_rng(3)
+    vals = [rng.standard_normal(200_000) * 10.0 ** rng.integers(-30, 30, 200_000),
+            rng.uniform(-3, 3, 200_000),
+            np.array([0., -0., 1., -1., 1.5, 3.4028234663852886e38, 3.4028235677973366e38, 1e39, -1e39,
+                      np.inf, -np.inf, np.nan, 1.1754943508222875e-38, 1e-45, 5e-324, 2.0 ** -149,
+                      1 + 2.0 ** -24, 1 + 3 * 2.0 ** -24, 1 + 2.0 ** -24 + 2.0 ** -40, 0.1, 1 / 3])]
+    # values exactly half-way between two floats (ties to even)
+    f = rng.standard_normal(10_000).astype(np.float32).astype(np.float64)
+    vals.append(f + np.spacing(f.astype(np.float32)).astype(np.float64) / 2)
+    x = np.ascontiguousarray(np.concatenate(vals))
+    lib = abi.load_library()
+    bad = ctypes.c_long()
+    abi.check(lib.hexed_gpu_check_conversions(x.ctypes.data_as(abi.P_double), x.size, ctypes.byref(bad)))
+    assert bad.value == 0

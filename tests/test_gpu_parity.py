@@ -192,6 +192,28 @@ def test_local_time_stepping_update():
     assert_close(a, b)
 
 
+@pytest.mark.parametrize("precision", [abi.FP64, abi.MIXED])
+@pytest.mark.parametrize("deformed", [False, True])
+def test_fused_local_time_step_matches_separate_max_dt(precision, deformed):
+    """With local time stepping the update computes each point's time-step scale inside the
+    first stage's volume kernel; the kernel-layer sequence Max_dt -> state BCs -> Euler stage
+    0 -> state BCs -> stage 1 must give the same state."""
+    from helpers import deformed_case
+    ar = deformed_case(3, 3, 3, abi.BC_RIEMANN) if deformed else cartesian_case(2, 4, 4)
+    p = abi.update_params(max_safety=0.5, local_time=True)
+    with Context(ar.copy(), precision) as a, Context(ar.copy(), precision) as b:
+        a.write_face()
+        b.write_face()
+        for _ in range(3):
+            assert a.update(p) == pytest.approx(1., rel=1e-15)   # chebyshev_step(1, 0) = 1 + 2e-16
+            dt = b.max_dt(0.5, 0.5, local_time=True)
+            for stage in (0, 1):
+                b.apply_state_bcs()
+                b.compute_euler(dt, stage)
+        sa, sb = a.download(abi.ARRAY_ELEM), b.download(abi.ARRAY_ELEM)
+    assert np.abs(sa - sb).max() <= 1e-13 * np.abs(sb).max()
+
+
 @pytest.mark.parametrize("nd", [2, 3])
 def test_rotated_connections(nd):
     """Neighbor / Neighbor_reconcile across every connection orientation (Face_permutation)."""
