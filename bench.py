@@ -325,6 +325,44 @@ def run_serving(args):
     return 0
 
 
+def run_serving_probe(args):
+    """Per-batch time, residual-check time and per-kernel launch time of serving pools
+    (FP64 and mixed; one 10x10 solve at row sizes 4 and 6, and 24 solves of 16x16 at row
+    size 6): 3 warm-up batches, 30 timed batches of 20 updates, 30 timed residual checks,
+    then one eager batch under the library's CUDA-event profiler."""
+    from hexed_gb300 import serving
+    params = abi.update_params(max_safety=0.5, local_time=True)
+    out = {}
+    for prec, pname in ((abi.FP64, "fp64"), (abi.MIXED, "mixed")):
+        for rs, side, n_cases in ((4, 10, 1), (6, 10, 1), (6, 16, 24)):
+            pool = serving.Pool(rs, prec, capacity=8192, params=params, updates_per_batch=20)
+            for i in range(n_cases):
+                pool.admit(serving.Request(i, side, rs, 0.5, 0., seed=1 + i))
+            for _ in range(3):
+                pool.enqueue_batch()
+                pool.residuals()
+            pool.ctx.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(30):
+                pool.enqueue_batch()
+            pool.ctx.synchronize()
+            t_batch = (time.perf_counter() - t0) / 30
+            t0 = time.perf_counter()
+            for _ in range(30):
+                pool.residuals()
+            t_res = (time.perf_counter() - t0) / 30
+            pool.ctx.profile_enable(True)
+            pool.ctx.update_n(params, 20, False)
+            prof = pool.ctx.profile_read()
+            out[f"{pname}_rs{rs}_side{side}_x{n_cases}"] = {
+                "elements": side * side * n_cases, "batch_of_20_ms": round(t_batch * 1e3, 3),
+                "residual_check_ms": round(t_res * 1e3, 3),
+                "kernel_us_per_launch": {k: round(v[1] / v[0] * 1e3, 2) for k, v in prof.items()}}
+            pool.close()
+    print(json.dumps(out))
+    return 0
+
+
 # ------------------------------------------------------------------ GPU arm
 def main():
     ap = argparse.ArgumentParser()
@@ -341,6 +379,7 @@ def main():
     ap.add_argument("--err-steps", type=int, default=200, help="updates for the mixed-vs-FP64 error report")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-form measurement beside FP64")
     ap.add_argument("--serving", action="store_true", help="serve a stream of steady 2D solves instead")
+    ap.add_argument("--serving-probe", action="store_true", help="time batches and kernels of serving pools")
     ap.add_argument("--solves", type=int, default=64)
     ap.add_argument("--rate", type=float, default=200.)
     ap.add_argument("--max-side", type=int, default=16)
@@ -354,6 +393,8 @@ def main():
         return run_reference(args)
     if args.serving:
         return run_serving(args)
+    if args.serving_probe:
+        return run_serving_probe(args)
 
     import torch
     rank, world, local_rank = dist_env()

@@ -137,6 +137,7 @@ def load_library(path=LIB_PATH):
         "hexed_gpu_set_launch_shape": ([vp, c_int, c_int], c_int),
         "hexed_gpu_check_conversions": ([P_double, ctypes.c_long, ctypes.POINTER(ctypes.c_long)], c_int),
         "hexed_gpu_is_admissible": ([vp, P_int, P_int], c_int),
+        "hexed_gpu_device_flags": ([vp, P_int], c_int),
         "hexed_gpu_launch_shape": ([vp, P_int, P_int], c_int),
         "hexed_gpu_write_range": ([vp, c_int, ctypes.c_long, ctypes.c_long, P_double], c_int),
         "hexed_gpu_read_range": ([vp, c_int, ctypes.c_long, ctypes.c_long, P_double], c_int),

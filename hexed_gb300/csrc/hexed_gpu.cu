@@ -548,6 +548,16 @@ int hexed_gpu_is_admissible(hexed_gpu_ctx* c, int* admissible, int* record)
   return HEXED_OK;
 }
 
+int hexed_gpu_device_flags(hexed_gpu_ctx* c, int* flags)
+{
+  if (int st = check_ctx(c)) return st;
+  if (!flags) return fail(HEXED_ERR_INVALID, "null output");
+  HX_CUDA(cudaMemcpyAsync(c->h_pinned, c->status + 1, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  HX_CUDA(cudaStreamSynchronize(c->stream));
+  std::memcpy(flags, c->h_pinned, sizeof(int));
+  return HEXED_OK;
+}
+
 int hexed_gpu_check_conversions(const double* host, long n, long* mismatches)
 {
   if (!mismatches || n < 0 || (n && !host)) return fail(HEXED_ERR_INVALID, "bad arguments");

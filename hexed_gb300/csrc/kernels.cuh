@@ -420,6 +420,44 @@ __device__ __forceinline__ void write_faces_from_smem(const Dev<FaceT>& m, const
 
 // ------------------------------------------------------------------- Local
 // Spatial::Local (include/Spatial.hpp:326-509) fused with the stage update and Write_face.
+// ------------------------------------------------------------------- bulk async copies
+// One-dimensional bulk copy (TMA) of `bytes` contiguous bytes from global to shared memory,
+// completing on an mbarrier, and the bounded wait for it. Both addresses and `bytes` must be
+// multiples of 16 (the caller checks and otherwise reads global memory directly).
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count)
+{
+  const unsigned mb = (unsigned)__cvta_generic_to_shared(bar);
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(mb), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void bulk_load(void* smem_dst, const void* gmem_src, unsigned bytes,
+                                          unsigned long long* bar)
+{
+  const unsigned dst = (unsigned)__cvta_generic_to_shared(smem_dst);
+  const unsigned mb = (unsigned)__cvta_generic_to_shared(bar);
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(mb), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               :: "r"(dst), "l"(gmem_src), "r"(bytes), "r"(mb) : "memory");
+}
+
+// Waits for phase `phase` of the mbarrier, giving up after `max_polls` polls (false).
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned phase, unsigned max_polls)
+{
+  const unsigned mb = (unsigned)__cvta_generic_to_shared(bar);
+  for (unsigned i = 0; i < max_polls; ++i) {
+    unsigned done;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                 " selp.u32 %0, 1, 0, p;\n}" : "=r"(done) : "r"(mb), "r"(phase) : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+constexpr unsigned bulk_wait_polls = 1u << 20;
+// status[1] bits (read by hexed_gpu_device_flags): a bulk-copy wait gave up and the kernel
+// read global memory instead
+constexpr int flag_bulk_wait = 1;
+
 template <int ND, int RS, typename R, bool DEF, bool VISC, int EPB = Shape<ND, RS>::epb>
 struct LocalSmem {
   using S = Shape<ND, RS>;
@@ -427,7 +465,11 @@ struct LocalSmem {
                                 + ND*S::nv*S::nq         // s_f
                                 + (VISC ? ND*S::nv*S::nq : 0)   // s_g
                                 + ND*2*S::nv*S::nfq;     // s_bf
-  static constexpr size_t bytes = sizeof(STab<RS, R>) + sizeof(R)*(size_t)per_elem*EPB + 16;
+  // [tables][mbarrier, 16 B][element states, EPB x (nv + 3) x nq doubles][s_u s_f s_g s_bf]
+  static constexpr size_t tab_bytes = (sizeof(STab<RS, R>) + 15)/16*16;
+  static constexpr size_t state_bytes = sizeof(double)*(size_t)EPB*(S::nv + 3)*S::nq;
+  static constexpr size_t work_offset = tab_bytes + 16 + (state_bytes + 15)/16*16;
+  static constexpr size_t bytes = work_offset + sizeof(R)*(size_t)per_elem*EPB + 16;
 };
 
 // Max_dt of one quadrature point (include/Spatial.hpp:793-826): the local time step from the
@@ -503,23 +545,37 @@ __device__ __forceinline__ void local_body(Dev<FaceT> m, const Tab<RS>& tab, int
   // metric identity sum_d [D.n_d + lift.(n_face - B.n_d)] = 0 (free-stream preservation), so
   // this is the same scheme up to roundoff, without differences of nearly equal floats.
   constexpr bool split = !std::is_same<FaceT, double>::value;
+  using L = LocalSmem<ND, RS, R, DEF, VISC, EPB>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   STab<RS, R>& st = *reinterpret_cast<STab<RS, R>*>(smem_raw);
-  R* s_u = reinterpret_cast<R*>(smem_raw + (sizeof(STab<RS, R>) + 15)/16*16);
+  unsigned long long* s_bar = reinterpret_cast<unsigned long long*>(smem_raw + L::tab_bytes);
+  double* s_state = reinterpret_cast<double*>(smem_raw + L::tab_bytes + 16);
+  R* s_u = reinterpret_cast<R*>(smem_raw + L::work_offset);
   R* s_f = s_u + EPB*nv*nq;
   R* s_g = s_f + EPB*ND*nv*nq;
   R* s_bf = s_g + (VISC ? EPB*ND*nv*nq : 0);
-  st.load(tab);
   const int le = threadIdx.x/nq;
   const int q = threadIdx.x%nq;
   const int e0 = e_begin + blockIdx.x*EPB;
   const int e = e0 + le;
   const bool active = threadIdx.x < EPB*nq && e < e_end;
+  // The CTA's element states ([n][nv + 3][nq], contiguous) arrive in shared memory by one bulk
+  // copy while the tables load; where the range is not 16-byte aligned, threads read global
+  // memory directly (same values).
+  const double* g_state = m.elem + (size_t)e0*(nv + 3)*nq;
+  const unsigned state_bytes = unsigned(min(EPB, e_end - e0)*(nv + 3)*nq*sizeof(double));
+  const bool bulk = ((reinterpret_cast<unsigned long long>(g_state) | state_bytes) & 15u) == 0;
+  if (bulk && threadIdx.x == 0) mbar_init(s_bar, 1);
+  __syncthreads();
+  if (bulk && threadIdx.x == 0) bulk_load(s_state, g_state, state_bytes, s_bar);
+  st.load(tab);
   const int ed = e - m.n_car;
   const double d_pos = active ? m.nom_size[e] : 1.;
   const double inv_dpos = 1./d_pos;
   const R inv_dpos_r = split ? R(1)/to_R<R>(d_pos) : R(inv_dpos);
-  const double* state_g = m.elem + (size_t)e*(nv + 3)*nq;
+  const bool staged = bulk && mbar_wait(s_bar, 0, bulk_wait_polls);
+  if (bulk && !staged) atomicOr(m.status + 1, flag_bulk_wait);
+  const double* state_g = (staged ? s_state : g_state) + (size_t)le*(nv + 3)*nq;
 
   R u[nv + 2];   // state + bulk AV + Laplacian AV (include/pde.hpp:79-84)
   R up[nv];      // offset form of the state
@@ -811,7 +867,7 @@ __device__ __forceinline__ void local_body(Dev<FaceT> m, const Tab<RS>& tab, int
       else tss = step;
       st_w[nv*nq + q] = tss;
     } else {
-      tss = st_w[nv*nq + q];
+      tss = state_g[nv*nq + q];
     }
     if constexpr (!split) {
       double mult = update_coef*tss*inv_dpos;
@@ -828,7 +884,7 @@ __device__ __forceinline__ void local_body(Dev<FaceT> m, const Tab<RS>& tab, int
         uu *= mult;
         if (compute_residual) rc[v*nq + q] = FaceT(uu);
         else {
-          double nu = st_w[v*nq + q] + uu;
+          double nu = state_g[v*nq + q] + uu;
           st_w[v*nq + q] = nu;
           up[v] = offset_var<ND, R>(m, e, v, nu);
         }
@@ -851,7 +907,7 @@ __device__ __forceinline__ void local_body(Dev<FaceT> m, const Tab<RS>& tab, int
         const R inc = ur*mult;
         if (compute_residual) rc[v*nq + q] = FaceT(inc);
         else {
-          st_w[v*nq + q] = st_w[v*nq + q] + f64_of(inc);
+          st_w[v*nq + q] = state_g[v*nq + q] + f64_of(inc);
           up[v] += inc;
         }
       }
@@ -867,6 +923,8 @@ __device__ __forceinline__ void local_body(Dev<FaceT> m, const Tab<RS>& tab, int
     __syncthreads();
     write_faces_from_smem<ND, RS, R, FaceT, EPB>(m, st, s_u, e0, e_end);
   }
+  // a bulk copy whose wait gave up must still land before the CTA's shared memory is released
+  if (bulk && !staged) mbar_wait(s_bar, 0, bulk_wait_polls);
 }
 
 // Spatial::Local (include/Spatial.hpp:293-510), one thread per quadrature point, EPB
@@ -880,12 +938,13 @@ k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int comput
                                               ldt);
 }
 
-// The float viscous volume kernel with its registers capped for three resident CTAs per SM:
-// it holds the offset state, its gradient and the reference state at once, and its default
-// allocation drops it to two.
+// The float viscous volume kernel with its registers capped for four resident CTAs per SM
+// (72 registers, 4 bytes of spill at 3D row size 6): it holds the offset state, its gradient
+// and the reference state at once, and its default allocation leaves two CTAs per SM for a
+// kernel whose stalls are mostly memory and shared-memory latency.
 template <int ND, int RS, typename R, bool DEF, bool VISC, typename FaceT, int EPB = Shape<ND, RS>::epb>
-__global__ void __launch_bounds__(Tile<ND, RS, EPB>::threads, 3)
-k_local_3cta(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int compute_residual, int use_filter,
+__global__ void __launch_bounds__(Tile<ND, RS, EPB>::threads, 4)
+k_local_capped(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int compute_residual, int use_filter,
              TmT<R> visc, TmT<R> cond, LocalDt ldt)
 {
   local_body<ND, RS, R, DEF, VISC, FaceT, EPB>(m, tab, e_begin, e_end, stage, compute_residual, use_filter, visc, cond,
@@ -1324,7 +1383,11 @@ __global__ void k_bc_neighbor(Dev<FaceT> m)
 
 // Neighbor of a Cartesian-only mesh in one launch: blocks [0, car_blocks) take the Cartesian
 // connections (as k_neighbor), the remaining blocks the boundary connections (as
-// k_bc_neighbor). Same per-point arithmetic, one launch fewer per stage.
+// k_bc_neighbor) with one warp each. Same per-point arithmetic, one launch fewer per stage.
+// The boundary condition is long double-precision code, and on a small mesh its points would
+// otherwise sit in one CTA, bound by a single SM's FP64 throughput; one warp per CTA spreads
+// them over as many SMs as there are warps of points.
+constexpr int bc_warp = 32;
 template <int ND, int RS, typename R, bool VISC, bool FUSE, typename FaceT>
 __global__ void k_neighbor_car_bc(Dev<FaceT> m, int car_blocks)
 {
@@ -1337,9 +1400,10 @@ __global__ void k_neighbor_car_bc(Dev<FaceT> m, int car_blocks)
       neighbor_point<ND, RS, R, FaceT>(m, c[0], c[1], c[2] | (c[2] << 2) | (1 << 4), q, nullptr, VISC, nullptr);
     }
   } else {
+    if ((int)threadIdx.x >= bc_warp) return;
     const long total = (long)m.n_bc_con*nfq;
-    const long stride = (long)(gridDim.x - car_blocks)*blockDim.x;
-    for (long t = (blockIdx.x - car_blocks)*(long)blockDim.x + threadIdx.x; t < total; t += stride) {
+    const long stride = (long)(gridDim.x - car_blocks)*bc_warp;
+    for (long t = (blockIdx.x - car_blocks)*(long)bc_warp + threadIdx.x; t < total; t += stride) {
       const int i = int(t/nfq), q = int(t%nfq);
       const int* c = m.bc_con + 4*i;
       double gh[ND + 2];
@@ -1581,7 +1645,7 @@ k_max_dt(Dev<FaceT> m, Tab<RS> tab, double msc, double msd, int local_time, TmT<
          TmT<R> cond, double* partials)
 {
   using S = Shape<ND, RS>;
-  constexpr int nq = S::nq, nv = S::nv, nvert = S::nvert;
+  constexpr int nq = S::nq, nv = S::nv;
   const R inv_cfl_c = R(1./(tab.max_cfl*msc));
   const R inv_cfl_d = R(1./(-2/tab.min_eig_diffusion*msd));
   double dt = 1.7976931348623157e308;
@@ -1739,8 +1803,10 @@ static __global__ void k_fp64_fma(double* out, int iters, double a)
 
 // ------------------------------------------------------------------- artificial viscosity
 // Stab_art_visc (src/stabilizing_art_visc.cpp:26-60): per-element smoothness indicator of the
-// specific volume. The CTA stages 1/rho in shared memory; one thread per element forms the
-// sums in the reference's order.
+// specific volume. One thread per quadrature point: each forms its term of the norm and,
+// for the first nd*nfq points, the squared projection of one row onto the highest Legendre
+// mode; the element's threads then reduce both sums as a tree in shared memory (the
+// reference sums in sequence: the two orders differ in the last bits).
 template <int ND, int RS>
 __global__ void __launch_bounds__(Shape<ND, RS>::threads)
 k_av_uncert(const double* elem, const double* nom_size, int n_elem, Tab<RS> tab, double char_speed, double* uncert)
@@ -1748,34 +1814,43 @@ k_av_uncert(const double* elem, const double* nom_size, int n_elem, Tab<RS> tab,
   using S = Shape<ND, RS>;
   constexpr int nq = S::nq, nfq = S::nfq, nv = S::nv, EPB = S::epb;
   __shared__ double s_iv[EPB*nq];
+  __shared__ double s_norm[EPB*nq];
+  __shared__ double s_rough[EPB*nq];
   const int le = threadIdx.x/nq, q = threadIdx.x%nq;
   const int e = blockIdx.x*EPB + le;
-  const bool active = threadIdx.x < EPB*nq && e < n_elem;
-  if (active) s_iv[le*nq + q] = 1./elem[(size_t)e*(nv + 3)*nq + ND*nq + q];
+  const bool in_cta = threadIdx.x < EPB*nq;
+  const bool active = in_cta && e < n_elem;
+  if (in_cta) s_iv[le*nq + q] = active ? 1./elem[(size_t)e*(nv + 3)*nq + ND*nq + q] : 0.;
   __syncthreads();
-  if (!active || q != 0) return;
   const double* iv = s_iv + le*nq;
-  double norm_sq = 0;
-  for (int qq = 0; qq < nq; ++qq) {
+  double tn = 0., tr = 0.;
+  if (active) {
     double w = 1.;
-    for (int d = 0; d < ND; ++d) w *= tab.weight[(qq/ipow(RS, ND - 1 - d))%RS];
-    norm_sq += iv[qq]*iv[qq]*w;
-  }
-  double proj[RS];
-  for (int i = 0; i < RS; ++i) proj[i] = tab.ortho_last[i]*tab.weight[i];
-  double nonsmooth = 0;
-  for (int d = 0; d < ND; ++d) {
-    const int stride = S::stride(d);
-    for (int r = 0; r < nfq; ++r) {
+    for (int d = 0; d < ND; ++d) w *= tab.weight[(q/ipow(RS, ND - 1 - d))%RS];
+    tn = iv[q]*iv[q]*w;
+    if (q < ND*nfq) {
+      const int d = q/nfq, r = q%nfq;
+      const int stride = S::stride(d);
       const double* row = iv + (r/stride)*stride*RS + r%stride;
       double dot = 0.;
-      for (int i = 0; i < RS; ++i) dot += row[i*stride]*proj[i];
+      for (int i = 0; i < RS; ++i) dot += row[i*stride]*(tab.ortho_last[i]*tab.weight[i]);
       double fw = 1.;
       for (int k = 0; k < ND - 1; ++k) fw *= tab.weight[(r/ipow(RS, ND - 2 - k))%RS];
-      nonsmooth += dot*dot*fw;
+      tr = dot*dot*fw;
     }
   }
-  nonsmooth /= norm_sq*ND;
+  if (in_cta) { s_norm[le*nq + q] = tn; s_rough[le*nq + q] = tr; }
+  __syncthreads();
+  constexpr int top = nq <= 1 ? 1 : 1 << (32 - __builtin_clz(nq - 1));   // power of two >= nq
+  for (int h = top/2; h > 0; h >>= 1) {
+    if (in_cta && q < h && q + h < nq) {
+      s_norm[le*nq + q] += s_norm[le*nq + q + h];
+      s_rough[le*nq + q] += s_rough[le*nq + q + h];
+    }
+    __syncthreads();
+  }
+  if (!active || q != 0) return;
+  const double nonsmooth = s_rough[le*nq]/(s_norm[le*nq]*ND);
   const double ramp_center = -4.25*log(double(RS - 1))/log(10.);
   const double half_width = 0.5;
   double indicator = log(nonsmooth)/log(10.);

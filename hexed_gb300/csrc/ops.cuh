@@ -74,7 +74,7 @@ struct Runner
   template <bool DEF, bool VISC, int EPB, bool CAPPED>
   static auto pick_local()
   {
-    if constexpr (CAPPED) return k_local_3cta<ND, RS, R, DEF, VISC, FaceT, EPB>;
+    if constexpr (CAPPED) return k_local_capped<ND, RS, R, DEF, VISC, FaceT, EPB>;
     else return k_local<ND, RS, R, DEF, VISC, FaceT, EPB>;
   }
 
@@ -84,7 +84,7 @@ struct Runner
   {
     const int blocks = (e_end - e_begin + EPB - 1)/EPB;
     constexpr size_t smem = LocalSmem<ND, RS, R, DEF, VISC, EPB>::bytes;
-    // the float viscous 3D kernel is the register-capped variant (k_local_3cta)
+    // the float viscous 3D kernel is the register-capped variant
     constexpr bool capped = std::is_same<R, float>::value && VISC && ND == 3;
     auto kern = pick_local<DEF, VISC, EPB, capped>();
     static bool configured = false;
@@ -152,7 +152,7 @@ struct Runner
     // the leaner Cartesian kernel (the fused one carries the boundary code's registers)
     if (c.n_car_con && c.n_bc_con && !c.n_def_con && (long)c.n_car_con*S::nfq <= 2L*152*block) {
       const int car_blocks = grid_for((long)c.n_car_con*S::nfq, block);
-      const int blocks = car_blocks + grid_for((long)c.n_bc_con*S::nfq, block);
+      const int blocks = car_blocks + grid_for((long)c.n_bc_con*S::nfq, bc_warp);
       ProfScope ps(c, "neighbor_car_bc");
       if (fuse_bc) k_neighbor_car_bc<ND, RS, R, VISC, true, FaceT><<<blocks, block, 0, c.stream>>>(dev(c), car_blocks);
       else k_neighbor_car_bc<ND, RS, R, VISC, false, FaceT><<<blocks, block, 0, c.stream>>>(dev(c), car_blocks);

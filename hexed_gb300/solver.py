@@ -116,6 +116,12 @@ class Context:
                                                    rec.ctypes.data_as(abi.P_int) if records else None))
         return (bool(ok.value), rec) if records else bool(ok.value)
 
+    def device_flags(self):
+        """Flags raised by the kernels (hexed_gpu_device_flags); 0 when none."""
+        f = ctypes.c_int()
+        abi.check(self.lib.hexed_gpu_device_flags(self.handle, ctypes.byref(f)))
+        return f.value
+
     # -------------------------------------------------------------- solver layer
     def update(self, params, read_dt=True):
         out = ctypes.c_double()

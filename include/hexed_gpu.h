@@ -215,6 +215,12 @@ int hexed_gpu_compute_write_face(hexed_gpu_ctx* ctx);
  * ("state is not finite") if any of these values is not finite, where the reference asserts. */
 int hexed_gpu_is_admissible(hexed_gpu_ctx* ctx, int* admissible, int* record);
 
+/* Flags the kernels raised since the context was created (0 = none). Bit 0: a volume kernel
+ * gave up waiting for the bulk copy of its element states and read global memory instead
+ * (results are unaffected; the copy is slower than it should be). No counterpart in the
+ * reference. */
+int hexed_gpu_device_flags(hexed_gpu_ctx* ctx, int* flags);
+
 /* Checks the double <-> float conversions the mixed form does with integer operations against
  * the hardware conversions on n host values; *mismatches = values whose results differ in
  * any bit (values whose float result is subnormal are skipped: the mixed form flushes them

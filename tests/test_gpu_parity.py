@@ -237,3 +237,15 @@ def test_rotated_connections(nd):
         a, b, _ = run_pair(ar, o_op, g_op)
         errs, bad = compare_arenas(a, b)
         assert not bad, (d, errs)
+
+
+@pytest.mark.parametrize("nd", [2, 3])
+def test_bulk_staging_completes(nd):
+    """The volume kernels stage element states by bulk copies; none of the waits gives up."""
+    ar = cartesian_case(2, 5, 4) if nd == 2 else deformed_case(3, 4, 3, abi.BC_RIEMANN)
+    for prec in (abi.FP64, abi.MIXED):
+        with Context(ar.copy(), prec) as c:
+            c.write_face()
+            for _ in range(3):
+                c.update(abi.update_params(max_safety=0.5))
+            assert c.device_flags() == 0
