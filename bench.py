@@ -135,8 +135,8 @@ def kernel_bytes(name, ar, precision="fp64"):
 # DRAM bytes per element and launch measured by ncu on smaller cases of the same kernels
 # (read + write; profiles/k_local_tgv_rs6.md): FP64 at 16^3, mixed at 24^3 elements.
 NCU_DRAM_BYTES_PER_ELEM = {
-    ("local_def_ns", "fp64", 6): (219.576320e6 + 71.881728e6) / 4096,
-    ("local_def_ns", "mixed", 6): (479.313152e6 + 204.372480e6) / 13824,
+    ("local_def_ns", "fp64", 6): (219.963136e6 + 74.511616e6) / 4096,
+    ("local_def_ns", "mixed", 6): (479.854848e6 + 207.921664e6) / 13824,
 }
 
 
@@ -439,9 +439,9 @@ def main():
     value = replicas.job_rate(dofs_per_update(ar) * args.steps, world, ms) / 1e9
     launches = sum(v[0] for v in prof.values())
 
-    # ---- end to end through the C ABI with pinned host buffers: upload the state, one
-    # update, download the state, every step
-    host_in = torch.from_numpy(ar.elem.copy()).pin_memory()
+    # ---- end to end through the C ABI with pinned host buffers: write the conserved state
+    # from host memory, one update, read the conserved state back, every step
+    host_in = torch.from_numpy(np.ascontiguousarray(ar.elem[:, :ar.nv])).pin_memory()
     host_out = torch.empty_like(host_in).pin_memory()
     lib = ctx.lib
     n_bytes = host_in.numel() * 8
@@ -452,11 +452,9 @@ def main():
     f0.record(stream)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        abi.check(lib.hexed_gpu_upload(ctx.handle, abi.ARRAY_ELEM,
-                                       abi.ctypes.cast(host_in.data_ptr(), abi.P_double)))
+        abi.check(lib.hexed_gpu_write_state(ctx.handle, abi.ctypes.cast(host_in.data_ptr(), abi.P_double)))
         ctx.update(p, read_dt=False)
-        abi.check(lib.hexed_gpu_download(ctx.handle, abi.ARRAY_ELEM,
-                                         abi.ctypes.cast(host_out.data_ptr(), abi.P_double)))
+        abi.check(lib.hexed_gpu_read_state(ctx.handle, abi.ctypes.cast(host_out.data_ptr(), abi.P_double)))
     f1.record(stream)
     torch.cuda.synchronize()
     wall_e2e = time.perf_counter() - t0

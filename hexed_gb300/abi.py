@@ -22,7 +22,7 @@ STATUS_NAMES = {0: "HEXED_OK", -1: "HEXED_ERR_INVALID", -2: "HEXED_ERR_CUDA", -3
 BC_FREESTREAM, BC_RIEMANN, BC_NONPENETRATION, BC_COPY, BC_OUTFLOW, BC_PRESSURE_OUTFLOW, BC_NO_SLIP = range(7)
 THERMAL_HEAT_FLUX, THERMAL_ENERGY, THERMAL_EQUILIBRIUM = range(3)
 ARRAY_ELEM, ARRAY_RCACHE, ARRAY_FACE, ARRAY_BC_CACHE, ARRAY_NOM_SIZE, ARRAY_VERT_TSS, ARRAY_BC_NRML, \
-    ARRAY_REF_STATE = range(8)
+    ARRAY_REF_STATE, ARRAY_JAC, ARRAY_FACE_NRML, ARRAY_DEF_CON_NRML = range(11)
 INT_CAR_CON, INT_BC_CON = 0, 1
 FP64, MIXED = 0, 1
 
@@ -138,6 +138,9 @@ def load_library(path=LIB_PATH):
         "hexed_gpu_check_conversions": ([P_double, ctypes.c_long, ctypes.POINTER(ctypes.c_long)], c_int),
         "hexed_gpu_is_admissible": ([vp, P_int, P_int], c_int),
         "hexed_gpu_device_flags": ([vp, P_int], c_int),
+        "hexed_gpu_compute_jacobian": ([vp, P_double], c_int),
+        "hexed_gpu_write_state": ([vp, P_double], c_int),
+        "hexed_gpu_read_state": ([vp, P_double], c_int),
         "hexed_gpu_launch_shape": ([vp, P_int, P_int], c_int),
         "hexed_gpu_write_range": ([vp, c_int, ctypes.c_long, ctypes.c_long, P_double], c_int),
         "hexed_gpu_read_range": ([vp, c_int, ctypes.c_long, ctypes.c_long, P_double], c_int),

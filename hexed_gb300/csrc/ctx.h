@@ -46,6 +46,7 @@ struct OpsTable {
   void (*segment_residual_norms)(Ctx&, int n_seg, const int* d_begin, const int* d_count, double* d_out);
   int (*local_elems_per_cta)(int variant);
   void (*admissible)(Ctx&, int* d_record);
+  void (*compute_jacobian)(Ctx&, const double* d_vert_pos, double* d_fn, double* d_vtss);
 };
 
 // A captured multi-update sequence and the inputs it was captured for.

@@ -1164,103 +1164,160 @@ __global__ void k_neighbor(Dev<FaceT> m)
 
 // ------------------------------------------------------------------- boundary conditions
 // Characteristics (include/pde.hpp:182-256) solved with partially pivoted LU; apply_char
-// (src/Boundary_condition.cpp:82-95).
-template <int ND>
+// (src/Boundary_condition.cpp:82-95). Every loop is unrolled and the pivot row swaps are
+// selects, so the 3x3 system stays in registers (no local-memory arrays), and divisions
+// are reciprocal multiplies (one per pivot): on this part each warp-wide FP64 instruction
+// holds an SM's FP64 pipe for many cycles, and boundary points run this per face point.
+template <int ND, typename R = double>
 struct Characteristics {
-  double vals[3], vecs[3][3], dir[ND], mass, veloc[ND];
-  double lu[3][3]; int piv[3];
-  __device__ double nrml(const double* v) const { double r = 0.; for (int d = 0; d < ND; ++d) r += dir[d]*v[d]; return r; }
-  __device__ void tang(const double* v, double* out) const { double n = nrml(v); for (int d = 0; d < ND; ++d) out[d] = v[d] - dir[d]*n; }
-  __device__ Characteristics(const double* state, const double* direction)
+  R vals[3], vecs[3][3], dir[ND], mass, veloc[ND];
+  R lu[3][3], inv_diag[3]; int piv[3];
+  __device__ R nrml(const R* v) const
   {
-    double nsq = 0.;
+    R r = 0;
+    #pragma unroll
+    for (int d = 0; d < ND; ++d) r += dir[d]*v[d];
+    return r;
+  }
+  __device__ void tang(const R* v, R* out) const
+  {
+    R n = nrml(v);
+    #pragma unroll
+    for (int d = 0; d < ND; ++d) out[d] = v[d] - dir[d]*n;
+  }
+  __device__ Characteristics(const R* state, const R* direction)
+  {
+    R nsq = 0;
+    #pragma unroll
     for (int d = 0; d < ND; ++d) nsq += direction[d]*direction[d];
-    double norm = sqrt(nsq);
-    for (int d = 0; d < ND; ++d) dir[d] = direction[d]/norm;
+    const R inv_norm = R(1)/sqrt(nsq);
+    #pragma unroll
+    for (int d = 0; d < ND; ++d) dir[d] = direction[d]*inv_norm;
     mass = state[ND];
-    for (int d = 0; d < ND; ++d) veloc[d] = state[d]/mass;
-    double vsq = 0.;
+    const R inv_mass = R(1)/mass;
+    #pragma unroll
+    for (int d = 0; d < ND; ++d) veloc[d] = state[d]*inv_mass;
+    R vsq = 0;
+    #pragma unroll
     for (int d = 0; d < ND; ++d) vsq += veloc[d]*veloc[d];
-    double pres = .4*(state[ND + 1] - .5*mass*vsq);
-    double sound_speed = sqrt(1.4*fmax(pres, 0.)/mass);
+    R pres = R(.4)*(state[ND + 1] - R(.5)*mass*vsq);
+    R sound_speed = sqrt(R(1.4)*fmax(pres, R(0))*inv_mass);
     vals[2] = nrml(veloc);
     vals[0] = vals[2] - sound_speed;
     vals[1] = vals[2] + sound_speed;
+    #pragma unroll
     for (int sign = 0; sign < 2; ++sign) {
-      double d_veloc = (2*sign - 1)*sound_speed/mass*1.;
-      double d_pres = 1.4*pres/mass*1.;
-      vecs[0][sign] = 1.*vals[2] + mass*d_veloc;
-      vecs[1][sign] = 1.;
-      vecs[2][sign] = d_pres/.4 + .5*1.*vsq + mass*vals[2]*d_veloc;
+      R d_veloc = R(2*sign - 1)*sound_speed*inv_mass;
+      R d_pres = R(1.4)*pres*inv_mass;
+      vecs[0][sign] = vals[2] + mass*d_veloc;
+      vecs[1][sign] = 1;
+      vecs[2][sign] = d_pres/R(.4) + R(.5)*vsq + mass*vals[2]*d_veloc;
     }
-    vecs[0][2] = 1.*vals[2];
-    vecs[1][2] = 1.;
-    vecs[2][2] = .5*1.*vsq;
-    for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) lu[i][j] = vecs[i][j];
-    for (int i = 0; i < 3; ++i) piv[i] = i;
+    vecs[0][2] = vals[2];
+    vecs[1][2] = 1;
+    vecs[2][2] = R(.5)*vsq;
+    #pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      piv[i] = i;
+      #pragma unroll
+      for (int j = 0; j < 3; ++j) lu[i][j] = vecs[i][j];
+    }
+    #pragma unroll
     for (int k = 0; k < 3; ++k) {
       int p = k;
-      for (int i = k + 1; i < 3; ++i) if (fabs(lu[i][k]) > fabs(lu[p][k])) p = i;
-      if (p != k) {
-        for (int j = 0; j < 3; ++j) { double t = lu[k][j]; lu[k][j] = lu[p][j]; lu[p][j] = t; }
-        int t = piv[k]; piv[k] = piv[p]; piv[p] = t;
-      }
+      R best = fabs(lu[k][k]);
+      #pragma unroll
+      for (int i = k + 1; i < 3; ++i) if (fabs(lu[i][k]) > best) { p = i; best = fabs(lu[i][k]); }
+      #pragma unroll
       for (int i = k + 1; i < 3; ++i) {
-        double f = lu[k][k] != 0. ? lu[i][k]/lu[k][k] : 0.;
+        const bool sw = p == i;
+        #pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const R a = lu[k][j], b = lu[i][j];
+          lu[k][j] = sw ? b : a;
+          lu[i][j] = sw ? a : b;
+        }
+        const int pa = piv[k], pb = piv[i];
+        piv[k] = sw ? pb : pa;
+        piv[i] = sw ? pa : pb;
+      }
+      inv_diag[k] = lu[k][k] != R(0) ? R(1)/lu[k][k] : R(0);
+      #pragma unroll
+      for (int i = k + 1; i < 3; ++i) {
+        const R f = lu[i][k]*inv_diag[k];
         lu[i][k] = f;
+        #pragma unroll
         for (int j = k + 1; j < 3; ++j) lu[i][j] -= f*lu[k][j];
       }
     }
   }
-  __device__ void solve(const double* b, double* x) const
+  __device__ void solve(const R* b, R* x) const
   {
-    double y[3];
+    R y[3];
+    #pragma unroll
     for (int i = 0; i < 3; ++i) {
-      double acc = b[piv[i]];
+      R acc = piv[i] == 0 ? b[0] : piv[i] == 1 ? b[1] : b[2];
+      #pragma unroll
       for (int j = 0; j < i; ++j) acc -= lu[i][j]*y[j];
       y[i] = acc;
     }
+    #pragma unroll
     for (int i = 2; i >= 0; --i) {
-      double acc = y[i];
+      R acc = y[i];
+      #pragma unroll
       for (int j = i + 1; j < 3; ++j) acc -= lu[i][j]*x[j];
-      x[i] = lu[i][i] != 0. ? acc/lu[i][i] : 0.;
+      x[i] = acc*inv_diag[i];
     }
   }
-  __device__ void decomp(const double* state, double (*d)[3]) const
+  __device__ void decomp(const R* state, R (*d)[3]) const
   {
-    double mmtm[ND], tm[ND], tv[ND], corr[ND];
+    R mmtm[ND], tm[ND], tv[ND], corr[ND];
+    #pragma unroll
     for (int i = 0; i < ND; ++i) mmtm[i] = state[i];
     tang(mmtm, tm);
     tang(veloc, tv);
+    #pragma unroll
     for (int i = 0; i < ND; ++i) corr[i] = tm[i] - state[ND]*tv[i];
-    double vc = 0.;
+    R vc = 0;
+    #pragma unroll
     for (int i = 0; i < ND; ++i) vc += veloc[i]*corr[i];
-    double s1d[3] = {nrml(mmtm), state[ND], state[ND + 1] - vc};
-    double eb[3];
+    R s1d[3] = {nrml(mmtm), state[ND], state[ND + 1] - vc};
+    R eb[3];
     solve(s1d, eb);
-    double ed[3][3];
-    for (int r = 0; r < 3; ++r) for (int c = 0; c < 3; ++c) ed[r][c] = vecs[r][c]*eb[c];
+    R ed[3][3];
+    #pragma unroll
+    for (int r = 0; r < 3; ++r)
+      #pragma unroll
+      for (int c = 0; c < 3; ++c) ed[r][c] = vecs[r][c]*eb[c];
+    #pragma unroll
     for (int c = 0; c < 3; ++c) {
       d[ND][c] = ed[1][c];
       d[ND + 1][c] = ed[2][c];
+      #pragma unroll
       for (int i = 0; i < ND; ++i) d[i][c] = dir[i]*ed[0][c] + tv[i]*eb[c];
     }
+    #pragma unroll
     for (int i = 0; i < ND; ++i) d[i][2] += corr[i];
     d[ND + 1][2] += vc;
   }
 };
 
-template <int ND>
-__device__ void apply_char(const double* state, const double* normal, int sign, const double* inside,
-                           const double* outside, double* out)
+template <int ND, typename R = double>
+__device__ void apply_char(const R* state, const R* normal, int sign, const R* inside, const R* outside, R* out)
 {
   constexpr int nv = ND + 2;
-  Characteristics<ND> ch(state, normal);
-  double di[nv][3], fo[nv][3];
+  Characteristics<ND, R> ch(state, normal);
+  R di[nv][3], fo[nv][3];
   ch.decomp(inside, di);
   ch.decomp(outside, fo);
-  for (int i = 0; i < 3; ++i) if (sign*ch.vals[i] > 0) for (int r = 0; r < nv; ++r) di[r][i] = fo[r][i];
-  for (int r = 0; r < nv; ++r) { double acc = 0.; for (int c = 0; c < 3; ++c) acc += di[r][c]; out[r] = acc; }
+  #pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const bool take = sign*ch.vals[i] > 0;
+    #pragma unroll
+    for (int r = 0; r < nv; ++r) di[r][i] = take ? fo[r][i] : di[r][i];
+  }
+  #pragma unroll
+  for (int r = 0; r < nv; ++r) { R acc = 0; for (int c = 0; c < 3; ++c) acc += di[r][c]; out[r] = acc; }
 }
 
 __device__ __forceinline__ double ipow_d(double x, int e) { double r = 1; for (int i = 0; i < e; ++i) r *= x; return r; }
@@ -1301,6 +1358,31 @@ __device__ void bc_state_point(const Dev<FaceT>& m, int i_bc, int q, double* gh)
       for (int v = 0; v < nv; ++v) gh[v] = b.freestream[v];
       break;
     case HEXED_BC_RIEMANN_INVARIANTS: {
+      if constexpr (split) {
+        // Mixed form: apply_char is linear in (inside, outside) for a fixed linearization
+        // state and reproduces a state equal on both sides, so the ghost offset from the
+        // reference is apply_char of the offsets; that runs in float with the accuracy of the
+        // offsets. The clamps of the reference (src/Boundary_condition.cpp:126-130) replace
+        // the offset only where they act.
+        float d_in[nv], d_fs[nv], u_in[nv], nf[ND], st[nv], rf[nv];
+        for (int v = 0; v < nv; ++v) {
+          rf[v] = to_R<float>(ref[v]);
+          d_in[v] = float(in[v*nfq + q]);
+          d_fs[v] = to_R<float>(b.freestream[v] - ref[v]);
+          u_in[v] = rf[v] + d_in[v];
+        }
+        for (int d = 0; d < ND; ++d) nf[d] = to_R<float>(n[d]);
+        apply_char<ND, float>(u_in, nf, 1 - 2*ifs, d_in, d_fs, st);
+        if (rf[ND] + st[ND] < u_in[ND]*.5f) st[ND] = u_in[ND]*.5f - rf[ND];
+        float sq = 0.f, isq = 0.f;
+        for (int d = 0; d < ND; ++d) { sq += (rf[d] + st[d])*(rf[d] + st[d]); isq += u_in[d]*u_in[d]; }
+        const float kin = .5f*sq/(rf[ND] + st[ND]);
+        const float ikin = .5f*isq/u_in[ND];
+        const float half_int = (u_in[ND + 1] - ikin)*.5f;
+        if (rf[ND + 1] + st[ND + 1] - kin < half_int) st[ND + 1] = fmaxf(kin + half_int, 0.f) - rf[ND + 1];
+        for (int v = 0; v < nv; ++v) { gh[v] = ref[v] + f64_of(st[v]); sc[v*nfq + q] = inside[v]; }
+        break;
+      }
       double st[nv];
       apply_char<ND>(inside, n, 1 - 2*ifs, inside, b.freestream, st);
       st[ND] = fmax(st[ND], inside[ND]/2);

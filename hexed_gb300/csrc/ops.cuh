@@ -6,6 +6,7 @@
 // compute_navier_stokes (src/kernels_diffusive.cpp:8-32), max_dt_* (src/kernels_max_dt.cpp).
 #pragma once
 #include "kernels.cuh"
+#include "metrics.cuh"
 #include "ctx.h"
 
 namespace hx {
@@ -114,6 +115,41 @@ struct Runner
   }
 
   static int local_elems_per_cta(int v) { return has_variants(false) ? epb_of(v) : S::epb; }
+
+  // Deformed_element::set_jacobian + Solver::calc_jacobian (metrics.cuh) from the deformed
+  // elements' vertex positions d_vert_pos [n_def][nvert][nd]; d_fn [n_def][2nd][nd][nfq] and
+  // d_vtss [n_def][nvert] are scratch. Leaves jac, face_nrml, def_con_nrml, bc_nrml, vert_tss.
+  static void compute_jacobian(Ctx& c, const double* d_vert_pos, double* d_fn, double* d_vtss)
+  {
+    if (c.n_def) {
+      constexpr size_t smem = MetricSmem<ND, RS>::bytes;
+      static bool configured = false;
+      if (!configured) {
+        cudaFuncSetAttribute(k_set_jacobian<ND, RS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        configured = true;
+      }
+      ProfScope ps(c, "set_jacobian");
+      k_set_jacobian<ND, RS><<<c.n_def, (S::nq + 31)/32*32, smem, c.stream>>>(d_vert_pos, c.nom_size + c.n_car, tab(c),
+                                                                             c.jac, d_fn, d_vtss);
+      k_identity_face_normals<ND, RS><<<grid_for((long)c.n_def*2*ND*ND*S::nfq, 256), 256, 0, c.stream>>>(c.face_nrml,
+                                                                                                      c.n_def);
+      if (c.n_def_con)
+        k_def_con_normals<ND, RS><<<grid_for((long)c.n_def_con*S::nfq, 256), 256, 0, c.stream>>>(
+            c.def_con, c.n_def_con, c.n_car, d_fn, c.face_nrml, c.def_con_nrml);
+    }
+    if (c.n_bc_con)
+      k_bc_normals<ND, RS><<<grid_for((long)c.n_bc_con*S::nfq, 256), 256, 0, c.stream>>>(c.bc_con, c.n_bc_con, c.n_car,
+                                                                                      d_fn, c.face_nrml, c.bc_nrml);
+    const int n_elem = c.n_car + c.n_def;
+    k_element_vtss<ND><<<grid_for((long)n_elem*S::nvert, 256), 256, 0, c.stream>>>(c.nom_size, c.n_car, n_elem, d_vtss,
+                                                                                 c.vert_tss);
+    if (c.n_vert > 0) {
+      k_vertex_min_init<<<grid_for(c.n_vert, 256), 256, 0, c.stream>>>(c.vmax, c.n_vert);
+      k_vertex_min<ND><<<grid_for((long)n_elem*S::nvert, 256), 256, 0, c.stream>>>(c.vert_id, n_elem, c.vert_tss, c.vmax);
+      k_vertex_gather<ND><<<grid_for((long)n_elem*S::nvert, 256), 256, 0, c.stream>>>(c.vert_id, n_elem, c.vmax,
+                                                                                    c.vert_tss);
+    }
+  }
 
   // Solver::is_admissible (src/Solver.cpp:921-959); record [n_elem] and status[0] cleared first
   static void admissible(Ctx& c, int* record)
@@ -305,7 +341,7 @@ struct Runner
   {
     static const OpsTable t = {
       compute_euler, compute_navier_stokes, max_dt, refine, write_face, bc_state, bc_flux, residual_norm,
-      set_art_visc_admis, segment_residual_norms, local_elems_per_cta, admissible,
+      set_art_visc_admis, segment_residual_norms, local_elems_per_cta, admissible, compute_jacobian,
     };
     return &t;
   }

@@ -72,6 +72,7 @@ class Arena:
         # set-up only data (not part of the device arena)
         self.qpoint_pos = None        # [E][nd][nq] physical qpoint positions
         self.vert_ids = None          # [E][nvert] global vertex ids
+        self.vert_pos = None          # [E][nvert][nd] element vertex positions
 
     def finalize(self):
         nv, nfq = self.nv, self.nfq
@@ -291,6 +292,7 @@ def structured_mesh(n_dim, row_size, n_per_dim, lo, hi, deformed=False, displace
         on_b = (gv == 0) | (gv == n)
         gpos = gpos + displacement(gpos.copy(), on_b)
     vert_pos = gpos[vert_ids]                                           # [E][nvert][nd]
+    ar.vert_pos = vert_pos
     if deformed:
         jac_dat, fn, vtss, qpos = deformed_metrics(vert_pos, ar.nom_size, basis, n_dim)
         ar.jac[:] = jac_dat
@@ -407,6 +409,7 @@ def general_mesh(n_dim, row_size, vert_pos, nom_size, is_deformed, connections, 
     nfq = ar.nfq
     ar.nom_size[:] = nom_size
     vert_pos = np.asarray(vert_pos, dtype=np.float64)
+    ar.vert_pos = vert_pos
     if n_def:
         jac_dat, fn, vtss_def, qpos_def = deformed_metrics(vert_pos[n_car:], ar.nom_size[n_car:], basis, nd)
         ar.jac[:] = jac_dat

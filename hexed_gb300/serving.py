@@ -429,6 +429,9 @@ def autotune(pool, n_probes=4, reps=3, clock=time.perf_counter):
 # ------------------------------------------------------------------ server
 @dataclass
 class Result:
+    """Outcome of one request. status: "converged"; "max_updates" (retired unconverged);
+    "diverged" (non-finite residual, elements reset to a quiet state); "rejected" (no pool of
+    its row size, or larger than its pool); "cancelled"."""
     rid: int
     arrival: float
     admitted: float
@@ -436,6 +439,7 @@ class Result:
     updates: int
     residual: float
     converged: bool
+    status: str = "converged"
 
     @property
     def latency(self):
@@ -449,11 +453,14 @@ class ServeStats:
     batches: int = 0
 
     def summary(self):
-        lat = np.array([r.latency for r in self.results]) if self.results else np.zeros(1)
-        first = min((r.arrival for r in self.results), default=0.)
-        last = max((r.done for r in self.results), default=0.)
-        return {"solves": len(self.results), "converged": sum(r.converged for r in self.results),
-                "solves_per_s": len(self.results) / max(last - first, 1e-9),
+        served = [r for r in self.results if r.status not in ("rejected", "cancelled")]
+        lat = np.array([r.latency for r in served]) if served else np.zeros(1)
+        first = min((r.arrival for r in served), default=0.)
+        last = max((r.done for r in served), default=0.)
+        return {"solves": len(served), "converged": sum(r.converged for r in served),
+                "rejected": sum(r.status == "rejected" for r in self.results),
+                "cancelled": sum(r.status == "cancelled" for r in self.results),
+                "solves_per_s": len(served) / max(last - first, 1e-9),
                 "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
                 "wall_s": self.wall, "batches": self.batches,
                 "updates": int(sum(r.updates for r in self.results))}
@@ -466,16 +473,26 @@ class Server:
     one-solve-at-a-time loop the batched one is compared with)."""
 
     def __init__(self, precision=abi.FP64, row_sizes=(4, 6), capacity=None, max_live=None, tol=1e-8,
-                 max_updates=400_000, updates_per_batch=None, params=None, memory_fraction=0.5, tune=True):
+                 max_updates=400_000, updates_per_batch=None, params=None, memory_fraction=0.5, tune=True,
+                 pools=None):
         self.tol, self.max_updates = tol, max_updates
         self.max_live = max_live
+        self.cancelled = set()
         k_default = {4: 20, 6: 20}
+        if pools is not None:        # pools built by the caller (any objects with the Pool interface)
+            self.pools = dict(pools)
+            self.tuning = {}
+            return
         self.pools = {}
         for rs in row_sizes:
             cap = capacity or capacity_from_free_memory(rs, precision, memory_fraction / len(row_sizes))
             k = (updates_per_batch or {}).get(rs, k_default.get(rs, 20))
             self.pools[rs] = Pool(rs, precision, capacity=cap, params=params, updates_per_batch=k)
         self.tuning = {rs: autotune(p) for rs, p in self.pools.items()} if tune else {}
+
+    def cancel(self, rid):
+        """Withdraw a request: dropped if still queued, retired at the next batch if live."""
+        self.cancelled.add(rid)
 
     def close(self):
         for p in self.pools.values():
@@ -490,30 +507,50 @@ class Server:
     def n_live(self):
         return sum(len(p.slots) for p in self.pools.values())
 
-    def run(self, requests, clock=time.perf_counter, on_retire=None):
-        """Serve `requests` (arrival times in seconds from the start) to completion."""
+    def run(self, requests, clock=time.perf_counter, on_retire=None, cases=None, sleep=time.sleep):
+        """Serve `requests` (arrival times in seconds from the start) to completion. `cases`
+        maps request ids to prepared CaseData (otherwise each case is built at admission)."""
         pending = sorted(requests, key=lambda r: r.arrival)
         queue = []
         stats = ServeStats()
         t0 = clock()
         i_next = 0
+        cases = cases or {}
+
+        def finish(req, status, now, admitted=0., updates=0, residual=float("nan")):
+            stats.results.append(Result(req.rid, req.arrival, admitted, now, updates, residual,
+                                        status == "converged", status))
+
         while i_next < len(pending) or queue or self.n_live():
             now = clock() - t0
             while i_next < len(pending) and pending[i_next].arrival <= now:
-                queue.append(pending[i_next])
+                req = pending[i_next]
                 i_next += 1
-            if not queue and not self.n_live():
-                # idle until the next arrival
-                time.sleep(max(0., min(pending[i_next].arrival - now, 0.01)))
-                continue
+                pool = self.pools.get(req.row_size)
+                if pool is None or req.side < 1 or req.side * req.side > pool.cap:
+                    finish(req, "rejected", now)
+                else:
+                    queue.append(req)
             waiting = []
             for req in queue:
+                if req.rid in self.cancelled:
+                    finish(req, "cancelled", now)
+                    continue
                 if self.max_live is not None and self.n_live() >= self.max_live:
                     waiting.append(req)
                     continue
-                if self.pools[req.row_size].admit(req, now=now) is None:
+                if self.pools[req.row_size].admit(req, case=cases.get(req.rid), now=now) is None:
                     waiting.append(req)
             queue = waiting
+            if not self.n_live():
+                # an empty device that still cannot take a queued request never will
+                for req in queue:
+                    finish(req, "rejected", now)
+                queue = []
+                if i_next < len(pending):
+                    # idle until the next arrival
+                    sleep(max(0., min(pending[i_next].arrival - now, 0.01)))
+                continue
             for p in self.pools.values():
                 p.enqueue_batch()
             stats.batches += 1
@@ -526,9 +563,11 @@ class Server:
                     finite = bool(np.all(np.isfinite(r)))
                     res = normalized(slot, r) if finite else float("nan")
                     slot.residual = res
-                    if not finite or res <= self.tol or slot.updates >= self.max_updates:
-                        stats.results.append(Result(slot.req.rid, slot.req.arrival, slot.admitted_at, done_now,
-                                                    slot.updates, res, finite and res <= self.tol))
+                    status = ("cancelled" if slot.req.rid in self.cancelled else "diverged" if not finite
+                              else "converged" if res <= self.tol else "max_updates" if slot.updates >= self.max_updates
+                              else None)
+                    if status is not None:
+                        finish(slot.req, status, done_now, slot.admitted_at, slot.updates, res)
                         if on_retire is not None:
                             on_retire(p, slot)
                         p.retire(slot, diverged=not finite)

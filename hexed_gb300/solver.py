@@ -69,6 +69,18 @@ class Context:
         for w in (abi.ARRAY_ELEM, abi.ARRAY_RCACHE, abi.ARRAY_FACE, abi.ARRAY_BC_CACHE):
             self.download(w, self._array(w))
 
+    def write_state(self, state):
+        """Conserved state [n_elem][nv][nq] into the device arena (hexed_gpu_write_state)."""
+        st = np.ascontiguousarray(state, dtype=np.float64)
+        abi.check(self.lib.hexed_gpu_write_state(self.handle, st.ctypes.data_as(abi.P_double)))
+
+    def read_state(self, out=None):
+        """Conserved state [n_elem][nv][nq] from the device arena (hexed_gpu_read_state)."""
+        a = self.arena
+        out = np.empty((a.n_elem, a.nv, a.nq)) if out is None else out
+        abi.check(self.lib.hexed_gpu_read_state(self.handle, out.ctypes.data_as(abi.P_double)))
+        return out
+
     def synchronize(self):
         abi.check(self.lib.hexed_gpu_synchronize(self.handle))
 
@@ -115,6 +127,12 @@ class Context:
         abi.check(self.lib.hexed_gpu_is_admissible(self.handle, ctypes.byref(ok),
                                                    rec.ctypes.data_as(abi.P_int) if records else None))
         return (bool(ok.value), rec) if records else bool(ok.value)
+
+    def compute_jacobian(self, vert_pos_def):
+        """Metric set-up of the deformed elements on the device from their vertex positions
+        [n_def][nvert][nd] (hexed_gpu_compute_jacobian)."""
+        vp = np.ascontiguousarray(vert_pos_def, dtype=np.float64)
+        abi.check(self.lib.hexed_gpu_compute_jacobian(self.handle, vp.ctypes.data_as(abi.P_double)))
 
     def device_flags(self):
         """Flags raised by the kernels (hexed_gpu_device_flags); 0 when none."""

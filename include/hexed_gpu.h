@@ -136,8 +136,11 @@ enum hexed_array {
   HEXED_ARRAY_NOM_SIZE = 4,
   HEXED_ARRAY_VERT_TSS = 5,
   HEXED_ARRAY_BC_NRML = 6,
-  HEXED_ARRAY_REF_STATE = 7   /* mixed form only: [n_elem][nv] reference state of each element
+  HEXED_ARRAY_REF_STATE = 7,  /* mixed form only: [n_elem][nv] reference state of each element
                                  (write it before the element's state and traces) */
+  HEXED_ARRAY_JAC = 8,        /* [n_def][nd*nd + 1][nq] (read / write) */
+  HEXED_ARRAY_FACE_NRML = 9,  /* [n_def][2nd][nd][nfq] */
+  HEXED_ARRAY_DEF_CON_NRML = 10 /* [n_def_con][nd][nfq] */
 };
 
 /* Arithmetic of the volume and face kernels. */
@@ -208,6 +211,16 @@ int hexed_gpu_compute_prolong(hexed_gpu_ctx* ctx, int scale, int offset);
 int hexed_gpu_compute_restrict(hexed_gpu_ctx* ctx, int scale, int offset);
 int hexed_gpu_compute_write_face(hexed_gpu_ctx* ctx);
 
+/* Metric set-up on the device: Deformed_element::set_jacobian (src/Deformed_element.cpp:15-134)
+ * for every deformed element from its vertex positions vert_pos [n_def][nvert][nd] (vertex bit
+ * d <-> reference dimension d, dim 0 most significant), then the connection part of
+ * Solver::calc_jacobian (src/Solver.cpp:273-381): shared normals of the deformed connections,
+ * boundary normals, and the vertex time-step scale shared (minimum) over the vertex table when
+ * the arena has one. Overwrites jac, face_nrml, def_con_nrml, bc_nrml and vert_tss of the
+ * arena. For conforming deformed meshes (hanging faces only between Cartesian elements, as
+ * the arena builds them). */
+int hexed_gpu_compute_jacobian(hexed_gpu_ctx* ctx, const double* vert_pos);
+
 /* Solver::is_admissible (src/Solver.cpp:921-959, thermo::admissible src/thermo.cpp:6-18):
  * *admissible = 1 if density and total energy are positive at every point of every element
  * state, element face trace and fine mortar face, else 0. record (optional, [n_elem] of the
@@ -244,6 +257,14 @@ int hexed_gpu_launch_shape(hexed_gpu_ctx* ctx, int* local_elems_per_cta, int* fa
  * Call this before the states and traces it applies to are written. No effect in the FP64
  * form. No counterpart in the reference. */
 int hexed_gpu_set_reference_state(hexed_gpu_ctx* ctx, const double* state);
+
+/* The conserved state of the active elements as host arrays [n_elem][nv][nq] (the first nv
+ * rows of each element of the arena, without the time-step and AV rows): the copy a caller
+ * whose state lives in host memory makes around each update, as the reference's elements hold
+ * it (Element::state(), src/Element.cpp:119-142). One strided copy; returns when it is
+ * complete. Pinned host memory gives the full transfer rate. */
+int hexed_gpu_write_state(hexed_gpu_ctx* ctx, const double* state);
+int hexed_gpu_read_state(hexed_gpu_ctx* ctx, double* state);
 
 /* Write_face for elements [elem_begin, elem_begin + elem_count) only: initialises the face
  * traces of one newly admitted solve without touching the traces of solves already running.

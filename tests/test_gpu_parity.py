@@ -249,3 +249,19 @@ def test_bulk_staging_completes(nd):
             for _ in range(3):
                 c.update(abi.update_params(max_safety=0.5))
             assert c.device_flags() == 0
+
+
+@pytest.mark.parametrize("precision", [abi.FP64, abi.MIXED])
+def test_write_and_read_state(precision):
+    """hexed_gpu_write_state / read_state move exactly the conserved rows of every element."""
+    ar = deformed_case(3, 3, 3, abi.BC_RIEMANN)
+    rng = np.random.default_rng(4)
+    with Context(ar.copy(), precision) as c:
+        st = c.read_state()
+        assert np.array_equal(st, ar.elem[:, :ar.nv])
+        new = ar.elem[:, :ar.nv] * (1 + 0.01 * rng.standard_normal(st.shape))
+        c.write_state(new)
+        full = c.download(abi.ARRAY_ELEM)
+        assert np.array_equal(full[:, :ar.nv], new)
+        assert np.array_equal(full[:, ar.nv:], ar.elem[:, ar.nv:])   # time-step and AV rows untouched
+        assert np.array_equal(c.read_state(), new)

@@ -133,3 +133,29 @@ def test_mixed_solve_reaches_fp64_tolerance():
         counts[prec] = {r.rid: r.updates for r in st.results}
     for rid in (0, 1):
         assert counts[abi.MIXED][rid] <= 1.2 * counts[abi.FP64][rid] + 100
+
+
+def test_diverged_solve_is_retired_without_touching_the_others():
+    """A request whose initial state is not finite (planted on the host) is retired as
+    diverged; the solves sharing its pool finish bit-identical to a run without it."""
+    reqs = [serving.Request(0, 6, 4, 0.5, 2., seed=1), serving.Request(1, 5, 4, 0.4, -3., seed=2),
+            serving.Request(2, 7, 4, 0.6, 5., seed=3)]
+    bad = serving.build_case(reqs[1])
+    bad.elem[3, 2, 5] = np.nan
+    runs = {}
+    for with_bad in (True, False):
+        got = {}
+
+        def grab(pool, slot):
+            got[slot.req.rid] = pool.state(slot).copy()
+
+        with serving.Server(abi.FP64, row_sizes=(4,), capacity=512, tol=1e-3, params=PARAMS, tune=False,
+                            updates_per_batch={4: 10}) as srv:
+            st = srv.run(reqs if with_bad else [reqs[0], reqs[2]], on_retire=grab,
+                         cases={1: bad} if with_bad else None)
+        runs[with_bad] = (got, {r.rid: r.status for r in st.results})
+    got_bad, status_bad = runs[True]
+    got_ok, status_ok = runs[False]
+    assert status_bad == {0: "converged", 1: "diverged", 2: "converged"}
+    for rid in (0, 2):
+        assert np.array_equal(got_bad[rid], got_ok[rid])

@@ -70,3 +70,82 @@ def test_pool_memory_estimate_orders():
     b64 = serving.pool_bytes_per_element(6, abi.FP64)
     b32 = serving.pool_bytes_per_element(6, abi.MIXED)
     assert 4000 < b64 < 6000 and b32 < b64
+
+
+class FakePool:
+    """Pool stand-in for the scheduler: a solve 'converges' after a fixed number of updates
+    (its side, in batches); `fail` solve ids report non-finite residuals."""
+
+    def __init__(self, rs, cap=400, k=10, fail=()):
+        self.rs, self.cap, self.k, self.fail = rs, cap, k, set(fail)
+        self.slots = []
+        self.used = 0
+        self.admitted, self.retired = [], []
+
+    def admit(self, req, case=None, now=0.):
+        n = req.side * req.side
+        if self.used + n > self.cap:
+            return None
+        self.used += n
+        slot = serving.Slot(req, 0, n, 0, None, None, None, admitted_at=now)
+        self.slots.append(slot)
+        self.admitted.append(req.rid)
+        return slot
+
+    def enqueue_batch(self):
+        for s in self.slots:
+            s.updates += self.k
+
+    def residuals(self):
+        out = []
+        for s in self.slots:
+            if s.req.rid in self.fail:
+                out.append([np.nan] * 3)
+            else:
+                out.append([10.0 ** (-s.updates / (self.k * s.req.side))] * 3)
+        return np.array(out)
+
+    def retire(self, slot, diverged=False):
+        self.slots.remove(slot)
+        self.used -= slot.n_elem
+        self.retired.append((slot.req.rid, diverged))
+
+
+def _reqs(specs):
+    return [serving.Request(i, side, rs, 0.5, 0., seed=i, arrival=t) for i, (side, rs, t) in enumerate(specs)]
+
+
+def test_scheduler_admits_in_arrival_order_within_capacity():
+    pools = {4: FakePool(4, cap=300), 6: FakePool(6, cap=300)}
+    srv = serving.Server(pools=pools, tol=1e-3)
+    reqs = _reqs([(10, 4, 0.), (10, 4, 0.), (10, 4, 0.), (10, 4, 0.), (12, 6, 0.)])
+    st = srv.run(reqs, sleep=lambda s: None)
+    res = {r.rid: r for r in st.results}
+    assert all(res[i].status == "converged" for i in range(5))
+    # three 10x10 solves fit in 300 elements; the fourth waits for a retirement
+    assert pools[4].admitted[:3] == [0, 1, 2] and pools[4].admitted[3] == 3
+    assert res[3].admitted > 0 or res[3].updates == res[0].updates
+    # every solve needs 3*side batches after its first (the normalizing one) to reach 1e-3 here,
+    # whatever else shares the pool
+    for r in st.results:
+        assert r.updates == (reqs[r.rid].side * 3 + 1) * pools[reqs[r.rid].row_size].k
+
+
+def test_scheduler_rejects_cancels_and_retires_diverged():
+    pools = {4: FakePool(4, cap=200, fail={2})}
+    srv = serving.Server(pools=pools, tol=1e-3, max_live=1)
+    reqs = _reqs([(8, 4, 0.), (20, 4, 0.), (8, 4, 0.), (8, 6, 0.), (8, 4, 0.)])
+    srv.cancel(4)
+    st = srv.run(reqs, sleep=lambda s: None)
+    status = {r.rid: r.status for r in st.results}
+    assert status == {0: "converged", 1: "rejected", 2: "diverged", 3: "rejected", 4: "cancelled"}
+    assert (2, True) in pools[4].retired and (0, False) in pools[4].retired
+    summ = st.summary()
+    assert summ["solves"] == 2 and summ["rejected"] == 2 and summ["cancelled"] == 1
+
+
+def test_scheduler_max_updates():
+    pools = {4: FakePool(4, cap=500)}
+    srv = serving.Server(pools=pools, tol=1e-30, max_updates=50)
+    st = srv.run(_reqs([(5, 4, 0.)]), sleep=lambda s: None)
+    assert st.results[0].status == "max_updates" and st.results[0].updates == 50
