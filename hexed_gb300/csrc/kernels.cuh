@@ -384,11 +384,126 @@ struct STab {
   }
 };
 
+// ------------------------------------------------------------------- row tasks
+// The tensor-product line contractions of Derivative (include/Derivative.hpp:50-60) run as
+// row tasks: one thread per (element, variable, row along a dimension). A task loads the RS
+// values of its row from shared memory once, forms both boundary products B.x from them and
+// writes all RS outputs of the row. The 1-D operators are kernel parameters indexed only by
+// compile-time constants, so each entry is a constant operand of its FMA. Per output this is
+// one shared-memory load and one store, where a thread per point loads the whole row and the
+// operator row for every output.
+template <int RS, typename R>
+struct RowTab {
+  R diff[RS*RS];     // diff[i*RS + j] = L_j'(x_i)
+  R bound[2*RS];     // bound[s*RS + j] = L_j(s)
+  R lift[2*RS];      // lift[i*2 + s] (include/Derivative.hpp:22-28)
+  R filter[RS*RS];
+};
+
+template <int RS, typename R>
+inline RowTab<RS, R> make_rowtab(const Tab<RS>& t)
+{
+  RowTab<RS, R> r;
+  for (int i = 0; i < RS*RS; ++i) { r.diff[i] = R(t.diff[i]); r.filter[i] = R(t.filter[i]); }
+  for (int i = 0; i < 2*RS; ++i) { r.bound[i] = R(t.bound[i]); r.lift[i] = R(t.lift[i]); }
+  return r;
+}
+
+// Element-local index of the first point of row r (0 <= r < nfq) along dimension D.
+template <int ND, int RS, int D>
+__device__ __forceinline__ int row_base(int r)
+{
+  constexpr int stride = Shape<ND, RS>::stride(D);
+  return (r/stride)*stride*RS + r%stride;
+}
+
+template <int RS, int STRIDE, typename R>
+__device__ __forceinline__ void load_row(const R* p, R (&x)[RS])
+{
+  #pragma unroll
+  for (int k = 0; k < RS; ++k) x[k] = p[k*STRIDE];
+}
+
+// a0 = B_0.x, a1 = B_1.x (the row extrapolated to its two faces)
+template <int RS, typename R>
+__device__ __forceinline__ void bound_dot(const RowTab<RS, R>& t, const R (&x)[RS], R& a0, R& a1)
+{
+  a0 = 0;
+  a1 = 0;
+  #pragma unroll
+  for (int k = 0; k < RS; ++k) { a0 += t.bound[k]*x[k]; a1 += t.bound[RS + k]*x[k]; }
+}
+
+// (D.x)_i + lift_i.(b0, b1): Derivative::operator() at node i, with b_s the face value minus
+// the extrapolated row (include/Derivative.hpp:56-60)
+template <int RS, typename R>
+__device__ __forceinline__ R row_deriv(const RowTab<RS, R>& t, const R (&x)[RS], int i, R b0, R b1)
+{
+  R acc = 0;
+  #pragma unroll
+  for (int k = 0; k < RS; ++k) acc += t.diff[i*RS + k]*x[k];
+  R l = 0;
+  l += t.lift[i*2]*b0;
+  l += t.lift[i*2 + 1]*b1;
+  return acc + l;
+}
+
+// Calls f(std::integral_constant<int, I>()) for I = 0 .. N-1 in order.
+template <int N, int I = 0, typename F>
+__device__ __forceinline__ void static_for(F&& f)
+{
+  if constexpr (I < N) {
+    f(std::integral_constant<int, I>());
+    static_for<N, I + 1>(f);
+  }
+}
+
+// Calls f(std::integral_constant<int, d>) for a runtime dimension d, so that a task loop
+// balanced over all dimensions still sees compile-time strides.
+template <int ND, typename F>
+__device__ __forceinline__ void dim_switch(int d, F&& f)
+{
+  if (d == 0) f(std::integral_constant<int, 0>());
+  else if constexpr (ND == 3) {
+    if (d == 1) f(std::integral_constant<int, 1>());
+    else f(std::integral_constant<int, 2>());
+  } else f(std::integral_constant<int, ND - 1>());
+}
+
 // ------------------------------------------------------------------- Write_face helper
 // Extrapolate an element's state (shared memory, [nv][nq]) to its 2nd face slots
 // (Spatial::Write_face, include/Spatial.hpp:41-57). Called by all threads of the CTA.
 template <int ND, int RS, typename R, typename FaceT, int EPB = Shape<ND, RS>::epb>
-__device__ __forceinline__ void write_faces_from_smem(const Dev<FaceT>& m, const STab<RS, R>& st,
+__device__ __forceinline__ void write_faces_from_smem(const Dev<FaceT>& m, const RowTab<RS, R>& rt, const R* s_u,
+                                                      int e0, int e_end)
+{
+  using S = Shape<ND, RS>;
+  constexpr int nq = S::nq, nfq = S::nfq, nv = S::nv;
+  constexpr int per_d = EPB*nv*nfq;
+  for (int t = threadIdx.x; t < ND*per_d; t += blockDim.x) {
+    const int d = t/per_d, rem = t - d*per_d;
+    const int r = rem%nfq, rest = rem/nfq;
+    const int v = rest%nv, le = rest/nv;
+    const int e = e0 + le;
+    if (e >= e_end) continue;
+    dim_switch<ND>(d, [&](auto dc) {
+      constexpr int D = decltype(dc)::value;
+      R x[RS];
+      load_row<RS, S::stride(D)>(s_u + (le*nv + v)*nq + row_base<ND, RS, D>(r), x);
+      R a0, a1;
+      bound_dot(rt, x, a0, a1);
+      FaceT* f0 = m.face + (size_t)(e*2*ND + 2*D)*S::slot_dof + v*nfq + r;
+      f0[0] = FaceT(a0);
+      f0[S::slot_dof] = FaceT(a1);   // slot of face 2d + 1
+    });
+  }
+}
+
+// Write_face of the per-point body: the same extrapolation with the boundary rows read from
+// the CTA's shared table and runtime row strides (fewer registers than the compile-time-stride
+// row tasks, which the FP64 kernels' occupancy needs).
+template <int ND, int RS, typename R, typename FaceT, int EPB = Shape<ND, RS>::epb>
+__device__ __forceinline__ void write_faces_points(const Dev<FaceT>& m, const STab<RS, R>& st,
                                                       const R* s_u, int e0, int e_end)
 {
   using S = Shape<ND, RS>;
@@ -459,7 +574,7 @@ constexpr unsigned bulk_wait_polls = 1u << 20;
 constexpr int flag_bulk_wait = 1;
 
 template <int ND, int RS, typename R, bool DEF, bool VISC, int EPB = Shape<ND, RS>::epb>
-struct LocalSmem {
+struct LocalSmemPoints {
   using S = Shape<ND, RS>;
   static constexpr int per_elem = S::nv*S::nq            // s_u
                                 + ND*S::nv*S::nq         // s_f
@@ -470,6 +585,23 @@ struct LocalSmem {
   static constexpr size_t state_bytes = sizeof(double)*(size_t)EPB*(S::nv + 3)*S::nq;
   static constexpr size_t work_offset = tab_bytes + 16 + (state_bytes + 15)/16*16;
   static constexpr size_t bytes = work_offset + sizeof(R)*(size_t)per_elem*EPB + 16;
+};
+
+template <int ND, int RS, typename R, bool DEF, bool VISC, int EPB = Shape<ND, RS>::epb>
+struct LocalSmemRows {
+  using S = Shape<ND, RS>;
+  // work fields per element, in R:
+  //   s_u  [nv][nq]     offset state (Cartesian gradient, Write_face); the convective residual
+  //   s_x  [ND][nv][nq] metric-weighted offset state of the deformed gradient; then the fluxes
+  //   s_g  [ND][nv][nq] gradient; then the viscous fluxes (viscous path)
+  //   s_vr [nv][nq]     viscous residual (viscous path)
+  static constexpr int per_elem = S::nv*S::nq + ND*S::nv*S::nq + (VISC ? (ND + 1)*S::nv*S::nq : 0);
+  // [mbarrier, 16 B][1/element size, EPB x R][element states, EPB x (nv + 3) x nq doubles][work]
+  static constexpr size_t idp_offset = 16;
+  static constexpr size_t state_offset = idp_offset + (sizeof(R)*EPB + 15)/16*16;
+  static constexpr size_t state_bytes = sizeof(double)*(size_t)EPB*(S::nv + 3)*S::nq;
+  static constexpr size_t work_offset = state_offset + (state_bytes + 15)/16*16;
+  static constexpr size_t bytes = work_offset + sizeof(R)*(size_t)per_elem*EPB;
 };
 
 // Max_dt of one quadrature point (include/Spatial.hpp:793-826): the local time step from the
@@ -533,8 +665,12 @@ __device__ __forceinline__ R offset_var(const Dev<FaceT>& m, int e, int v, doubl
   else return to_R<R>(x - m.ref[(size_t)e*(ND + 2) + v]);
 }
 
+// Spatial::Local (include/Spatial.hpp:326-509) with one thread per quadrature point for the
+// point work and the contractions alike: each thread forms its own point's D.f + lift.(fb - B.f)
+// from its row in shared memory, after per-row boundary corrections fb - B.f have been formed
+// once per row.
 template <int ND, int RS, typename R, bool DEF, bool VISC, typename FaceT, int EPB>
-__device__ __forceinline__ void local_body(Dev<FaceT> m, const Tab<RS>& tab, int e_begin, int e_end, int stage,
+__device__ __forceinline__ void local_body_points(Dev<FaceT> m, const Tab<RS>& tab, int e_begin, int e_end, int stage,
                                            int compute_residual, int use_filter, const TmT<R>& visc,
                                            const TmT<R>& cond, const LocalDt& ldt)
 {
@@ -545,7 +681,7 @@ __device__ __forceinline__ void local_body(Dev<FaceT> m, const Tab<RS>& tab, int
   // metric identity sum_d [D.n_d + lift.(n_face - B.n_d)] = 0 (free-stream preservation), so
   // this is the same scheme up to roundoff, without differences of nearly equal floats.
   constexpr bool split = !std::is_same<FaceT, double>::value;
-  using L = LocalSmem<ND, RS, R, DEF, VISC, EPB>;
+  using L = LocalSmemPoints<ND, RS, R, DEF, VISC, EPB>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   STab<RS, R>& st = *reinterpret_cast<STab<RS, R>*>(smem_raw);
   unsigned long long* s_bar = reinterpret_cast<unsigned long long*>(smem_raw + L::tab_bytes);
@@ -921,34 +1057,402 @@ __device__ __forceinline__ void local_body(Dev<FaceT> m, const Tab<RS>& tab, int
       for (int v = 0; v < nv; ++v) my_u[v*nq + q] = up[v];
     }
     __syncthreads();
-    write_faces_from_smem<ND, RS, R, FaceT, EPB>(m, st, s_u, e0, e_end);
+    write_faces_points<ND, RS, R, FaceT, EPB>(m, st, s_u, e0, e_end);
   }
   // a bulk copy whose wait gave up must still land before the CTA's shared memory is released
   if (bulk && !staged) mbar_wait(s_bar, 0, bulk_wait_polls);
 }
 
-// Spatial::Local (include/Spatial.hpp:293-510), one thread per quadrature point, EPB
-// elements per CTA (see local_body).
-template <int ND, int RS, typename R, bool DEF, bool VISC, typename FaceT, int EPB = Shape<ND, RS>::epb>
-__global__ void __launch_bounds__(Tile<ND, RS, EPB>::threads)
-k_local(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int compute_residual, int use_filter,
-        TmT<R> visc, TmT<R> cond, LocalDt ldt)
+// Spatial::Local (include/Spatial.hpp:326-509). Point work (state, fluxes, stage update) runs
+// one thread per quadrature point; the line contractions run as row tasks over the CTA's
+// shared-memory fields. The arithmetic of every output is that of Derivative, in its order.
+template <int ND, int RS, typename R, bool DEF, bool VISC, typename FaceT, int EPB>
+__device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab, const RowTab<RS, R>& rt,
+                                                int e_begin, int e_end, int stage, int compute_residual, int use_filter,
+                                                const TmT<R>& visc, const TmT<R>& cond, const LocalDt& ldt)
 {
-  local_body<ND, RS, R, DEF, VISC, FaceT, EPB>(m, tab, e_begin, e_end, stage, compute_residual, use_filter, visc, cond,
-                                              ldt);
+  using S = Shape<ND, RS>;
+  constexpr int nq = S::nq, nfq = S::nfq, nv = S::nv;
+  // Mixed form: traces and convective fluxes are offsets from the element's reference state
+  // (flux_delta). The reference flux's parts of interior and face fluxes cancel by the discrete
+  // metric identity sum_d [D.n_d + lift.(n_face - B.n_d)] = 0 (free-stream preservation), so
+  // this is the same scheme up to roundoff, without differences of nearly equal floats.
+  constexpr bool split = !std::is_same<FaceT, double>::value;
+  using L = LocalSmemRows<ND, RS, R, DEF, VISC, EPB>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  unsigned long long* s_bar = reinterpret_cast<unsigned long long*>(smem_raw);
+  R* s_idp = reinterpret_cast<R*>(smem_raw + L::idp_offset);
+  double* s_state = reinterpret_cast<double*>(smem_raw + L::state_offset);
+  R* s_u = reinterpret_cast<R*>(smem_raw + L::work_offset);
+  R* s_x = s_u + EPB*nv*nq;
+  R* s_g = s_x + EPB*ND*nv*nq;
+  R* s_vr = s_g + (VISC ? EPB*ND*nv*nq : 0);
+  const int le = threadIdx.x/nq;
+  const int q = threadIdx.x%nq;
+  const int e0 = e_begin + blockIdx.x*EPB;
+  const int e = e0 + le;
+  const bool active = threadIdx.x < EPB*nq && e < e_end;
+  // The CTA's element states ([n][nv + 3][nq], contiguous) arrive in shared memory by one bulk
+  // copy; where the range is not 16-byte aligned, threads read global memory directly (same
+  // values).
+  const double* g_state = m.elem + (size_t)e0*(nv + 3)*nq;
+  const unsigned state_bytes = unsigned(min(EPB, e_end - e0)*(nv + 3)*nq*sizeof(double));
+  const bool bulk = ((reinterpret_cast<unsigned long long>(g_state) | state_bytes) & 15u) == 0;
+  if (bulk && threadIdx.x == 0) mbar_init(s_bar, 1);
+  if (threadIdx.x < EPB) {
+    const int ee = e0 + threadIdx.x;
+    const double dp = ee < e_end ? m.nom_size[ee] : 1.;
+    s_idp[threadIdx.x] = split ? R(1)/to_R<R>(dp) : R(1./dp);
+  }
+  __syncthreads();
+  if (bulk && threadIdx.x == 0) bulk_load(s_state, g_state, state_bytes, s_bar);
+  const int ed = e - m.n_car;
+  const double d_pos = active ? m.nom_size[e] : 1.;
+  const double inv_dpos = 1./d_pos;
+  const R inv_dpos_r = split ? R(1)/to_R<R>(d_pos) : R(inv_dpos);
+  const bool staged = bulk && mbar_wait(s_bar, 0, bulk_wait_polls);
+  if (bulk && !staged) atomicOr(m.status + 1, flag_bulk_wait);
+  const double* state_g = (staged ? s_state : g_state) + (size_t)le*(nv + 3)*nq;
+
+  R u[nv + 2];   // state + bulk AV + Laplacian AV (include/pde.hpp:79-84)
+  R up[nv];      // offset form of the state
+  const double* ref_e = split ? m.ref + (size_t)(active ? e : 0)*nv : nullptr;
+  R nrm[ND][ND]; // nrm[j][i] = comp.normal(j, i)
+  #pragma unroll
+  for (int i = 0; i < ND; ++i)
+    #pragma unroll
+    for (int j = 0; j < ND; ++j) nrm[j][i] = (i == j) ? R(1) : R(0);
+  if (active) {
+    #pragma unroll
+    for (int v = 0; v < nv; ++v) {
+      const double x = state_g[v*nq + q];
+      up[v] = offset_var<ND, R>(m, e, v, x);
+      if constexpr (split) u[v] = to_R<R>(ref_e[v]) + up[v];
+      else u[v] = R(x);
+    }
+    u[nv] = to_R<R>(state_g[(nv + 1)*nq + q]);
+    u[nv + 1] = to_R<R>(state_g[(nv + 2)*nq + q]);
+    if constexpr (DEF) {
+      const FaceT* nr = m.nrm + (size_t)ed*(ND*ND + 1)*nq;
+      #pragma unroll
+      for (int i = 0; i < ND; ++i)
+        #pragma unroll
+        for (int j = 0; j < ND; ++j) nrm[j][i] = R(nr[(i*ND + j)*nq + q]);
+    }
+  } else {
+    #pragma unroll
+    for (int v = 0; v < nv + 2; ++v) u[v] = R(1);
+    #pragma unroll
+    for (int v = 0; v < nv; ++v) up[v] = R(0);
+  }
+
+  R grad[nv][ND];
+  if constexpr (VISC) {
+    // ---- gradient times Jacobian determinant (Spatial.hpp:371-402)
+    if constexpr (!DEF) {
+      if (active) {
+        #pragma unroll
+        for (int v = 0; v < nv; ++v) s_u[(le*nv + v)*nq + q] = up[v];
+      }
+      __syncthreads();
+      // grad[v][d] along each row: D.u + lift.(face LDG state - B.u), over 1/size
+      constexpr int per_d = EPB*nv*nfq;
+      for (int t = threadIdx.x; t < ND*per_d; t += blockDim.x) {
+        const int d = t/per_d, rem = t - d*per_d;
+        const int r = rem%nfq, rest = rem/nfq;
+        const int v = rest%nv, l = rest/nv;
+        const int ee = e0 + l;
+        if (ee >= e_end) continue;
+        dim_switch<ND>(d, [&](auto dc) {
+          constexpr int D = decltype(dc)::value;
+          constexpr int stride = S::stride(D);
+          const int base = row_base<ND, RS, D>(r);
+          R x[RS];
+          load_row<RS, stride>(s_u + (l*nv + v)*nq + base, x);
+          R a0, a1;
+          bound_dot(rt, x, a0, a1);
+          const FaceT* fl = m.face + (size_t)(ee*2*ND + 2*D)*S::slot_dof + nv*nfq + v*nfq + r;
+          const R b0 = R(fl[0]) - a0, b1 = R(fl[S::slot_dof]) - a1;
+          const R idp = s_idp[l];
+          R* g = s_g + ((l*ND + D)*nv + v)*nq + base;
+          #pragma unroll
+          for (int i = 0; i < RS; ++i) g[i*stride] = row_deriv(rt, x, i, b0, b1)*idp;
+        });
+      }
+    } else {
+      // grad[v][j] = sum_d [D_d.(n_dj u) + lift_d.(n_face u_face - B_d.(n_dj u))] / size
+      const FaceT* fnr_e = m.face_nrml;
+      static_for<ND>([&](auto dc) {
+        constexpr int d = decltype(dc)::value;
+        if constexpr (d > 0) __syncthreads();   // the previous dimension's tasks have read s_x
+        if (active) {
+          #pragma unroll
+          for (int j = 0; j < ND; ++j)
+            #pragma unroll
+            for (int v = 0; v < nv; ++v) s_x[((le*ND + j)*nv + v)*nq + q] = nrm[j][d]*up[v];
+        }
+        __syncthreads();
+        constexpr int stride = S::stride(d);
+        constexpr int n_task = EPB*ND*nv*nfq;
+        for (int t = threadIdx.x; t < n_task; t += blockDim.x) {
+          const int r = t%nfq;
+          int rest = t/nfq;
+          const int v = rest%nv; rest /= nv;
+          const int j = rest%ND, l = rest/ND;
+          const int ee = e0 + l;
+          if (ee >= e_end) continue;
+          const int base = row_base<ND, RS, d>(r);
+          R x[RS];
+          load_row<RS, stride>(s_x + ((l*ND + j)*nv + v)*nq + base, x);
+          R a0, a1;
+          bound_dot(rt, x, a0, a1);
+          const FaceT* fl = m.face + (size_t)(ee*2*ND + 2*d)*S::slot_dof + nv*nfq + v*nfq + r;
+          const FaceT* fnr = fnr_e + ((size_t)(ee - m.n_car)*2*ND + 2*d)*ND*nfq + j*nfq + r;
+          const R b0 = R(fnr[0])*R(fl[0]) - a0;
+          const R b1 = R(fnr[ND*nfq])*R(fl[S::slot_dof]) - a1;
+          const R idp = s_idp[l];
+          R* g = s_g + ((l*ND + j)*nv + v)*nq + base;
+          #pragma unroll
+          for (int i = 0; i < RS; ++i) {
+            const R o = row_deriv(rt, x, i, b0, b1);
+            g[i*stride] = d ? g[i*stride] + o*idp : o*idp;
+          }
+        }
+      });
+    }
+    __syncthreads();
+    if (active) {
+      #pragma unroll
+      for (int v = 0; v < nv; ++v)
+        #pragma unroll
+        for (int j = 0; j < ND; ++j) grad[v][j] = s_g[((le*ND + j)*nv + v)*nq + q];
+    }
+  }
+
+  // ---- fluxes (Spatial.hpp:405-442): s_x [i][v] convective, s_g [i][v] viscous (each point
+  // overwrites only its own gradient entries)
+  if (active) {
+    Conv<ND, R> c(u);
+    RefState<ND, R> rs;   // formed here, not kept live through the gradient part
+    if constexpr (split) rs.set(ref_e);
+    #pragma unroll
+    for (int i = 0; i < ND; ++i) {
+      R col[ND], f[nv];
+      #pragma unroll
+      for (int j = 0; j < ND; ++j) col[j] = nrm[j][i];
+      if constexpr (split) flux_delta<ND, R>(u, up, rs, c, col, f);
+      else c.flux(u, col, f);
+      #pragma unroll
+      for (int v = 0; v < nv; ++v) s_x[((le*ND + i)*nv + v)*nq + q] = f[v];
+    }
+    if constexpr (VISC) {
+      R g[nv][ND];
+      const R inv_det = DEF ? to_R<R>(m.inv_det[(size_t)ed*nq + q]) : R(1);
+      #pragma unroll
+      for (int v = 0; v < nv; ++v)
+        #pragma unroll
+        for (int j = 0; j < ND; ++j) g[v][j] = DEF ? grad[v][j]*inv_det : grad[v][j];
+      DiffScalars<ND, R> df(u, c, u[nv], u[nv + 1], visc, cond);
+      R fd[nv][ND];
+      flux_diff<ND, R, !DEF>(u, c, df, g, nrm, fd);
+      #pragma unroll
+      for (int i = 0; i < ND; ++i)
+        #pragma unroll
+        for (int v = 0; v < nv; ++v) s_g[((le*ND + i)*nv + v)*nq + q] = fd[v][i];
+    }
+  }
+
+  // ---- residual (Spatial.hpp:445-470), one dimension at a time: s_u += -(D.f + lift.(f* - B.f));
+  // viscous: s_vr += -D.g, and B.g to the faces' LDG slots
+  static_for<ND>([&](auto dc) {
+    constexpr int d = decltype(dc)::value;
+    __syncthreads();
+    constexpr int stride = S::stride(d);
+    constexpr int n_task = EPB*nv*nfq;
+    for (int t = threadIdx.x; t < n_task; t += blockDim.x) {
+      const int r = t%nfq, rest = t/nfq;
+      const int v = rest%nv, l = rest/nv;
+      const int ee = e0 + l;
+      if (ee >= e_end) continue;
+      const int base = row_base<ND, RS, d>(r);
+      R x[RS];
+      load_row<RS, stride>(s_x + ((l*ND + d)*nv + v)*nq + base, x);
+      R a0, a1;
+      bound_dot(rt, x, a0, a1);
+      FaceT* fl = m.face + (size_t)(ee*2*ND + 2*d)*S::slot_dof + v*nfq + r;
+      const R b0 = R(fl[0]) - a0, b1 = R(fl[S::slot_dof]) - a1;
+      R* ra = s_u + (l*nv + v)*nq + base;
+      #pragma unroll
+      for (int i = 0; i < RS; ++i) {
+        const R o = row_deriv(rt, x, i, b0, b1);
+        ra[i*stride] = d ? ra[i*stride] + -o : -o;
+      }
+      if constexpr (VISC) {
+        load_row<RS, stride>(s_g + ((l*ND + d)*nv + v)*nq + base, x);
+        bound_dot(rt, x, a0, a1);
+        fl[nv*nfq] = FaceT(a0);
+        fl[S::slot_dof + nv*nfq] = FaceT(a1);
+        R* vr = s_vr + (l*nv + v)*nq + base;
+        #pragma unroll
+        for (int i = 0; i < RS; ++i) {
+          R ag = 0;
+          #pragma unroll
+          for (int k = 0; k < RS; ++k) ag += rt.diff[i*RS + k]*x[k];
+          vr[i*stride] = d ? vr[i*stride] + -ag : -ag;
+        }
+      }
+    }
+  });
+  __syncthreads();
+  R rate[nv], vrate[nv];
+  #pragma unroll
+  for (int v = 0; v < nv; ++v) { rate[v] = 0; vrate[v] = 0; }
+  if (active) {
+    #pragma unroll
+    for (int v = 0; v < nv; ++v) {
+      rate[v] = s_u[(le*nv + v)*nq + q];
+      if constexpr (VISC) vrate[v] = s_vr[(le*nv + v)*nq + q];
+    }
+  }
+
+  // ---- modal filter (Spatial.hpp:473-481), one dimension at a time, rows filtered in place
+  if (use_filter) {
+    constexpr int nf = VISC ? 2*nv : nv;   // rate, then vrate (s_x holds ND*nv >= 2*nv fields)
+    static_for<ND>([&](auto dc) {
+      constexpr int d = decltype(dc)::value;
+      __syncthreads();
+      if (active) {
+        #pragma unroll
+        for (int v = 0; v < nv; ++v) {
+          s_x[(le*nf + v)*nq + q] = rate[v];
+          if constexpr (VISC) s_x[(le*nf + nv + v)*nq + q] = vrate[v];
+        }
+      }
+      __syncthreads();
+      constexpr int stride = S::stride(d);
+      for (int t = threadIdx.x; t < EPB*nf*nfq; t += blockDim.x) {
+        const int r = t%nfq, rest = t/nfq;
+        const int v = rest%nf, l = rest/nf;
+        R* row = s_x + (l*nf + v)*nq + row_base<ND, RS, d>(r);
+        R x[RS];
+        load_row<RS, stride>(row, x);
+        #pragma unroll
+        for (int i = 0; i < RS; ++i) {
+          R acc = 0;
+          #pragma unroll
+          for (int k = 0; k < RS; ++k) acc += rt.filter[i*RS + k]*x[k];
+          row[i*stride] = acc;
+        }
+      }
+      __syncthreads();
+      if (active) {
+        #pragma unroll
+        for (int v = 0; v < nv; ++v) {
+          rate[v] = s_x[(le*nf + v)*nq + q];
+          if constexpr (VISC) vrate[v] = s_x[(le*nf + nv + v)*nq + q];
+        }
+      }
+    });
+  }
+
+  // ---- stage update (Spatial.hpp:484-503): the state accumulates in double
+  if (active) {
+    const double dt = ldt.mode ? ldt.dt : m.scalars[SC_DT];
+    const double update_coef = stage ? dt*tab.step_ratio : dt;
+    double* st_w = m.elem + (size_t)e*(nv + 3)*nq;
+    FaceT* rc = m.rcache + (size_t)e*nv*nq;
+    double tss;
+    if (ldt.mode == 1) {
+      const R inv_cfl_c = R(1./(tab.max_cfl*ldt.msc));
+      const R inv_cfl_d = R(1./(-2/tab.min_eig_diffusion*ldt.msd));
+      const R step = point_step<ND, RS, R, VISC>(m, tab, e, q, inv_cfl_c, inv_cfl_d, visc, cond);
+      if constexpr (split) tss = f64_of(step);
+      else tss = step;
+      st_w[nv*nq + q] = tss;
+    } else {
+      tss = state_g[nv*nq + q];
+    }
+    if constexpr (!split) {
+      double mult = update_coef*tss*inv_dpos;
+      if constexpr (DEF) mult *= m.inv_det[(size_t)ed*nq + q];
+      #pragma unroll
+      for (int v = 0; v < nv; ++v) {
+        double uu = double(rate[v]);
+        if (stage) {
+          uu -= rc[v*nq + q];
+        } else {
+          rc[v*nq + q] = uu;
+          if constexpr (VISC) uu += double(vrate[v]);
+        }
+        uu *= mult;
+        if (compute_residual) rc[v*nq + q] = FaceT(uu);
+        else {
+          double nu = state_g[v*nq + q] + uu;
+          st_w[v*nq + q] = nu;
+          up[v] = offset_var<ND, R>(m, e, v, nu);
+        }
+      }
+    } else {
+      // Mixed form: the increment is formed in float; only its accumulation into the state
+      // is a double add. The offset-form trace of the new state is the old one plus the
+      // increment.
+      R mult = to_R<R>(update_coef)*to_R<R>(tss)*inv_dpos_r;
+      if constexpr (DEF) mult *= to_R<R>(m.inv_det[(size_t)ed*nq + q]);
+      #pragma unroll
+      for (int v = 0; v < nv; ++v) {
+        R ur = rate[v];
+        if (stage) {
+          ur -= R(rc[v*nq + q]);
+        } else {
+          rc[v*nq + q] = FaceT(ur);
+          if constexpr (VISC) ur += vrate[v];
+        }
+        const R inc = ur*mult;
+        if (compute_residual) rc[v*nq + q] = FaceT(inc);
+        else {
+          st_w[v*nq + q] = state_g[v*nq + q] + f64_of(inc);
+          up[v] += inc;
+        }
+      }
+    }
+  }
+  // ---- Write_face of the new state (Spatial.hpp:507); the viscous path defers it
+  if constexpr (!VISC) {
+    __syncthreads();
+    if (active) {
+      #pragma unroll
+      for (int v = 0; v < nv; ++v) s_u[(le*nv + v)*nq + q] = up[v];
+    }
+    __syncthreads();
+    write_faces_from_smem<ND, RS, R, FaceT, EPB>(m, rt, s_u, e0, e_end);
+  }
+  // a bulk copy whose wait gave up must still land before the CTA's shared memory is released
+  if (bulk && !staged) mbar_wait(s_bar, 0, bulk_wait_polls);
 }
 
-// The float viscous volume kernel with its registers capped for four resident CTAs per SM
-// (72 registers, 4 bytes of spill at 3D row size 6): it holds the offset state, its gradient
-// and the reference state at once, and its default allocation leaves two CTAs per SM for a
-// kernel whose stalls are mostly memory and shared-memory latency.
-template <int ND, int RS, typename R, bool DEF, bool VISC, typename FaceT, int EPB = Shape<ND, RS>::epb>
-__global__ void __launch_bounds__(Tile<ND, RS, EPB>::threads, 4)
-k_local_capped(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int stage, int compute_residual, int use_filter,
-             TmT<R> visc, TmT<R> cond, LocalDt ldt)
+// Shared memory of one k_local CTA: the per-point body (FP64) or the row-task body (float).
+template <int ND, int RS, typename R, bool DEF, bool VISC, int EPB = Shape<ND, RS>::epb>
+using LocalSmem = typename std::conditional<std::is_same<R, double>::value, LocalSmemPoints<ND, RS, R, DEF, VISC, EPB>,
+                                            LocalSmemRows<ND, RS, R, DEF, VISC, EPB>>::type;
+
+// Spatial::Local (include/Spatial.hpp:293-510), one thread per quadrature point and EPB
+// elements per CTA. The FP64 form uses the per-point contractions (local_body_points) and the
+// float form the row tasks (local_body_rows): on this GPU the FP64 kernels are bound by the
+// FP64 pipe, which the row tasks do not relieve (they ran 9-14% slower there), while the float
+// kernels are bound by shared-memory instruction issue, which the row tasks cut (1.6x faster
+// for the deformed viscous kernel at row size 6). MINB > 1 caps the registers for MINB
+// resident CTAs per SM.
+template <int ND, int RS, typename R, bool DEF, bool VISC, typename FaceT, int EPB = Shape<ND, RS>::epb, int MINB = 1>
+__global__ void __launch_bounds__(Tile<ND, RS, EPB>::threads, MINB)
+k_local(Dev<FaceT> m, Tab<RS> tab, RowTab<RS, R> rt, int e_begin, int e_end, int stage, int compute_residual,
+        int use_filter, TmT<R> visc, TmT<R> cond, LocalDt ldt)
 {
-  local_body<ND, RS, R, DEF, VISC, FaceT, EPB>(m, tab, e_begin, e_end, stage, compute_residual, use_filter, visc, cond,
-                                              ldt);
+  if constexpr (std::is_same<R, double>::value)
+    local_body_points<ND, RS, R, DEF, VISC, FaceT, EPB>(m, tab, e_begin, e_end, stage, compute_residual, use_filter,
+                                                        visc, cond, ldt);
+  else
+    local_body_rows<ND, RS, R, DEF, VISC, FaceT, EPB>(m, tab, rt, e_begin, e_end, stage, compute_residual, use_filter,
+                                                      visc, cond, ldt);
 }
 
 // ------------------------------------------------------------------- Reconcile_ldg_flux
@@ -961,7 +1465,8 @@ struct ReconcileSmem {
 
 template <int ND, int RS, typename R, bool DEF, typename FaceT>
 __global__ void __launch_bounds__(Shape<ND, RS>::threads)
-k_reconcile_ldg(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int compute_residual, int use_filter)
+k_reconcile_ldg(Dev<FaceT> m, Tab<RS> tab, RowTab<RS, R> rt, int e_begin, int e_end, int compute_residual,
+                int use_filter)
 {
   using S = Shape<ND, RS>;
   constexpr int nq = S::nq, nfq = S::nfq, nv = S::nv, EPB = S::epb;
@@ -1057,7 +1562,7 @@ k_reconcile_ldg(Dev<FaceT> m, Tab<RS> tab, int e_begin, int e_end, int compute_r
     for (int v = 0; v < nv; ++v) my_u[v*nq + q] = offset_var<ND, R>(m, e, v, st_w[v*nq + q]);
   }
   __syncthreads();
-  write_faces_from_smem<ND, RS, R, FaceT>(m, st, s_u, e0, e_end);
+  write_faces_from_smem<ND, RS, R, FaceT>(m, rt, s_u, e0, e_end);
 }
 
 // ------------------------------------------------------------------- Neighbor

@@ -72,30 +72,27 @@ struct Runner
   static constexpr int epb_of(int v) { return v == 1 ? (S::epb > 1 ? S::epb/2 : 1) : v == 2 ? 2*S::epb : S::epb; }
   static constexpr bool has_variants(bool def) { return ND == 2 && !def; }
 
-  template <bool DEF, bool VISC, int EPB, bool CAPPED>
-  static auto pick_local()
-  {
-    if constexpr (CAPPED) return k_local_capped<ND, RS, R, DEF, VISC, FaceT, EPB>;
-    else return k_local<ND, RS, R, DEF, VISC, FaceT, EPB>;
-  }
-
   template <bool DEF, bool VISC, int EPB>
   static void local_shape(Ctx& c, int stage, int cr, int uf, const hexed_transport& visc, const hexed_transport& cond,
                           int e_begin, int e_end, const LocalDt& ldt)
   {
     const int blocks = (e_end - e_begin + EPB - 1)/EPB;
     constexpr size_t smem = LocalSmem<ND, RS, R, DEF, VISC, EPB>::bytes;
-    // the float viscous 3D kernel is the register-capped variant
-    constexpr bool capped = std::is_same<R, float>::value && VISC && ND == 3;
-    auto kern = pick_local<DEF, VISC, EPB, capped>();
+    // 3D kernels of row size >= 6 are register-capped for more resident CTAs: 72 registers
+    // per thread in float (4 CTAs per SM at row size 6), 128 for the FP64 viscous kernel (2)
+    constexpr int threads = Tile<ND, RS, EPB>::threads;
+    constexpr int cap = std::is_same<R, float>::value ? 72 : VISC ? 128 : 0;
+    constexpr int minb = (cap && ND == 3 && S::nq > 128 && 65536/(threads*cap) > 1) ? 65536/(threads*cap) : 1;
+    auto kern = k_local<ND, RS, R, DEF, VISC, FaceT, EPB, minb>;
     static bool configured = false;
     if (!configured) {
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       configured = true;
     }
     ProfScope ps(c, DEF ? (VISC ? "local_def_ns" : "local_def_euler") : (VISC ? "local_car_ns" : "local_car_euler"));
-    kern<<<blocks, Tile<ND, RS, EPB>::threads, smem, c.stream>>>(dev(c), tab(c), e_begin, e_end, stage, cr, uf,
-                                                                 make_tm<R>(visc), make_tm<R>(cond), ldt);
+    const Tab<RS> t = tab(c);
+    kern<<<blocks, threads, smem, c.stream>>>(dev(c), t, make_rowtab<RS, R>(t), e_begin, e_end, stage, cr, uf,
+                                              make_tm<R>(visc), make_tm<R>(cond), ldt);
   }
 
   template <bool DEF, bool VISC>
@@ -177,7 +174,8 @@ struct Runner
       configured = true;
     }
     ProfScope ps(c, DEF ? "reconcile_ldg_def" : "reconcile_ldg_car");
-    kern<<<blocks, S::threads, smem, c.stream>>>(dev(c), tab(c), e_begin, e_end, cr, uf);
+    const Tab<RS> t = tab(c);
+    kern<<<blocks, S::threads, smem, c.stream>>>(dev(c), t, make_rowtab<RS, R>(t), e_begin, e_end, cr, uf);
   }
 
   template <bool VISC>
