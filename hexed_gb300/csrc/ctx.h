@@ -101,6 +101,11 @@ struct Ctx {
   int face_threads;
 };
 
+// Max_dt's CFL reciprocals for convective and diffusive safety factors (include/Spatial.hpp:
+// 776-777): uniform over a launch, so formed once on the host
+inline double inv_cfl_conv(const Ctx& c, double msc) { return 1./(c.tables.max_cfl*msc); }
+inline double inv_cfl_diff(const Ctx& c, double msd) { return 1./(-2/c.tables.min_eig_diffusion*msd); }
+
 // Bracket one launch with timing events when profiling is enabled.
 struct ProfScope {
   Ctx& c; int pair;

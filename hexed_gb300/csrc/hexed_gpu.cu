@@ -737,8 +737,9 @@ int enqueue_update(hexed_gpu_ctx* c, const hexed_update_params* p, double* host_
       const double cheby = chebyshev_step(p->n_cheby_flow, i_cheby);
       if (fuse_dt) {
         const double dt = std::fmin(1., p->max_time_step)*cheby;
-        c->ops->compute_euler(*c, 0, 0, p->use_filter, true, hx::LocalDt{1, msc, msd, dt});
-        c->ops->compute_euler(*c, 1, 0, p->use_filter, true, hx::LocalDt{2, msc, msd, dt});
+        const double icc = hx::inv_cfl_conv(*c, msc), icd = hx::inv_cfl_diff(*c, msd);
+        c->ops->compute_euler(*c, 0, 0, p->use_filter, true, hx::LocalDt{1, icc, icd, dt});
+        c->ops->compute_euler(*c, 1, 0, p->use_filter, true, hx::LocalDt{2, icc, icd, dt});
         if (host_dt) *host_dt = dt;
         continue;
       }

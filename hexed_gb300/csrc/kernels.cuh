@@ -569,6 +569,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned phas
   return false;
 }
 constexpr unsigned bulk_wait_polls = 1u << 20;
+
 // status[1] bits (read by hexed_gpu_device_flags): a bulk-copy wait gave up and the kernel
 // read global memory instead
 constexpr int flag_bulk_wait = 1;
@@ -605,10 +606,12 @@ struct LocalSmemRows {
 };
 
 // Max_dt of one quadrature point (include/Spatial.hpp:793-826): the local time step from the
-// vertex time-step scales interpolated to the point, the characteristic speed and, for
-// diffusion, the diffusivity. Shared by k_max_dt and the fused local-time path of k_local.
+// vertex time-step scales interpolated to the point at reference coordinates `coord`, the
+// characteristic speed and, for diffusion, the diffusivity. inv_cfl_c = 1/(max_cfl*conv
+// safety) and inv_cfl_d = 1/(-2/min_eig_diffusion*diff safety) come from the host. Shared by
+// k_max_dt and the fused local-time path of k_local.
 template <int ND, int RS, typename R, bool VISC, typename FaceT>
-__device__ __forceinline__ R point_step(const Dev<FaceT>& m, const Tab<RS>& tab, int e, int q, R inv_cfl_c,
+__device__ __forceinline__ R point_step(const Dev<FaceT>& m, int e, int q, const R (&coord)[ND], R inv_cfl_c,
                                         R inv_cfl_d, const TmT<R>& visc, const TmT<R>& cond)
 {
   using S = Shape<ND, RS>;
@@ -620,10 +623,9 @@ __device__ __forceinline__ R point_step(const Dev<FaceT>& m, const Tab<RS>& tab,
   int stride = nvert;
   #pragma unroll
   for (int d = 0; d < ND; ++d) {
-    const R coord = to_R<R>(tab.node[(q/ipow(RS, ND - 1 - d))%RS]);
     stride /= 2;
     #pragma unroll
-    for (int i = 0; i < (nvert >> (d + 1)); ++i) vals[i] += coord*(vals[i + stride] - vals[i]);
+    for (int i = 0; i < (nvert >> (d + 1)); ++i) vals[i] += coord[d]*(vals[i + stride] - vals[i]);
   }
   const R spacing = vals[0];
   R s[nv];
@@ -641,6 +643,14 @@ __device__ __forceinline__ R point_step(const Dev<FaceT>& m, const Tab<RS>& tab,
   return R(1)/scale;
 }
 
+// Reference coordinates of point q from a node table (RS entries in R)
+template <int ND, int RS, typename R, typename NodeT>
+__device__ __forceinline__ void point_coords(const NodeT* node, int q, R (&coord)[ND])
+{
+  #pragma unroll
+  for (int d = 0; d < ND; ++d) coord[d] = to_R<R>(node[(q/ipow(RS, ND - 1 - d))%RS]);
+}
+
 // Time step of a k_local launch. mode 0: the step is scalars[SC_DT] and the time-step scale
 // row of the state holds each point's scale (written by k_max_dt). mode 1 (first stage of an
 // update with local time stepping): the step is `dt` and the kernel computes each point's
@@ -648,7 +658,8 @@ __device__ __forceinline__ R point_step(const Dev<FaceT>& m, const Tab<RS>& tab,
 // scale row is read.
 struct LocalDt {
   int mode;
-  double msc, msd, dt;
+  double inv_cfl_c, inv_cfl_d;   // mode 1: point_step's safety-scaled CFL reciprocals
+  double dt;
 };
 
 // Threads of a volume-kernel CTA holding EPB elements (whole warps).
@@ -996,9 +1007,10 @@ __device__ __forceinline__ void local_body_points(Dev<FaceT> m, const Tab<RS>& t
     FaceT* rc = m.rcache + (size_t)e*nv*nq;
     double tss;
     if (ldt.mode == 1) {
-      const R inv_cfl_c = R(1./(tab.max_cfl*ldt.msc));
-      const R inv_cfl_d = R(1./(-2/tab.min_eig_diffusion*ldt.msd));
-      const R step = point_step<ND, RS, R, VISC>(m, tab, e, q, inv_cfl_c, inv_cfl_d, visc, cond);
+      R coord[ND];
+      point_coords<ND, RS>(tab.node, q, coord);
+      const R step = point_step<ND, RS, R, VISC>(m, e, q, coord, to_R<R>(ldt.inv_cfl_c), to_R<R>(ldt.inv_cfl_d),
+                                                 visc, cond);
       if constexpr (split) tss = f64_of(step);
       else tss = step;
       st_w[nv*nq + q] = tss;
@@ -1363,9 +1375,10 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
     FaceT* rc = m.rcache + (size_t)e*nv*nq;
     double tss;
     if (ldt.mode == 1) {
-      const R inv_cfl_c = R(1./(tab.max_cfl*ldt.msc));
-      const R inv_cfl_d = R(1./(-2/tab.min_eig_diffusion*ldt.msd));
-      const R step = point_step<ND, RS, R, VISC>(m, tab, e, q, inv_cfl_c, inv_cfl_d, visc, cond);
+      R coord[ND];
+      point_coords<ND, RS>(tab.node, q, coord);
+      const R step = point_step<ND, RS, R, VISC>(m, e, q, coord, to_R<R>(ldt.inv_cfl_c), to_R<R>(ldt.inv_cfl_d),
+                                                 visc, cond);
       if constexpr (split) tss = f64_of(step);
       else tss = step;
       st_w[nv*nq + q] = tss;
@@ -2228,28 +2241,31 @@ __global__ void k_write_face(Dev<FaceT> m, Tab<RS> tab, int e_begin, int n_elem)
 // step is a CFL limit with a safety factor and needs no more than float accuracy.
 template <int ND, int RS, typename R, bool VISC, typename FaceT>
 __global__ void __launch_bounds__(256)
-k_max_dt(Dev<FaceT> m, Tab<RS> tab, double msc, double msd, int local_time, TmT<R> visc,
-         TmT<R> cond, double* partials)
+k_max_dt(Dev<FaceT> m, Tab<RS> tab, R inv_cfl_c, R inv_cfl_d, int local_time, TmT<R> visc, TmT<R> cond,
+         double* partials)
 {
   using S = Shape<ND, RS>;
   constexpr int nq = S::nq, nv = S::nv;
-  const R inv_cfl_c = R(1./(tab.max_cfl*msc));
-  const R inv_cfl_d = R(1./(-2/tab.min_eig_diffusion*msd));
+  __shared__ R s_node[RS];
+  if (threadIdx.x < RS) s_node[threadIdx.x] = to_R<R>(tab.node[threadIdx.x]);
+  __syncthreads();
   double dt = 1.7976931348623157e308;
   R dt_r = R(3.4e38);   // running minimum in the compute type (float form)
   const long total = (long)m.n_elem*nq;
   for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
     const int e = int(t/nq), q = int(t%nq);
     double* state = m.elem + (size_t)e*(nv + 3)*nq;
+    R coord[ND];
+    point_coords<ND, RS>(s_node, q, coord);
     if constexpr (std::is_same<R, double>::value) {
-      const double step = point_step<ND, RS, R, VISC>(m, tab, e, q, inv_cfl_c, inv_cfl_d, visc, cond);
+      const double step = point_step<ND, RS, R, VISC>(m, e, q, coord, inv_cfl_c, inv_cfl_d, visc, cond);
       if (local_time) state[nv*nq + q] = step;
       else {
         state[nv*nq + q] = 1.;
         dt = fmin(dt, step);
       }
     } else {
-      const R step = point_step<ND, RS, R, VISC>(m, tab, e, q, inv_cfl_c, inv_cfl_d, visc, cond);
+      const R step = point_step<ND, RS, R, VISC>(m, e, q, coord, inv_cfl_c, inv_cfl_d, visc, cond);
       if (local_time) state[nv*nq + q] = f64_of(step);
       else {
         state[nv*nq + q] = 1.;

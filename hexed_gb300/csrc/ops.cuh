@@ -284,8 +284,9 @@ struct Runner
     const int grid = grid_for(total, 256, c.max_partials);
     {
       ProfScope ps(c, "max_dt");
-      if (viscous) k_max_dt<ND, RS, R, true, FaceT><<<grid, 256, 0, c.stream>>>(dev(c), tab(c), msc, msd, local_time, make_tm<R>(visc), make_tm<R>(cond), c.partials);
-      else k_max_dt<ND, RS, R, false, FaceT><<<grid, 256, 0, c.stream>>>(dev(c), tab(c), msc, msd, local_time, make_tm<R>(visc), make_tm<R>(cond), c.partials);
+      const R icc = R(inv_cfl_conv(c, msc)), icd = R(inv_cfl_diff(c, msd));
+      if (viscous) k_max_dt<ND, RS, R, true, FaceT><<<grid, 256, 0, c.stream>>>(dev(c), tab(c), icc, icd, local_time, make_tm<R>(visc), make_tm<R>(cond), c.partials);
+      else k_max_dt<ND, RS, R, false, FaceT><<<grid, 256, 0, c.stream>>>(dev(c), tab(c), icc, icd, local_time, make_tm<R>(visc), make_tm<R>(cond), c.partials);
     }
     ProfScope ps(c, "finalize_dt");
     k_finalize_dt<<<1, 256, 0, c.stream>>>(c.scalars, c.partials, grid, local_time, max_time_step, cheby);
