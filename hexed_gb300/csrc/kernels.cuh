@@ -570,6 +570,32 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned phas
 }
 constexpr unsigned bulk_wait_polls = 1u << 20;
 
+// Bulk prefetch of [p, p + bytes) from HBM into L2 (no data returned to the SM); skipped unless
+// the range starts on 16 bytes and its length is a multiple of 16, as the bulk copy requires.
+__device__ __forceinline__ void prefetch_l2(const void* p, size_t bytes)
+{
+  if (((reinterpret_cast<unsigned long long>(p) | bytes) & 15u) || bytes == 0) return;
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(p), "r"((unsigned)bytes) : "memory");
+}
+
+// The per-element arrays a volume-kernel CTA reads after its state, prefetched into L2 at its
+// start so that the later per-point and per-row loads hit L2 rather than HBM: the element face
+// slots, the residual cache (read by the second stage) and, for deformed elements, the metric
+// normals, the determinant reciprocals and (viscous) the face normals.
+template <int ND, int RS, bool DEF, bool VISC, typename FaceT>
+__device__ __forceinline__ void prefetch_element_arrays(const Dev<FaceT>& m, int e0, int n_here, int stage)
+{
+  using S = Shape<ND, RS>;
+  constexpr int nq = S::nq, nfq = S::nfq, nv = S::nv;
+  prefetch_l2(m.face + (size_t)e0*2*ND*S::slot_dof, sizeof(FaceT)*(size_t)n_here*2*ND*S::slot_dof);
+  if (stage) prefetch_l2(m.rcache + (size_t)e0*nv*nq, sizeof(FaceT)*(size_t)n_here*nv*nq);
+  if constexpr (DEF) {
+    const size_t ed0 = (size_t)(e0 - m.n_car);
+    prefetch_l2(m.nrm + ed0*(ND*ND + 1)*nq, sizeof(FaceT)*(size_t)n_here*(ND*ND + 1)*nq);
+    prefetch_l2(m.inv_det + ed0*nq, sizeof(double)*(size_t)n_here*nq);
+    if constexpr (VISC) prefetch_l2(m.face_nrml + ed0*2*ND*ND*nfq, sizeof(FaceT)*(size_t)n_here*2*ND*ND*nfq);
+  }
+}
 // status[1] bits (read by hexed_gpu_device_flags): a bulk-copy wait gave up and the kernel
 // read global memory instead
 constexpr int flag_bulk_wait = 1;
@@ -715,6 +741,7 @@ __device__ __forceinline__ void local_body_points(Dev<FaceT> m, const Tab<RS>& t
   if (bulk && threadIdx.x == 0) mbar_init(s_bar, 1);
   __syncthreads();
   if (bulk && threadIdx.x == 0) bulk_load(s_state, g_state, state_bytes, s_bar);
+  if (threadIdx.x == 32) prefetch_element_arrays<ND, RS, DEF, VISC>(m, e0, min(EPB, e_end - e0), stage);
   st.load(tab);
   const int ed = e - m.n_car;
   const double d_pos = active ? m.nom_size[e] : 1.;
@@ -1118,6 +1145,7 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
   }
   __syncthreads();
   if (bulk && threadIdx.x == 0) bulk_load(s_state, g_state, state_bytes, s_bar);
+  if (threadIdx.x == 32) prefetch_element_arrays<ND, RS, DEF, VISC>(m, e0, min(EPB, e_end - e0), stage);
   const int ed = e - m.n_car;
   const double d_pos = active ? m.nom_size[e] : 1.;
   const double inv_dpos = 1./d_pos;
