@@ -133,16 +133,28 @@ def kernel_bytes(name, ar, precision="fp64"):
 
 
 # DRAM bytes per element and launch measured by ncu on smaller cases of the same kernels
-# (read + write; profiles/k_local_tgv_rs6.md): FP64 at 16^3, mixed at 24^3 elements.
+# (read + write; profiles/fp64_flops_tgv16_rs6.md: FP64 at 16^3; profiles/k_local_tgv_rs6.md:
+# mixed at 24^3 elements).
 NCU_DRAM_BYTES_PER_ELEM = {
-    ("local_def_ns", "fp64", 6): (219.963136e6 + 74.511616e6) / 4096,
-    ("local_def_ns", "mixed", 6): (479.854848e6 + 207.921664e6) / 13824,
+    ("local_def_ns", "fp64", 6): 73281.,
+    ("local_def_euler", "fp64", 6): 69966.,
+    ("local_def_ns", "mixed", 6): (479.844352e6 + 200.925952e6) / 13824,
+    ("local_def_euler", "mixed", 6): (453.252864e6 + 146.395392e6) / 13824,
 }
 
 
 # Busiest pipe of the same kernels in those captures (% of peak sustained, active cycles).
 NCU_PIPE_FRAC = {
     ("local_def_ns", "fp64", 6): ("fp64", 0.919),
+    ("local_def_euler", "fp64", 6): ("fp64", 0.879),
+}
+
+# FP64 flops per element of the FP64 kernels (2 x DFMA + DADD + DMUL thread instructions,
+# ncu on the 16^3 case; profiles/fp64_flops_tgv16_rs6.md): the compute roofline of the FP64
+# form, against the FP64 FMA rate hexed_gpu_fp64_peak measures in the same run.
+NCU_FP64_FLOPS_PER_ELEM = {
+    ("local_def_ns", 6): 455624.,
+    ("local_def_euler", 6): 106920.,
 }
 
 
@@ -491,6 +503,17 @@ def main():
     if pipe is not None:
         # what bounds this kernel instead of HBM: the busiest pipe in ncu (profiles/k_local_tgv_rs6.md)
         roofline["compute_bound"] = {"pipe": pipe[0], "frac_of_peak_ncu": pipe[1]}
+    flops = NCU_FP64_FLOPS_PER_ELEM.get((top_name, wl.rs)) if wl.kind in ("tgv", "mach2") else None
+    if flops is not None and precision == abi.FP64 and fp64_peak:
+        # the FP64 form's own roof: its FP64 flops per launch over the launch time, against the
+        # FP64 FMA rate measured in this run
+        n = ar.n_def if "def" in top_name else ar.n_car
+        achieved_tf = flops * n / (per_launch_ms * 1e-3) / 1e12
+        roofline["fp64"] = {"achieved": achieved_tf, "peak": fp64_peak, "unit": "TFLOP/s",
+                            "frac": achieved_tf / fp64_peak, "flops_per_launch": flops * n,
+                            "flops_source": "ncu 2*dfma + dadd + dmul thread instructions per element of the "
+                                            "16^3 case, scaled by elements (profiles/fp64_flops_tgv16_rs6.md)",
+                            "peak_source": "hexed_gpu_fp64_peak, measured in this run"}
     kernels = {k: {"launches": v[0], "total_ms": round(v[1], 4), "share": round(v[1] / sum(x[1] for x in prof.values()), 4)}
                for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])}
 

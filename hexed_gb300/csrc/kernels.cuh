@@ -1515,11 +1515,11 @@ k_reconcile_ldg(Dev<FaceT> m, Tab<RS> tab, RowTab<RS, R> rt, int e_begin, int e_
   STab<RS, R>& st = *reinterpret_cast<STab<RS, R>*>(smem_raw);
   R* s_u = reinterpret_cast<R*>(smem_raw + (sizeof(STab<RS, R>) + 15)/16*16);
   R* s_t = s_u + EPB*nv*nq;
-  st.load(tab);
-  __syncthreads();
   const int le = threadIdx.x/nq, q = threadIdx.x%nq;
   const int e0 = e_begin + blockIdx.x*EPB, e = e0 + le;
   const bool active = threadIdx.x < EPB*nq && e < e_end;
+  st.load(tab);
+  __syncthreads();
   R tr[nv];
   #pragma unroll
   for (int v = 0; v < nv; ++v) tr[v] = 0;
