@@ -623,11 +623,14 @@ struct LocalSmemRows {
   //   s_g  [ND][nv][nq] gradient; then the viscous fluxes (viscous path)
   //   s_vr [nv][nq]     viscous residual (viscous path)
   static constexpr int per_elem = S::nv*S::nq + ND*S::nv*S::nq + (VISC ? (ND + 1)*S::nv*S::nq : 0);
-  // [mbarrier, 16 B][1/element size, EPB x R][element states, EPB x (nv + 3) x nq doubles][work]
+  // [mbarrier, 16 B][1/element size, EPB x R][element states, EPB x (nv + 3) x nq doubles]
+  // [deformed: metric normals and determinant, EPB x (nd^2 + 1) x nq in R][work]
   static constexpr size_t idp_offset = 16;
   static constexpr size_t state_offset = idp_offset + (sizeof(R)*EPB + 15)/16*16;
   static constexpr size_t state_bytes = sizeof(double)*(size_t)EPB*(S::nv + 3)*S::nq;
-  static constexpr size_t work_offset = state_offset + (state_bytes + 15)/16*16;
+  static constexpr size_t nrm_offset = state_offset + (state_bytes + 15)/16*16;
+  static constexpr size_t nrm_bytes = DEF ? sizeof(R)*(size_t)EPB*(ND*ND + 1)*S::nq : 0;
+  static constexpr size_t work_offset = nrm_offset + (nrm_bytes + 15)/16*16;
   static constexpr size_t bytes = work_offset + sizeof(R)*(size_t)per_elem*EPB;
 };
 
@@ -1122,30 +1125,39 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
   unsigned long long* s_bar = reinterpret_cast<unsigned long long*>(smem_raw);
   R* s_idp = reinterpret_cast<R*>(smem_raw + L::idp_offset);
   double* s_state = reinterpret_cast<double*>(smem_raw + L::state_offset);
+  R* s_n = reinterpret_cast<R*>(smem_raw + L::nrm_offset);   // deformed: [EPB][nd^2 + 1][nq]
   R* s_u = reinterpret_cast<R*>(smem_raw + L::work_offset);
   R* s_x = s_u + EPB*nv*nq;
   R* s_g = s_x + EPB*ND*nv*nq;
   R* s_vr = s_g + (VISC ? EPB*ND*nv*nq : 0);
+  static_assert(sizeof(FaceT) == sizeof(R), "the row-task body stages FaceT metric normals as R");
   const int le = threadIdx.x/nq;
   const int q = threadIdx.x%nq;
   const int e0 = e_begin + blockIdx.x*EPB;
   const int e = e0 + le;
   const bool active = threadIdx.x < EPB*nq && e < e_end;
-  // The CTA's element states ([n][nv + 3][nq], contiguous) arrive in shared memory by one bulk
-  // copy; where the range is not 16-byte aligned, threads read global memory directly (same
-  // values).
+  const int n_here = min(EPB, e_end - e0);
+  // The CTA's element states ([n][nv + 3][nq], contiguous) and, for deformed elements, their
+  // metric normals ([n][nd^2 + 1][nq], contiguous) arrive in shared memory by bulk copies;
+  // where a range is not 16-byte aligned, threads read global memory instead (same values).
   const double* g_state = m.elem + (size_t)e0*(nv + 3)*nq;
-  const unsigned state_bytes = unsigned(min(EPB, e_end - e0)*(nv + 3)*nq*sizeof(double));
+  const unsigned state_bytes = unsigned(n_here*(nv + 3)*nq*sizeof(double));
   const bool bulk = ((reinterpret_cast<unsigned long long>(g_state) | state_bytes) & 15u) == 0;
-  if (bulk && threadIdx.x == 0) mbar_init(s_bar, 1);
+  const FaceT* g_nrm = DEF ? m.nrm + (size_t)(e0 - m.n_car)*(ND*ND + 1)*nq : nullptr;
+  const unsigned nrm_bytes = DEF ? unsigned(n_here*(ND*ND + 1)*nq*sizeof(FaceT)) : 0u;
+  const bool bulk_n = DEF && bulk && ((reinterpret_cast<unsigned long long>(g_nrm) | nrm_bytes) & 15u) == 0;
+  if (bulk && threadIdx.x == 0) mbar_init(s_bar, bulk_n ? 2 : 1);
   if (threadIdx.x < EPB) {
     const int ee = e0 + threadIdx.x;
     const double dp = ee < e_end ? m.nom_size[ee] : 1.;
     s_idp[threadIdx.x] = split ? R(1)/to_R<R>(dp) : R(1./dp);
   }
   __syncthreads();
-  if (bulk && threadIdx.x == 0) bulk_load(s_state, g_state, state_bytes, s_bar);
-  if (threadIdx.x == 32) prefetch_element_arrays<ND, RS, DEF, VISC>(m, e0, min(EPB, e_end - e0), stage);
+  if (bulk && threadIdx.x == 0) {
+    bulk_load(s_state, g_state, state_bytes, s_bar);
+    if (bulk_n) bulk_load(s_n, g_nrm, nrm_bytes, s_bar);
+  }
+  if (threadIdx.x == 32) prefetch_element_arrays<ND, RS, DEF, VISC>(m, e0, n_here, stage);
   const int ed = e - m.n_car;
   const double d_pos = active ? m.nom_size[e] : 1.;
   const double inv_dpos = 1./d_pos;
@@ -1153,15 +1165,21 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
   const bool staged = bulk && mbar_wait(s_bar, 0, bulk_wait_polls);
   if (bulk && !staged) atomicOr(m.status + 1, flag_bulk_wait);
   const double* state_g = (staged ? s_state : g_state) + (size_t)le*(nv + 3)*nq;
+  if constexpr (DEF) {
+    // normals not staged by the bulk copy: each point copies its own (visible after the next
+    // barrier, before any other thread reads them)
+    if (!(bulk_n && staged) && active) {
+      const FaceT* nr = m.nrm + (size_t)ed*(ND*ND + 1)*nq;
+      #pragma unroll
+      for (int k = 0; k < ND*ND; ++k) s_n[(le*(ND*ND + 1) + k)*nq + q] = R(nr[k*nq + q]);
+    }
+  }
+  // comp.normal(j, i) of this thread's point, in shared memory (deformed elements)
+  auto normal = [&](int l, int j, int i, int p) { return s_n[(l*(ND*ND + 1) + i*ND + j)*nq + p]; };
 
   R u[nv + 2];   // state + bulk AV + Laplacian AV (include/pde.hpp:79-84)
   R up[nv];      // offset form of the state
   const double* ref_e = split ? m.ref + (size_t)(active ? e : 0)*nv : nullptr;
-  R nrm[ND][ND]; // nrm[j][i] = comp.normal(j, i)
-  #pragma unroll
-  for (int i = 0; i < ND; ++i)
-    #pragma unroll
-    for (int j = 0; j < ND; ++j) nrm[j][i] = (i == j) ? R(1) : R(0);
   if (active) {
     #pragma unroll
     for (int v = 0; v < nv; ++v) {
@@ -1172,13 +1190,6 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
     }
     u[nv] = to_R<R>(state_g[(nv + 1)*nq + q]);
     u[nv + 1] = to_R<R>(state_g[(nv + 2)*nq + q]);
-    if constexpr (DEF) {
-      const FaceT* nr = m.nrm + (size_t)ed*(ND*ND + 1)*nq;
-      #pragma unroll
-      for (int i = 0; i < ND; ++i)
-        #pragma unroll
-        for (int j = 0; j < ND; ++j) nrm[j][i] = R(nr[(i*ND + j)*nq + q]);
-    }
   } else {
     #pragma unroll
     for (int v = 0; v < nv + 2; ++v) u[v] = R(1);
@@ -1220,42 +1231,46 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
         });
       }
     } else {
-      // grad[v][j] = sum_d [D_d.(n_dj u) + lift_d.(n_face u_face - B_d.(n_dj u))] / size
-      const FaceT* fnr_e = m.face_nrml;
+      // grad[v][j] = sum_d [D_d.(n_dj u) + lift_d.(n_face u_face - B_d.(n_dj u))] / size. One task
+      // per (variable, row) forms all nd products n_dj u along its row from the staged offset
+      // state and normals, sharing the row's state and face values.
+      if (active) {
+        #pragma unroll
+        for (int v = 0; v < nv; ++v) s_u[(le*nv + v)*nq + q] = up[v];
+      }
       static_for<ND>([&](auto dc) {
         constexpr int d = decltype(dc)::value;
-        if constexpr (d > 0) __syncthreads();   // the previous dimension's tasks have read s_x
-        if (active) {
-          #pragma unroll
-          for (int j = 0; j < ND; ++j)
-            #pragma unroll
-            for (int v = 0; v < nv; ++v) s_x[((le*ND + j)*nv + v)*nq + q] = nrm[j][d]*up[v];
-        }
-        __syncthreads();
+        __syncthreads();   // d = 0: s_u and s_n complete; d > 0: the previous dimension's tasks are done
         constexpr int stride = S::stride(d);
-        constexpr int n_task = EPB*ND*nv*nfq;
+        constexpr int n_task = EPB*nv*nfq;
         for (int t = threadIdx.x; t < n_task; t += blockDim.x) {
-          const int r = t%nfq;
-          int rest = t/nfq;
-          const int v = rest%nv; rest /= nv;
-          const int j = rest%ND, l = rest/ND;
+          const int r = t%nfq, rest = t/nfq;
+          const int v = rest%nv, l = rest/nv;
           const int ee = e0 + l;
           if (ee >= e_end) continue;
           const int base = row_base<ND, RS, d>(r);
-          R x[RS];
-          load_row<RS, stride>(s_x + ((l*ND + j)*nv + v)*nq + base, x);
-          R a0, a1;
-          bound_dot(rt, x, a0, a1);
+          R xu[RS];
+          load_row<RS, stride>(s_u + (l*nv + v)*nq + base, xu);
           const FaceT* fl = m.face + (size_t)(ee*2*ND + 2*d)*S::slot_dof + nv*nfq + v*nfq + r;
-          const FaceT* fnr = fnr_e + ((size_t)(ee - m.n_car)*2*ND + 2*d)*ND*nfq + j*nfq + r;
-          const R b0 = R(fnr[0])*R(fl[0]) - a0;
-          const R b1 = R(fnr[ND*nfq])*R(fl[S::slot_dof]) - a1;
+          const R fl0 = R(fl[0]), fl1 = R(fl[S::slot_dof]);
+          const FaceT* fnr = m.face_nrml + ((size_t)(ee - m.n_car)*2*ND + 2*d)*ND*nfq + r;
           const R idp = s_idp[l];
-          R* g = s_g + ((l*ND + j)*nv + v)*nq + base;
           #pragma unroll
-          for (int i = 0; i < RS; ++i) {
-            const R o = row_deriv(rt, x, i, b0, b1);
-            g[i*stride] = d ? g[i*stride] + o*idp : o*idp;
+          for (int j = 0; j < ND; ++j) {
+            const R* nrow = s_n + (l*(ND*ND + 1) + d*ND + j)*nq + base;
+            R x[RS];
+            #pragma unroll
+            for (int k = 0; k < RS; ++k) x[k] = nrow[k*stride]*xu[k];
+            R a0, a1;
+            bound_dot(rt, x, a0, a1);
+            const R b0 = R(fnr[j*nfq])*fl0 - a0;
+            const R b1 = R(fnr[ND*nfq + j*nfq])*fl1 - a1;
+            R* g = s_g + ((l*ND + j)*nv + v)*nq + base;
+            #pragma unroll
+            for (int i = 0; i < RS; ++i) {
+              const R o = row_deriv(rt, x, i, b0, b1);
+              g[i*stride] = d ? g[i*stride] + o*idp : o*idp;
+            }
           }
         }
       });
@@ -1275,6 +1290,11 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
     Conv<ND, R> c(u);
     RefState<ND, R> rs;   // formed here, not kept live through the gradient part
     if constexpr (split) rs.set(ref_e);
+    R nrm[ND][ND]; // nrm[j][i] = comp.normal(j, i)
+    #pragma unroll
+    for (int i = 0; i < ND; ++i)
+      #pragma unroll
+      for (int j = 0; j < ND; ++j) nrm[j][i] = DEF ? normal(le, j, i, q) : (i == j) ? R(1) : R(0);
     #pragma unroll
     for (int i = 0; i < ND; ++i) {
       R col[ND], f[nv];
