@@ -57,7 +57,8 @@ class KernelTime(ctypes.Structure):
 class UpdateParams(ctypes.Structure):
     _fields_ = [("max_safety", c_double), ("max_time_step", c_double), ("n_cheby_flow", c_int),
                 ("flow_iters", c_int), ("local_time", c_int), ("use_filter", c_int), ("use_ldg", c_int),
-                ("visc", Transport), ("cond", Transport), ("av_admis_char_speed", c_double)]
+                ("visc", Transport), ("cond", Transport), ("av_admis_char_speed", c_double),
+                ("fix_admis", c_int), ("fix_admis_max_safety", c_double)]
 
 
 def transport_inviscid():
@@ -76,15 +77,18 @@ def transport_sutherland(ref_value, ref_temp, offset):
 
 
 def update_params(max_safety=0.7, max_time_step=1.7976931348623157e308, n_cheby_flow=1, flow_iters=1,
-                  local_time=False, use_filter=False, visc=None, cond=None, use_ldg=None, av_admis_char_speed=0.):
+                  local_time=False, use_filter=False, visc=None, cond=None, use_ldg=None, av_admis_char_speed=0.,
+                  fix_admis=False, fix_admis_max_safety=0.7):
     """Defaults of the Solver namespace (src/Solver.cpp:151-174). use_ldg follows
-    Solver::use_ldg (src/Solver.cpp:117-120): viscous transport or artificial viscosity."""
+    Solver::use_ldg (src/Solver.cpp:117-120): viscous transport or artificial viscosity.
+    fix_admis: Solver::fix_admissibility after every stage (Solver::set_fix_admissibility)."""
     visc = visc or transport_inviscid()
     cond = cond or transport_inviscid()
     if use_ldg is None:
         use_ldg = bool(visc.is_viscous or cond.is_viscous or av_admis_char_speed > 0)
     return UpdateParams(max_safety, max_time_step, n_cheby_flow, flow_iters, int(local_time),
-                        int(use_filter), int(use_ldg), visc, cond, av_admis_char_speed)
+                        int(use_filter), int(use_ldg), visc, cond, av_admis_char_speed, int(fix_admis),
+                        fix_admis_max_safety)
 
 
 class HexedError(RuntimeError):
@@ -137,6 +141,7 @@ def load_library(path=LIB_PATH):
         "hexed_gpu_set_launch_shape": ([vp, c_int, c_int], c_int),
         "hexed_gpu_check_conversions": ([P_double, ctypes.c_long, ctypes.POINTER(ctypes.c_long)], c_int),
         "hexed_gpu_is_admissible": ([vp, P_int, P_int], c_int),
+        "hexed_gpu_fix_admissibility": ([vp, ctypes.POINTER(UpdateParams), c_double, P_int], c_int),
         "hexed_gpu_device_flags": ([vp, P_int], c_int),
         "hexed_gpu_compute_jacobian": ([vp, P_double], c_int),
         "hexed_gpu_write_state": ([vp, P_double], c_int),

@@ -47,6 +47,7 @@ struct OpsTable {
   int (*local_elems_per_cta)(int variant);
   void (*admissible)(Ctx&, int* d_record);
   void (*compute_jacobian)(Ctx&, const double* d_vert_pos, double* d_fn, double* d_vtss);
+  void (*fix_admis_coef)(Ctx&, const int* d_record, bool swap_only);
 };
 
 // A captured multi-update sequence and the inputs it was captured for.
@@ -99,6 +100,8 @@ struct Ctx {
   // per CTA of the face kernels
   int local_variant;
   int face_threads;
+  // 1 while Solver::fix_admissibility's diffusion runs: the kernels compute pde::Fix_therm_admis
+  int fta;
 };
 
 // Max_dt's CFL reciprocals for convective and diffusive safety factors (include/Spatial.hpp:

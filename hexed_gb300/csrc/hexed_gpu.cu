@@ -11,6 +11,7 @@
 #include <vector>
 #include <algorithm>
 #include <mutex>
+#include <limits>
 #include "ctx.h"
 #include "kernels.cuh"
 #include "basis_tables.h"
@@ -715,6 +716,78 @@ int hexed_gpu_apply_flux_bcs(hexed_gpu_ctx* c)
 }
 
 namespace {
+// Solver::is_admissible on the device, read back to the host (synchronizes the stream)
+int admissible_now(Ctx* c, bool* admissible)
+{
+  c->ops->admissible(*c, c->record);
+  HX_LAUNCHED();
+  HX_CUDA(cudaMemcpyAsync(c->h_pinned, c->status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  HX_CUDA(cudaStreamSynchronize(c->stream));
+  int flags;
+  std::memcpy(&flags, c->h_pinned, sizeof(int));
+  if (flags & 2) return fail(HEXED_ERR_NUMERICAL, "state is not finite");
+  *admissible = !(flags & 1);
+  return HEXED_OK;
+}
+
+// The diffusion of one Solver::fix_admissibility iteration (src/Solver.cpp:985-1089), after
+// its admissibility check: the coefficient set-up and bulk/Laplacian swap, the local Max_dt of
+// pde::Fix_therm_admis, two Fix_therm_admis sub-steps of the LDG chain (state BC fused into
+// the boundary Neighbor: ghost = inside), the flow's Max_dt of the fixed state, and the swap
+// back. The flow's step and raw max_dt (scalars[0, 2)) are kept across it, as the reference's
+// stage keeps its opts.dt.
+int fix_iteration(Ctx* c, const hexed_update_params* p, double stability_ratio)
+{
+  const hexed_transport inv = inviscid();
+  c->ops->fix_admis_coef(*c, c->record, false);
+  hx::k_copy_scalars<<<1, 32, 0, c->stream>>>(c->scalars, hx::SC_DT, hx::SC_SAVED, 2);
+  c->fta = 1;
+  c->ops->max_dt(*c, stability_ratio, stability_ratio, 1, 1, inv, inv, std::numeric_limits<double>::max(), 1.);
+  // dt = 1 split into two sub-steps (src/Solver.cpp:1060-1064)
+  const double linear = 1., quadratic = 1./8/0.9;
+  double step[2];
+  step[1] = (linear + std::sqrt(linear*linear - 4*quadratic))/2.;
+  step[0] = quadratic/step[1];
+  for (double s : step) {
+    if (int st = set_dt(c, s)) { c->fta = 0; return st; }
+    c->ops->compute_navier_stokes(*c, 0, 0, 0, inv, inv, true);
+  }
+  c->fta = 0;
+  const double max_cheby = chebyshev_step(p->n_cheby_flow, p->n_cheby_flow - 1);
+  c->ops->max_dt(*c, p->max_safety/max_cheby, p->max_safety, p->local_time, p->use_ldg, p->visc, p->cond,
+                 p->max_time_step, 1.);
+  hx::k_copy_scalars<<<1, 32, 0, c->stream>>>(c->scalars, hx::SC_SAVED, hx::SC_DT, 2);
+  c->ops->fix_admis_coef(*c, nullptr, true);
+  HX_LAUNCHED();
+  return HEXED_OK;
+}
+
+// Solver::fix_admissibility (src/Solver.cpp:961-1095): *iters as the reference returns it
+int fix_admissibility(Ctx* c, const hexed_update_params* p, double stability_ratio, int* iters)
+{
+  if (c->n_vert > 0 && !c->uncert) return fail(HEXED_ERR_INVALID, "vertex scratch missing");
+  int iter;
+  int n_iters = std::numeric_limits<int>::max();
+  for (iter = 0; iter < n_iters; ++iter) {
+    if (iter >= 100000) return fail(HEXED_ERR_NUMERICAL, "failed to fix thermodynamic admissability in %i iterations", iter);
+    bool adm;
+    if (int st = admissible_now(c, &adm)) return st;
+    if (adm) {
+      if (iter) n_iters = std::min(n_iters, 2*iter);
+      else {
+        ++iter;
+        break;
+      }
+    } else {
+      n_iters = std::numeric_limits<int>::max();
+    }
+    if (int st = fix_iteration(c, p, stability_ratio)) return st;
+  }
+  --iter;
+  *iters = iter;
+  return HEXED_OK;
+}
+
 // Enqueues one Solver::update (src/Solver.cpp:834-886) on the context's stream. With local
 // time stepping and no diffusion the step is known on the host (the global part is 1, times
 // max_time_step and the Chebyshev factor, as k_finalize_dt would give): the first stage's
@@ -729,7 +802,7 @@ int enqueue_update(hexed_gpu_ctx* c, const hexed_update_params* p, double* host_
     if (c->n_vert <= 0) return fail(HEXED_ERR_INVALID, "artificial viscosity needs the arena's vertex table");
     c->ops->set_art_visc_admis(*c, p->av_admis_char_speed);
   }
-  const bool fuse_dt = p->local_time && !p->use_ldg;
+  const bool fuse_dt = p->local_time && !p->use_ldg && !p->fix_admis;
   const double max_cheby = chebyshev_step(p->n_cheby_flow, p->n_cheby_flow - 1);
   for (int i_flow = 0; i_flow < p->flow_iters; ++i_flow) {
     for (int i_cheby = 0; i_cheby < p->n_cheby_flow; ++i_cheby) {
@@ -744,10 +817,19 @@ int enqueue_update(hexed_gpu_ctx* c, const hexed_update_params* p, double* host_
         continue;
       }
       c->ops->max_dt(*c, msc, msd, p->local_time, p->use_ldg, p->visc, p->cond, p->max_time_step, cheby);
+      bool fixed = false;
       for (int i = 0; i < 2; ++i) {
         if (p->use_ldg && !i) c->ops->compute_navier_stokes(*c, 0, 0, p->use_filter, p->visc, p->cond, true);
         else c->ops->compute_euler(*c, i, 0, p->use_filter, true, hx::LocalDt{0, 0., 0., 0.});
+        if (p->fix_admis) {
+          // Solver.cpp:866-867: every stage ends with fix_admissibility; a fixed update
+          // leaves the Chebyshev loop after its two stages
+          int iters = 0;
+          if (int st = fix_admissibility(c, p, p->fix_admis_max_safety, &iters)) return st;
+          fixed = iters || fixed;
+        }
       }
+      if (fixed) break;
     }
   }
   return HEXED_OK;
@@ -759,11 +841,19 @@ bool same_params(const hexed_update_params& a, const hexed_update_params& b)
 }
 } // namespace
 
+int hexed_gpu_fix_admissibility(hexed_gpu_ctx* c, const hexed_update_params* p, double stability_ratio, int* iterations)
+{
+  if (int st = check_ctx(c)) return st;
+  if (!p || !iterations || p->n_cheby_flow < 1 || !(stability_ratio > 0))
+    return fail(HEXED_ERR_INVALID, "bad fix_admissibility arguments");
+  return fix_admissibility(c, p, stability_ratio, iterations);
+}
+
 int hexed_gpu_update_n(hexed_gpu_ctx* c, const hexed_update_params* p, int n, int use_graph)
 {
   if (int st = check_ctx(c)) return st;
   if (!p || p->n_cheby_flow < 1 || p->flow_iters < 0 || n < 0) return fail(HEXED_ERR_INVALID, "bad update parameters");
-  if (!use_graph) {
+  if (!use_graph || p->fix_admis) {   // the admissibility fix reads back to the host: eager
     for (int i = 0; i < n; ++i) if (int st = enqueue_update(c, p)) return st;
     HX_LAUNCHED();
     return HEXED_OK;

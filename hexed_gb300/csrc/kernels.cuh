@@ -73,9 +73,14 @@ struct Dev {
   double* scalars;       // [0] dt of the current stage, [1] raw max_dt, ...
   double* partials;      // per-block reduction scratch
   int* status;           // device-side error flags
+  // 1: the viscous chain and Max_dt compute pde::Fix_therm_admis (include/pde.hpp:437-493)
+  // instead of Navier-Stokes: no convection, flux = -gradient*normal, diffusivity 1; its
+  // boundary conditions copy the inside state to the ghost face and negate the inside LDG
+  // flux (src/Solver.cpp:103-114, 1067-1072)
+  int fta;
 };
 
-enum { SC_DT = 0, SC_MAXDT = 1, SC_FLOWTIME = 2, SC_N = 8 };
+enum { SC_DT = 0, SC_MAXDT = 1, SC_FLOWTIME = 2, SC_SAVED = 4, SC_N = 8 };   // SC_SAVED: copy of [0, 2)
 
 template <int ND, int RS>
 struct Shape {
@@ -335,6 +340,23 @@ __device__ __forceinline__ void flux_diff(const R* s, const Conv<ND, R>& c, cons
       R acc = 0;
       #pragma unroll
       for (int j = 0; j < ND; ++j) acc += fd[v][j]*nrm[j][i];
+      out[v][i] = acc;
+    }
+  }
+}
+
+// Fix_therm_admis::compute_flux_diff (include/pde.hpp:481-485): flux = -gradient*normal
+template <int ND, typename R, bool IDENT>
+__device__ __forceinline__ void flux_fta(const R (&g)[ND + 2][ND], const R (&nrm)[ND][ND], R (&out)[ND + 2][ND])
+{
+  #pragma unroll
+  for (int v = 0; v < ND + 2; ++v) {
+    #pragma unroll
+    for (int i = 0; i < ND; ++i) {
+      if (IDENT) { out[v][i] = -g[v][i]; continue; }
+      R acc = 0;
+      #pragma unroll
+      for (int j = 0; j < ND; ++j) acc += -g[v][j]*nrm[j][i];
       out[v][i] = acc;
     }
   }
@@ -661,6 +683,7 @@ __device__ __forceinline__ R point_step(const Dev<FaceT>& m, int e, int q, const
   #pragma unroll
   for (int v = 0; v < nv; ++v) s[v] = to_R<R>(state[v*nq + q]);
   const R inv_spacing = R(1)/spacing;
+  if (m.fta) return R(1)/(inv_cfl_d*inv_spacing*inv_spacing);   // Fix_therm_admis: diffusivity 1
   Conv<ND, R> c(s);
   R scale = 0;
   scale += char_speed<ND, R>(s, c.inv_mass)*inv_cfl_c*inv_spacing;
@@ -919,7 +942,10 @@ __device__ __forceinline__ void local_body_points(Dev<FaceT> m, const Tab<RS>& t
       R col[ND], f[nv];
       #pragma unroll
       for (int j = 0; j < ND; ++j) col[j] = nrm[j][i];
-      if constexpr (split) flux_delta<ND, R>(u, up, rs, c, col, f);
+      if (VISC && m.fta) {
+        #pragma unroll
+        for (int v = 0; v < nv; ++v) f[v] = R(0);   // Fix_therm_admis has no convection
+      } else if constexpr (split) flux_delta<ND, R>(u, up, rs, c, col, f);
       else c.flux(u, col, f);
       #pragma unroll
       for (int v = 0; v < nv; ++v) my_f[(i*nv + v)*nq + q] = f[v];
@@ -931,9 +957,13 @@ __device__ __forceinline__ void local_body_points(Dev<FaceT> m, const Tab<RS>& t
       for (int v = 0; v < nv; ++v)
         #pragma unroll
         for (int j = 0; j < ND; ++j) g[v][j] = DEF ? grad[v][j]*inv_det : grad[v][j];
-      DiffScalars<ND, R> df(u, c, u[nv], u[nv + 1], visc, cond);
       R fd[nv][ND];
-      flux_diff<ND, R, !DEF>(u, c, df, g, nrm, fd);
+      if (m.fta) {
+        flux_fta<ND, R, !DEF>(g, nrm, fd);
+      } else {
+        DiffScalars<ND, R> df(u, c, u[nv], u[nv + 1], visc, cond);
+        flux_diff<ND, R, !DEF>(u, c, df, g, nrm, fd);
+      }
       #pragma unroll
       for (int i = 0; i < ND; ++i)
         #pragma unroll
@@ -959,8 +989,10 @@ __device__ __forceinline__ void local_body_points(Dev<FaceT> m, const Tab<RS>& t
       for (int i = 0; i < RS; ++i) { R x = row[i*stride]; a0 += st.bound[i]*x; a1 += st.bound[RS + i]*x; }
       FaceT* fl = m.face + (size_t)(ee*2*ND + 2*d)*S::slot_dof + v*nfq + r;
       R* bf = s_bf + ((l*ND + d)*2*nv)*nfq;
-      bf[v*nfq + r] = R(fl[0]) - a0;
-      bf[(nv + v)*nfq + r] = R(fl[S::slot_dof]) - a1;
+      // Fix_therm_admis: no convective flux, in the faces as in the volume
+      const bool conv = !(VISC && m.fta);
+      bf[v*nfq + r] = (conv ? R(fl[0]) : R(0)) - a0;
+      bf[(nv + v)*nfq + r] = (conv ? R(fl[S::slot_dof]) : R(0)) - a1;
       if constexpr (VISC) {
         const R* rg = s_g + ((l*ND + d)*nv + v)*nq + off;
         R g0 = 0, g1 = 0;
@@ -1056,7 +1088,7 @@ __device__ __forceinline__ void local_body_points(Dev<FaceT> m, const Tab<RS>& t
         if (stage) {
           uu -= rc[v*nq + q];
         } else {
-          rc[v*nq + q] = uu;
+          if (!(VISC && m.fta)) rc[v*nq + q] = uu;   // Fix_therm_admis keeps no residual cache
           if constexpr (VISC) uu += double(vrate[v]);
         }
         uu *= mult;
@@ -1079,7 +1111,7 @@ __device__ __forceinline__ void local_body_points(Dev<FaceT> m, const Tab<RS>& t
         if (stage) {
           ur -= R(rc[v*nq + q]);
         } else {
-          rc[v*nq + q] = FaceT(ur);
+          if (!(VISC && m.fta)) rc[v*nq + q] = FaceT(ur);
           if constexpr (VISC) ur += vrate[v];
         }
         const R inc = ur*mult;
@@ -1300,7 +1332,10 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
       R col[ND], f[nv];
       #pragma unroll
       for (int j = 0; j < ND; ++j) col[j] = nrm[j][i];
-      if constexpr (split) flux_delta<ND, R>(u, up, rs, c, col, f);
+      if (VISC && m.fta) {
+        #pragma unroll
+        for (int v = 0; v < nv; ++v) f[v] = R(0);   // Fix_therm_admis has no convection
+      } else if constexpr (split) flux_delta<ND, R>(u, up, rs, c, col, f);
       else c.flux(u, col, f);
       #pragma unroll
       for (int v = 0; v < nv; ++v) s_x[((le*ND + i)*nv + v)*nq + q] = f[v];
@@ -1312,9 +1347,13 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
       for (int v = 0; v < nv; ++v)
         #pragma unroll
         for (int j = 0; j < ND; ++j) g[v][j] = DEF ? grad[v][j]*inv_det : grad[v][j];
-      DiffScalars<ND, R> df(u, c, u[nv], u[nv + 1], visc, cond);
       R fd[nv][ND];
-      flux_diff<ND, R, !DEF>(u, c, df, g, nrm, fd);
+      if (m.fta) {
+        flux_fta<ND, R, !DEF>(g, nrm, fd);
+      } else {
+        DiffScalars<ND, R> df(u, c, u[nv], u[nv + 1], visc, cond);
+        flux_diff<ND, R, !DEF>(u, c, df, g, nrm, fd);
+      }
       #pragma unroll
       for (int i = 0; i < ND; ++i)
         #pragma unroll
@@ -1340,7 +1379,9 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
       R a0, a1;
       bound_dot(rt, x, a0, a1);
       FaceT* fl = m.face + (size_t)(ee*2*ND + 2*d)*S::slot_dof + v*nfq + r;
-      const R b0 = R(fl[0]) - a0, b1 = R(fl[S::slot_dof]) - a1;
+      // Fix_therm_admis: no convective flux, in the faces as in the volume
+      const bool conv = !(VISC && m.fta);
+      const R b0 = (conv ? R(fl[0]) : R(0)) - a0, b1 = (conv ? R(fl[S::slot_dof]) : R(0)) - a1;
       R* ra = s_u + (l*nv + v)*nq + base;
       #pragma unroll
       for (int i = 0; i < RS; ++i) {
@@ -1442,7 +1483,7 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
         if (stage) {
           uu -= rc[v*nq + q];
         } else {
-          rc[v*nq + q] = uu;
+          if (!(VISC && m.fta)) rc[v*nq + q] = uu;   // Fix_therm_admis keeps no residual cache
           if constexpr (VISC) uu += double(vrate[v]);
         }
         uu *= mult;
@@ -1465,7 +1506,7 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
         if (stage) {
           ur -= R(rc[v*nq + q]);
         } else {
-          rc[v*nq + q] = FaceT(ur);
+          if (!(VISC && m.fta)) rc[v*nq + q] = FaceT(ur);
           if constexpr (VISC) ur += vrate[v];
         }
         const R inc = ur*mult;
@@ -1676,6 +1717,7 @@ __device__ __forceinline__ void neighbor_point(const Dev<FaceT>& m, int slot0, i
       f0[nv*nfq + v*nfq + q] = FaceT(avg);
       f1[nv*nfq + v*nfq + q1] = FaceT(avg);
     }
+    if (m.fta) return;   // Fix_therm_admis has no convection (Spatial.hpp:655-686 are skipped)
   }
   R u0[nv], u1[nv];
   #pragma unroll
@@ -1918,6 +1960,11 @@ __device__ void bc_state_point(const Dev<FaceT>& m, int i_bc, int q, double* gh)
   for (int v = 0; v < nv; ++v) ref[v] = !split ? 0. : m.ref[(size_t)(c[0]/(2*ND))*nv + v];
   double inside[nv], n[ND];
   for (int v = 0; v < nv; ++v) inside[v] = split ? double(in[v*nfq + q]) + ref[v] : double(in[v*nfq + q]);
+  if (m.fta) {
+    // Solver::fix_admissibility (src/Solver.cpp:1067-1072): ghost face = inside face
+    for (int v = 0; v < nv; ++v) { gh[v] = inside[v]; gf[v*nfq + q] = in[v*nfq + q]; }
+    return;
+  }
   for (int d = 0; d < ND; ++d) n[d] = nrml[d*nfq + q];
   switch (b.kind) {
     case HEXED_BC_FREESTREAM:
@@ -2076,6 +2123,11 @@ __device__ void bc_flux_point(const Dev<FaceT>& m, int i_bc, int q)
   const int ifs = (c[2] >> 2) & 1;
   FaceT* in_l = m.face + (size_t)c[0]*S::slot_dof + nv*nfq;
   FaceT* gh_l = m.face + (size_t)c[1]*S::slot_dof + nv*nfq;
+  if (m.fta) {
+    // Solver::apply_fta_flux_bcs (src/Solver.cpp:103-114): ghost LDG flux = -inside
+    for (int v = 0; v < nv; ++v) gh_l[v*nfq + q] = -in_l[v*nfq + q];
+    return;
+  }
   const double* nrml = m.bc_nrml + (size_t)i_bc*ND*nfq;
   double* sc = m.bc_cache + (size_t)i_bc*2*nv*nfq;
   double* fc = sc + nv*nfq;
@@ -2355,6 +2407,10 @@ static __global__ void k_finalize_dt(double* scalars, const double* partials, in
 }
 
 static __global__ void k_set_scalar(double* scalars, int which, double value) { scalars[which] = value; }
+static __global__ void k_copy_scalars(double* scalars, int from, int to, int n)
+{
+  for (int i = threadIdx.x; i < n; i += blockDim.x) scalars[to + i] = scalars[from + i];
+}
 
 // thermo::admissible (src/thermo.cpp:6-18) over every element state, every element face trace
 // and every fine mortar face, as Solver::is_admissible does (src/Solver.cpp:921-959): density
@@ -2522,6 +2578,40 @@ __global__ void k_av_vertex_max(const int* vert_id, int n_elem, const double* un
   for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
     const double x = uncert[t/nvert];
     atomicMax(reinterpret_cast<unsigned long long*>(vmax) + vert_id[t], (unsigned long long)__double_as_longlong(x));
+  }
+}
+
+// Solver::fix_admissibility's vertex coefficient (src/Solver.cpp:990-1008): an element's
+// admissibility record as the value its vertices start from ...
+static __global__ void k_record_to_value(const int* record, int n_elem, double* out)
+{
+  for (int e = blockIdx.x*blockDim.x + threadIdx.x; e < n_elem; e += gridDim.x*blockDim.x) out[e] = record[e];
+}
+
+// ... and, after the first vertex maximum, the maximum over each element's vertices
+template <int ND>
+__global__ void k_elem_vertex_max(const int* vert_id, int n_elem, const double* vmax, double* out)
+{
+  constexpr int nvert = 1 << ND;
+  for (int e = blockIdx.x*blockDim.x + threadIdx.x; e < n_elem; e += gridDim.x*blockDim.x) {
+    double x = 0;
+    for (int v = 0; v < nvert; ++v) x = fmax(x, vmax[vert_id[e*nvert + v]]);
+    out[e] = x;
+  }
+}
+
+// std::swap of the bulk and Laplacian artificial-viscosity rows of every qpoint
+// (src/Solver.cpp:1033-1039, 1083-1089)
+template <int ND, int RS>
+__global__ void k_swap_av(double* elem, int n_elem)
+{
+  constexpr int nq = Shape<ND, RS>::nq, nv = Shape<ND, RS>::nv;
+  const long total = (long)n_elem*nq;
+  for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
+    double* st = elem + (size_t)(t/nq)*(nv + 3)*nq + t%nq;
+    const double b = st[(nv + 1)*nq];
+    st[(nv + 1)*nq] = st[(nv + 2)*nq];
+    st[(nv + 2)*nq] = b;
   }
 }
 

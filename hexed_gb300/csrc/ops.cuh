@@ -35,6 +35,7 @@ struct Runner
     m.car_con = c.car_con; m.def_con = c.def_con;
     m.bc_con = c.bc_con; m.bc_nrml = c.bc_nrml; m.bc_cache = c.bc_cache; m.ref_face = c.ref_face;
     m.bc_spec = c.bc_spec; m.scalars = c.scalars; m.partials = c.partials; m.status = c.status;
+    m.fta = c.fta;
     if constexpr (std::is_same<R, double>::value) {
       m.rcache = c.rcache; m.face = c.face; m.nrm = c.jac; m.face_nrml = c.face_nrml;
       m.def_con_nrml = c.def_con_nrml; m.bc_nrml_t = c.bc_nrml;
@@ -330,6 +331,27 @@ struct Runner
     k_av_interp<ND, RS><<<grid_for((long)n_elem*S::nq, 256), 256, 0, c.stream>>>(c.elem, c.vert_id, n_elem, tab(c), c.vmax);
   }
 
+  // Solver::fix_admissibility's coefficient set-up (src/Solver.cpp:990-1039): the elements'
+  // admissibility records to a vertex maximum, the element maximum of that back to its
+  // vertices, interpolated into the Laplacian artificial-viscosity row, then the bulk and
+  // Laplacian rows swapped. swap_only: only the swap back (src/Solver.cpp:1083-1089). Without
+  // a vertex table the coefficient is not formed (the rows are swapped all the same).
+  static void fix_admis_coef(Ctx& c, const int* d_record, bool swap_only)
+  {
+    const int n_elem = c.n_car + c.n_def;
+    if (!swap_only && c.n_vert > 0) {
+      ProfScope ps(c, "fix_admis_coef");
+      k_record_to_value<<<grid_for(n_elem, 256), 256, 0, c.stream>>>(d_record, n_elem, c.uncert);
+      cudaMemsetAsync(c.vmax, 0, sizeof(double)*c.n_vert, c.stream);
+      k_av_vertex_max<ND><<<grid_for((long)n_elem*S::nvert, 256), 256, 0, c.stream>>>(c.vert_id, n_elem, c.uncert, c.vmax);
+      k_elem_vertex_max<ND><<<grid_for(n_elem, 256), 256, 0, c.stream>>>(c.vert_id, n_elem, c.vmax, c.uncert);
+      cudaMemsetAsync(c.vmax, 0, sizeof(double)*c.n_vert, c.stream);
+      k_av_vertex_max<ND><<<grid_for((long)n_elem*S::nvert, 256), 256, 0, c.stream>>>(c.vert_id, n_elem, c.uncert, c.vmax);
+      k_av_interp<ND, RS><<<grid_for((long)n_elem*S::nq, 256), 256, 0, c.stream>>>(c.elem, c.vert_id, n_elem, tab(c), c.vmax);
+    }
+    k_swap_av<ND, RS><<<grid_for((long)n_elem*S::nq, 256), 256, 0, c.stream>>>(c.elem, n_elem);
+  }
+
   static void segment_residual_norms(Ctx& c, int n_seg, const int* d_begin, const int* d_count, double* d_out)
   {
     ProfScope ps(c, "segment_residual");
@@ -341,6 +363,7 @@ struct Runner
     static const OpsTable t = {
       compute_euler, compute_navier_stokes, max_dt, refine, write_face, bc_state, bc_flux, residual_norm,
       set_art_visc_admis, segment_residual_norms, local_elems_per_cta, admissible, compute_jacobian,
+      fix_admis_coef,
     };
     return &t;
   }

@@ -118,6 +118,14 @@ class Context:
     def apply_flux_bcs(self):
         abi.check(self.lib.hexed_gpu_apply_flux_bcs(self.handle))
 
+    def fix_admissibility(self, params, stability_ratio=0.7):
+        """Solver::fix_admissibility: diffuse until admissible (and as long again); returns the
+        iteration count the reference returns (0: the state was admissible)."""
+        out = ctypes.c_int()
+        abi.check(self.lib.hexed_gpu_fix_admissibility(self.handle, ctypes.byref(params), stability_ratio,
+                                                       ctypes.byref(out)))
+        return out.value
+
     def is_admissible(self, records=False):
         """Solver::is_admissible: True if density and energy are positive everywhere
         (raises HexedError HEXED_ERR_NUMERICAL for a non-finite state); with records=True

@@ -163,6 +163,10 @@ typedef struct hexed_update_params {
   double av_admis_char_speed; /* > 0: Solver::set_art_visc_admis with this characteristic
                                  speed before every update, as Case.cpp:432 does when
                                  "diffusive_admissibility" is set; 0: off */
+  int fix_admis;              /* Solver::set_fix_admissibility (src/Solver.cpp:667-670): after
+                                 each stage, Solver::fix_admissibility restores thermodynamic
+                                 admissibility (on with set_shock, include/Case.hil:95) */
+  double fix_admis_max_safety; /* "fix_admis_max_safety" (src/Solver.cpp:153; default 0.7) */
 } hexed_update_params;
 
 typedef struct hexed_gpu_ctx hexed_gpu_ctx;
@@ -227,6 +231,17 @@ int hexed_gpu_compute_jacobian(hexed_gpu_ctx* ctx, const double* vert_pos);
  * active elements) receives 1 for each inadmissible element. Returns HEXED_ERR_NUMERICAL
  * ("state is not finite") if any of these values is not finite, where the reference asserts. */
 int hexed_gpu_is_admissible(hexed_gpu_ctx* ctx, int* admissible, int* record);
+
+/* Solver::fix_admissibility (src/Solver.cpp:961-1095). While the state is not admissible
+ * (hexed_gpu_is_admissible), and then for as many iterations again as it took, diffuse the
+ * state with pde::Fix_therm_admis (include/pde.hpp:437-493): local time step at
+ * `stability_ratio`, two sub-steps of the LDG diffusion chain with ghost state = inside and
+ * ghost LDG flux = -inside at the boundaries, then the flow's Max_dt of p (its step is
+ * kept). *iterations: the count the reference returns (0: was admissible). Fails with
+ * HEXED_ERR_NUMERICAL for a non-finite state or after 100000 iterations, as the reference
+ * asserts. Synchronizes the stream on every iteration. */
+int hexed_gpu_fix_admissibility(hexed_gpu_ctx* ctx, const hexed_update_params* p, double stability_ratio,
+                                int* iterations);
 
 /* Flags the kernels raised since the context was created (0 = none). Bit 0: a volume kernel
  * gave up waiting for the bulk copy of its element states and read global memory instead

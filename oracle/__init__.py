@@ -53,6 +53,7 @@ def load():
             "oracle_residual_norm": [D, P],
             "oracle_set_art_visc_admis": [D, c_double],
             "oracle_update": [D, U, P],
+            "oracle_fix_admissibility": [D, U, c_double, ctypes.POINTER(c_int)],
             "oracle_compute_residual": [D, U],
             "oracle_derivative": [c_int, P, P, P],
             "oracle_perm_index": [c_int, c_int, c_int, c_int],
@@ -154,6 +155,13 @@ class Oracle:
 
     def compute_residual(self, params):
         self._chk(self.lib.oracle_compute_residual(ctypes.byref(self.desc), ctypes.byref(params)))
+
+    def fix_admissibility(self, params, stability_ratio=0.7):
+        """Solver::fix_admissibility (src/Solver.cpp:961-1095): the iteration count."""
+        out = ctypes.c_int()
+        self._chk(self.lib.oracle_fix_admissibility(ctypes.byref(self.desc), ctypes.byref(params), stability_ratio,
+                                                    ctypes.byref(out)))
+        return out.value
 
     def set_art_visc_admis(self, char_speed):
         self._chk(self.lib.oracle_set_art_visc_admis(ctypes.byref(self.desc), char_speed))

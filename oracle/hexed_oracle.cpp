@@ -71,6 +71,9 @@ struct K
   const hexed_mesh_desc& m;
   Tables t;
   double lift[RS][2];   // Derivative::lift (include/Derivative.hpp:22-28)
+  // true while Solver::fix_admissibility diffuses the state: the viscous kernels, Max_dt and
+  // the boundary conditions then compute pde::Fix_therm_admis (include/pde.hpp:437-493)
+  mutable bool fta = false;
   explicit K(const hexed_mesh_desc& mesh) : m{mesh}, t{tables(RS)}
   {
     for (int i = 0; i < RS; ++i) {
@@ -284,6 +287,7 @@ struct K
           avg1[v*nfq + q1] = avg;
         }
       }
+      if (fta) continue;   // Fix_therm_admis has no convection (Spatial.hpp:655-686)
       double n[ND];
       if (deformed) for (int d = 0; d < ND; ++d) n[d] = sign[0]*nrml[d*nfq + q];
       else for (int d = 0; d < ND; ++d) n[d] = (d == i_dim0) ? 1. : 0.;
@@ -302,8 +306,10 @@ struct K
         out1[v*nfq + q1] = sign[1]*flux;
       }
     }
-    std::memcpy(f0, out0, sizeof(out0));
-    std::memcpy(f1, out1, sizeof(out1));
+    if (!fta) {
+      std::memcpy(f0, out0, sizeof(out0));
+      std::memcpy(f1, out1, sizeof(out1));
+    }
     if (viscous) {
       std::memcpy(l0, avg0, sizeof(avg0));
       std::memcpy(l1, avg1, sizeof(avg1));
@@ -458,19 +464,30 @@ struct K
       for (int i = 0; i < ND; ++i) for (int j = 0; j < ND; ++j)
         nmat[j][i] = deformed ? nrml[(i*ND + j)*nq + q] : (i == j ? 1. : 0.);
       Conv c = scalars_conv(s);
-      for (int i = 0; i < ND; ++i) {
-        double col[ND], f[nv];
-        for (int j = 0; j < ND; ++j) col[j] = nmat[j][i];
-        flux_conv(s, c, col, f);
-        for (int v = 0; v < nv; ++v) flux[i][v][q] = f[v];
+      if (!fta) {
+        for (int i = 0; i < ND; ++i) {
+          double col[ND], f[nv];
+          for (int j = 0; j < ND; ++j) col[j] = nmat[j][i];
+          flux_conv(s, c, col, f);
+          for (int v = 0; v < nv; ++v) flux[i][v][q] = f[v];
+        }
       }
       if (viscous) {
         double g[nv][ND];
         for (int d = 0; d < ND; ++d) for (int v = 0; v < nv; ++v) g[v][d] = visc_storage[d][v][q];
         if (deformed) for (int v = 0; v < nv; ++v) for (int d = 0; d < ND; ++d) g[v][d] /= det[q];
-        Diff df = scalars_diff(s, c, visc, cond);
         double fd[nv][ND];
-        flux_diff(s, c, df, g, nmat, !deformed, fd);
+        if (fta) {
+          // Fix_therm_admis::compute_flux_diff (include/pde.hpp:481-485): -gradient*normal
+          for (int v = 0; v < nv; ++v) for (int i = 0; i < ND; ++i) {
+            double acc = 0.;
+            for (int j = 0; j < ND; ++j) acc += -g[v][j]*nmat[j][i];
+            fd[v][i] = acc;
+          }
+        } else {
+          Diff df = scalars_diff(s, c, visc, cond);
+          flux_diff(s, c, df, g, nmat, !deformed, fd);
+        }
         for (int d = 0; d < ND; ++d) for (int v = 0; v < nv; ++v) visc_storage[d][v][q] = fd[v][d];
       }
     }
@@ -480,12 +497,14 @@ struct K
       for (int i_fq = 0; i_fq < nfq; ++i_fq) {
         for (int v = 0; v < nv; ++v) {
           double row_f[RS], face_f[2], der[RS];
-          for (int i = 0; i < RS; ++i) row_f[i] = flux[d][v][row_qpoint(d, i_fq, i)];
-          for (int s = 0; s < 2; ++s) face_f[s] = faces[2*d + s][v*nfq + i_fq];
-          derivative(row_f, face_f, der);
-          for (int i = 0; i < RS; ++i) {
-            double& x = time_rate[0][v][row_qpoint(d, i_fq, i)];
-            x = 1.*x + -der[i];
+          if (!fta) {
+            for (int i = 0; i < RS; ++i) row_f[i] = flux[d][v][row_qpoint(d, i_fq, i)];
+            for (int s = 0; s < 2; ++s) face_f[s] = faces[2*d + s][v*nfq + i_fq];
+            derivative(row_f, face_f, der);
+            for (int i = 0; i < RS; ++i) {
+              double& x = time_rate[0][v][row_qpoint(d, i_fq, i)];
+              x = 1.*x + -der[i];
+            }
           }
           if (viscous) {
             for (int i = 0; i < RS; ++i) row_f[i] = visc_storage[d][v][row_qpoint(d, i_fq, i)];
@@ -533,7 +552,7 @@ struct K
         if (stage) {
           u -= ref_state[v*nq + q];
         } else {
-          ref_state[v*nq + q] = u;
+          if (!fta) ref_state[v*nq + q] = u;   // Pde::has_convection
           if (viscous) u += time_rate[1][v][q];
         }
         u *= mult;
@@ -691,8 +710,12 @@ struct K
         s[nv] = state[(nv + 1)*nq + q];
         s[nv + 1] = state[(nv + 2)*nq + q];
         double scale = 0;
-        scale += char_speed(s)/max_cfl_c/spacing;
-        if (viscous) {
+        if (fta) {
+          scale += 1./max_cfl_d/spacing/spacing;   // Fix_therm_admis: diffusivity 1, no convection
+        } else {
+          scale += char_speed(s)/max_cfl_c/spacing;
+        }
+        if (viscous && !fta) {
           Conv c = scalars_conv(s);
           Diff df = scalars_diff(s, c, visc, cond);
           double diffusivity = std::abs(df.laplacian_av) + std::max(std::abs(df.bulk_av) + df.mu/c.mass, df.energy_cond/c.mass);
@@ -855,6 +878,10 @@ struct K
     int ifs = (c[2] >> 2) & 1;
     double* in = slot(c[0], false);
     double* gh = slot(c[1], false);
+    if (fta) {   // Solver::fix_admissibility (src/Solver.cpp:1067-1072): ghost face = inside face
+      for (int k = 0; k < nv*nfq; ++k) gh[k] = in[k];
+      return;
+    }
     const double* nrml = m.bc_nrml + (size_t)i*ND*nfq;
     double* sc = m.bc_cache + (size_t)i*2*nv*nfq;
     switch (b.kind) {
@@ -934,6 +961,10 @@ struct K
     int ifs = (c[2] >> 2) & 1;
     double* in_l = slot(c[0], true);
     double* gh_l = slot(c[1], true);
+    if (fta) {   // Solver::apply_fta_flux_bcs (src/Solver.cpp:103-114)
+      for (int k = 0; k < nv*nfq; ++k) gh_l[k] = -in_l[k];
+      return;
+    }
     const double* nrml = m.bc_nrml + (size_t)i*ND*nfq;
     double* sc = m.bc_cache + (size_t)i*2*nv*nfq;
     double* fc = sc + nv*nfq;
@@ -1089,6 +1120,125 @@ struct K
     }
   }
 
+  // ---------------------------------------------------------------- admissibility
+  // Solver::is_admissible (src/Solver.cpp:921-959) with thermo::admissible (src/thermo.cpp:6-18):
+  // density and energy positive at every point of every element state, element face and
+  // fine mortar face; record[e] = 1 marks an inadmissible element. *finite = false if any value
+  // is not finite (the reference asserts there).
+  bool is_admissible(std::vector<int>& record, bool* finite) const
+  {
+    record.assign(n_elem(), 0);
+    bool admiss = true, fin = true;
+    auto check = [&](const double* data, int n_point, int stride) {
+      bool a = true;
+      for (int q = 0; q < n_point; ++q) {
+        a = a && (data[ND*stride + q] > 0.) && (data[(ND + 1)*stride + q] > 0.);
+        for (int v = 0; v < nv; ++v) fin = fin && std::isfinite(data[v*stride + q]);
+      }
+      return a;
+    };
+    for (int e = 0; e < n_elem(); ++e) {
+      bool ea = check(elem(e), nq, nq);
+      for (int i = 0; i < 2*ND; ++i) ea = check(face(e, i, false), nfq, nfq) && ea;
+      if (!ea) record[e] = 1;
+      admiss = admiss && ea;
+    }
+    for (int i = 0; i < m.n_ref_face; ++i) {
+      const int* rf = m.ref_face + 7*i;
+      int n_fine = nvert/2;
+      for (int d = 0; d < ND - 1; ++d) n_fine /= 1 + (rf[5 + d] != 0);
+      for (int k = 0; k < n_fine; ++k) admiss = check(slot(rf[1 + k], false), nfq, nfq) && admiss;
+    }
+    *finite = fin;
+    return admiss;
+  }
+
+  // std::swap of the bulk and Laplacian artificial-viscosity rows (src/Solver.cpp:1033-1039)
+  void swap_av() const
+  {
+    for (int e = 0; e < n_elem(); ++e) {
+      double* st = elem(e);
+      for (int q = 0; q < nq; ++q) std::swap(st[(nv + 1)*nq + q], st[(nv + 2)*nq + q]);
+    }
+  }
+
+  // Solver::fix_admissibility's coefficient (src/Solver.cpp:990-1032): each element's record on
+  // its vertices, vertex maximum, the maximum over each element's vertices, vertex maximum
+  // again, multilinear interpolation into the Laplacian AV row (skipped without a vertex table)
+  void fix_admis_coef(const std::vector<int>& record) const
+  {
+    if (m.n_vert <= 0 || !m.vert_id) return;
+    std::vector<double> vmax(m.n_vert, 0.), emax(n_elem());
+    for (int e = 0; e < n_elem(); ++e)
+      for (int v = 0; v < nvert; ++v) { double& x = vmax[m.vert_id[e*nvert + v]]; x = std::max(x, double(record[e])); }
+    for (int e = 0; e < n_elem(); ++e) {
+      double mx = 0.;
+      for (int v = 0; v < nvert; ++v) mx = std::max(mx, vmax[m.vert_id[e*nvert + v]]);
+      emax[e] = mx;
+    }
+    std::fill(vmax.begin(), vmax.end(), 0.);
+    for (int e = 0; e < n_elem(); ++e)
+      for (int v = 0; v < nvert; ++v) { double& x = vmax[m.vert_id[e*nvert + v]]; x = std::max(x, emax[e]); }
+    for (int e = 0; e < n_elem(); ++e) {
+      double* lap = elem(e) + (nv + 2)*nq;
+      for (int q = 0; q < nq; ++q) {
+        double vals[nvert];
+        for (int v = 0; v < nvert; ++v) vals[v] = vmax[m.vert_id[e*nvert + v]];
+        int n = nvert;
+        for (int d = ND - 1; d >= 0; --d) {
+          const double x = t.node[(q/ipow(RS, ND - 1 - d))%RS];
+          for (int i = 0; i < n/2; ++i) vals[i] = (1. - x)*vals[2*i] + x*vals[2*i + 1];
+          n /= 2;
+        }
+        lap[q] = vals[0];
+      }
+    }
+  }
+
+  // Solver::fix_admissibility (src/Solver.cpp:961-1095); returns the iteration count the
+  // reference returns, or -1 for a non-finite state and -2 past 100000 iterations (where the
+  // reference asserts). The flow's Max_dt closing each iteration uses the update parameters p.
+  int fix_admissibility(const hexed_update_params& p, double stability_ratio, double (*cheby)(int, int)) const
+  {
+    const hexed_transport inv{0., 0., 1., 1., 0};
+    std::vector<int> record;
+    int iter;
+    int n_iters = std::numeric_limits<int>::max();
+    for (iter = 0; iter < n_iters; ++iter) {
+      if (iter >= 100000) return -2;
+      bool finite;
+      const bool adm = is_admissible(record, &finite);
+      if (!finite) return -1;
+      if (adm) {
+        if (iter) n_iters = std::min(n_iters, 2*iter);
+        else {
+          ++iter;
+          break;
+        }
+      } else {
+        n_iters = std::numeric_limits<int>::max();
+      }
+      fix_admis_coef(record);
+      swap_av();
+      fta = true;
+      max_dt(true, stability_ratio, stability_ratio, true, inv, inv);
+      const double linear = 1., quadratic = 1./8/0.9;
+      double step[2];
+      step[1] = (linear + std::sqrt(linear*linear - 4*quadratic))/2.;
+      step[0] = quadratic/step[1];
+      for (double st : step) {
+        apply_state_bcs();
+        compute_navier_stokes(st, 0, false, false, inv, inv);
+      }
+      fta = false;
+      const double max_cheby = cheby(p.n_cheby_flow, p.n_cheby_flow - 1);
+      max_dt(p.use_ldg, p.max_safety/max_cheby, p.max_safety, p.local_time, p.visc, p.cond);
+      swap_av();
+    }
+    --iter;
+    return iter;
+  }
+
   // integral_field of Physical_residual^2 (src/Solver.cpp:1113-1131, src/Qpoint_func.cpp:37-45)
   void residual_norm(double* out) const
   {
@@ -1210,7 +1360,8 @@ int oracle_characteristics(int nd, const double* state, const double* normal, co
 // Solver::update (src/Solver.cpp:834-886); returns the last dt through *out_dt
 int oracle_update(const hexed_mesh_desc* m, const hexed_update_params* p, double* out_dt)
 {
-  return dispatch(m, [&](auto& k) {
+  int st = HEXED_OK;
+  int ds = dispatch(m, [&](auto& k) {
     double dt = 0.;
     for (int i_flow = 0; i_flow < p->flow_iters; ++i_flow) {
       double max_cheby = chebyshev_step(p->n_cheby_flow, p->n_cheby_flow - 1);
@@ -1220,15 +1371,36 @@ int oracle_update(const hexed_mesh_desc* m, const hexed_update_params* p, double
         double nominal = std::min(k.max_dt(p->use_ldg, p->max_safety/max_cheby, p->max_safety, p->local_time,
                                            p->visc, p->cond), p->max_time_step);
         dt = nominal*chebyshev_step(p->n_cheby_flow, i_cheby);
+        bool fixed = false;
         for (int i = 0; i < 2; ++i) {
           k.apply_state_bcs();
           if (p->use_ldg && !i) k.compute_navier_stokes(dt, i, false, p->use_filter, p->visc, p->cond);
           else k.compute_euler(dt, i, false, p->use_filter);
+          if (p->fix_admis) {   // src/Solver.cpp:866-867
+            int iters = k.fix_admissibility(*p, p->fix_admis_max_safety, chebyshev_step);
+            if (iters < 0) { st = HEXED_ERR_NUMERICAL; return; }
+            fixed = iters || fixed;
+          }
         }
+        if (fixed) break;
       }
     }
     if (out_dt) *out_dt = dt;
   });
+  return st != HEXED_OK ? st : ds;
+}
+
+// Solver::fix_admissibility (src/Solver.cpp:961-1095)
+int oracle_fix_admissibility(const hexed_mesh_desc* m, const hexed_update_params* p, double stability_ratio,
+                             int* iterations)
+{
+  int st = HEXED_OK;
+  int ds = dispatch(m, [&](auto& k) {
+    const int it = k.fix_admissibility(*p, stability_ratio, chebyshev_step);
+    if (it < 0) st = HEXED_ERR_NUMERICAL;
+    else *iterations = it;
+  });
+  return st != HEXED_OK ? st : ds;
 }
 
 // Solver::compute_residual (src/Solver.cpp:899-913)

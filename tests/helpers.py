@@ -129,3 +129,21 @@ def rotated_pair_case(nd, rs, direction, kind=abi.BC_RIEMANN, seed=0):
     spec = bc_spec(kind, freestream=fs, pressure=0.9e5)
     ar = general_mesh(nd, rs, verts, [1., 1.], [True, True], [(0, 1, i0, i1, s0, s1)], bounds, [spec])
     return smooth_state(ar, seed)
+
+
+def planted_inadmissible(kind):
+    """An admissible flow with a dip of negative energy at a few points of one element, its
+    face traces written: "cartesian" (2D vortex, Riemann boundaries) or "deformed" (3D
+    Taylor-Green, walls)."""
+    import oracle
+    from hexed_gb300 import problems
+    if kind == "cartesian":
+        ar = problems.vortex_2d(n_per_side=6, row_size=4)
+        e = 14
+    else:
+        ar = problems.taylor_green_3d(n_per_side=3, row_size=3)
+        e = 13
+    energy = ar.elem[e, ar.nv - 1]
+    energy[:3] = -0.05*np.abs(energy).mean()
+    oracle.Oracle(ar).write_face()
+    return ar
