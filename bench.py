@@ -138,8 +138,8 @@ def kernel_bytes(name, ar, precision="fp64"):
 NCU_DRAM_BYTES_PER_ELEM = {
     ("local_def_ns", "fp64", 6): 73281.,
     ("local_def_euler", "fp64", 6): 69966.,
-    ("local_def_ns", "mixed", 6): (479.844352e6 + 200.925952e6) / 13824,
-    ("local_def_euler", "mixed", 6): (453.252864e6 + 146.395392e6) / 13824,
+    ("local_def_ns", "mixed", 6): (490.465792e6 + 201.874944e6) / 13824,
+    ("local_def_euler", "mixed", 6): (514.078720e6 + 149.316096e6) / 13824,
 }
 
 
