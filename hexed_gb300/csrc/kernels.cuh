@@ -652,7 +652,10 @@ struct LocalSmemRows {
   static constexpr size_t state_bytes = sizeof(double)*(size_t)EPB*(S::nv + 3)*S::nq;
   static constexpr size_t nrm_offset = state_offset + (state_bytes + 15)/16*16;
   static constexpr size_t nrm_bytes = DEF ? sizeof(R)*(size_t)EPB*(ND*ND + 1)*S::nq : 0;
-  static constexpr size_t work_offset = nrm_offset + (nrm_bytes + 15)/16*16;
+  // [inviscid: residual cache, EPB x nv x nq in R (read by the second stage)]
+  static constexpr size_t rc_offset = nrm_offset + (nrm_bytes + 15)/16*16;
+  static constexpr size_t rc_bytes = VISC ? 0 : sizeof(R)*(size_t)EPB*S::nv*S::nq;
+  static constexpr size_t work_offset = rc_offset + (rc_bytes + 15)/16*16;
   static constexpr size_t bytes = work_offset + sizeof(R)*(size_t)per_elem*EPB;
 };
 
@@ -1178,7 +1181,13 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
   const FaceT* g_nrm = DEF ? m.nrm + (size_t)(e0 - m.n_car)*(ND*ND + 1)*nq : nullptr;
   const unsigned nrm_bytes = DEF ? unsigned(n_here*(ND*ND + 1)*nq*sizeof(FaceT)) : 0u;
   const bool bulk_n = DEF && bulk && ((reinterpret_cast<unsigned long long>(g_nrm) | nrm_bytes) & 15u) == 0;
-  if (bulk && threadIdx.x == 0) mbar_init(s_bar, bulk_n ? 2 : 1);
+  // the second stage's residual cache of inviscid elements ([n][nv][nq], contiguous)
+  R* s_rc = reinterpret_cast<R*>(smem_raw + L::rc_offset);
+  const FaceT* g_rc = m.rcache + (size_t)e0*nv*nq;
+  const unsigned rc_bytes = unsigned(n_here*nv*nq*sizeof(FaceT));
+  const bool bulk_rc = !VISC && stage && !compute_residual && bulk &&
+                       ((reinterpret_cast<unsigned long long>(g_rc) | rc_bytes) & 15u) == 0;
+  if (bulk && threadIdx.x == 0) mbar_init(s_bar, 1 + bulk_n + bulk_rc);
   if (threadIdx.x < EPB) {
     const int ee = e0 + threadIdx.x;
     const double dp = ee < e_end ? m.nom_size[ee] : 1.;
@@ -1188,6 +1197,7 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
   if (bulk && threadIdx.x == 0) {
     bulk_load(s_state, g_state, state_bytes, s_bar);
     if (bulk_n) bulk_load(s_n, g_nrm, nrm_bytes, s_bar);
+    if (bulk_rc) bulk_load(s_rc, g_rc, rc_bytes, s_bar);
   }
   if (threadIdx.x == 32) prefetch_element_arrays<ND, RS, DEF, VISC>(m, e0, n_here, stage);
   const int ed = e - m.n_car;
@@ -1504,7 +1514,7 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
       for (int v = 0; v < nv; ++v) {
         R ur = rate[v];
         if (stage) {
-          ur -= R(rc[v*nq + q]);
+          ur -= (bulk_rc && staged) ? s_rc[(le*nv + v)*nq + q] : R(rc[v*nq + q]);
         } else {
           if (!(VISC && m.fta)) rc[v*nq + q] = FaceT(ur);
           if constexpr (VISC) ur += vrate[v];
@@ -2391,8 +2401,17 @@ k_max_dt(Dev<FaceT> m, Tab<RS> tab, R inv_cfl_c, R inv_cfl_d, int local_time, Tm
 static __global__ void k_finalize_dt(double* scalars, const double* partials, int n_part, int local_time,
                               double max_time_step, double cheby)
 {
-  double x = 1.7976931348623157e308;
-  for (int i = threadIdx.x; i < n_part; i += blockDim.x) x = fmin(x, partials[i]);
+  // four independent running minima per thread, so the partials' loads overlap
+  double x = 1.7976931348623157e308, x1 = x, x2 = x, x3 = x;
+  int i = threadIdx.x;
+  for (; i + 3*(int)blockDim.x < n_part; i += 4*blockDim.x) {
+    x = fmin(x, partials[i]);
+    x1 = fmin(x1, partials[i + blockDim.x]);
+    x2 = fmin(x2, partials[i + 2*blockDim.x]);
+    x3 = fmin(x3, partials[i + 3*blockDim.x]);
+  }
+  for (; i < n_part; i += blockDim.x) x = fmin(x, partials[i]);
+  x = fmin(fmin(x, x1), fmin(x2, x3));
   __shared__ double s_min[32];
   for (int o = 16; o > 0; o >>= 1) x = fmin(x, __shfl_xor_sync(0xffffffffu, x, o));
   if ((threadIdx.x & 31) == 0) s_min[threadIdx.x >> 5] = x;

@@ -290,7 +290,7 @@ struct Runner
       else k_max_dt<ND, RS, R, false, FaceT><<<grid, 256, 0, c.stream>>>(dev(c), tab(c), icc, icd, local_time, make_tm<R>(visc), make_tm<R>(cond), c.partials);
     }
     ProfScope ps(c, "finalize_dt");
-    k_finalize_dt<<<1, 256, 0, c.stream>>>(c.scalars, c.partials, grid, local_time, max_time_step, cheby);
+    k_finalize_dt<<<1, 1024, 0, c.stream>>>(c.scalars, c.partials, grid, local_time, max_time_step, cheby);
   }
 
   static void write_face(Ctx& c, int e_begin, int n_elem)
