@@ -647,8 +647,10 @@ struct LocalSmemRows {
   static constexpr int per_elem = S::nv*S::nq + ND*S::nv*S::nq + (VISC ? (ND + 1)*S::nv*S::nq : 0);
   // [mbarrier, 16 B][1/element size, EPB x R][element states, EPB x (nv + 3) x nq doubles]
   // [deformed: metric normals and determinant, EPB x (nd^2 + 1) x nq in R][work]
+  // [each element's reference state and its derived terms (RefState), EPB of them]
   static constexpr size_t idp_offset = 16;
-  static constexpr size_t state_offset = idp_offset + (sizeof(R)*EPB + 15)/16*16;
+  static constexpr size_t ref_offset = idp_offset + (sizeof(R)*EPB + 15)/16*16;
+  static constexpr size_t state_offset = ref_offset + (sizeof(RefState<ND, R>)*EPB + 15)/16*16;
   static constexpr size_t state_bytes = sizeof(double)*(size_t)EPB*(S::nv + 3)*S::nq;
   static constexpr size_t nrm_offset = state_offset + (state_bytes + 15)/16*16;
   static constexpr size_t nrm_bytes = DEF ? sizeof(R)*(size_t)EPB*(ND*ND + 1)*S::nq : 0;
@@ -1159,6 +1161,7 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned long long* s_bar = reinterpret_cast<unsigned long long*>(smem_raw);
   R* s_idp = reinterpret_cast<R*>(smem_raw + L::idp_offset);
+  RefState<ND, R>* s_ref = reinterpret_cast<RefState<ND, R>*>(smem_raw + L::ref_offset);
   double* s_state = reinterpret_cast<double*>(smem_raw + L::state_offset);
   R* s_n = reinterpret_cast<R*>(smem_raw + L::nrm_offset);   // deformed: [EPB][nd^2 + 1][nq]
   R* s_u = reinterpret_cast<R*>(smem_raw + L::work_offset);
@@ -1192,6 +1195,8 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
     const int ee = e0 + threadIdx.x;
     const double dp = ee < e_end ? m.nom_size[ee] : 1.;
     s_idp[threadIdx.x] = split ? R(1)/to_R<R>(dp) : R(1./dp);
+    // the element's reference state in the compute type, formed once instead of per point
+    if constexpr (split) if (ee < e_end) s_ref[threadIdx.x].set(m.ref + (size_t)ee*nv);
   }
   __syncthreads();
   if (bulk && threadIdx.x == 0) {
@@ -1221,13 +1226,12 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
 
   R u[nv + 2];   // state + bulk AV + Laplacian AV (include/pde.hpp:79-84)
   R up[nv];      // offset form of the state
-  const double* ref_e = split ? m.ref + (size_t)(active ? e : 0)*nv : nullptr;
   if (active) {
     #pragma unroll
     for (int v = 0; v < nv; ++v) {
       const double x = state_g[v*nq + q];
       up[v] = offset_var<ND, R>(m, e, v, x);
-      if constexpr (split) u[v] = to_R<R>(ref_e[v]) + up[v];
+      if constexpr (split) u[v] = s_ref[le].s[v] + up[v];
       else u[v] = R(x);
     }
     u[nv] = to_R<R>(state_g[(nv + 1)*nq + q]);
@@ -1330,8 +1334,8 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
   // overwrites only its own gradient entries)
   if (active) {
     Conv<ND, R> c(u);
-    RefState<ND, R> rs;   // formed here, not kept live through the gradient part
-    if constexpr (split) rs.set(ref_e);
+    RefState<ND, R> rs;   // read here, not kept live through the gradient part
+    if constexpr (split) rs = s_ref[le];
     R nrm[ND][ND]; // nrm[j][i] = comp.normal(j, i)
     #pragma unroll
     for (int i = 0; i < ND; ++i)
