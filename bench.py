@@ -464,7 +464,9 @@ def main():
     f0.record(stream)
     t0 = time.perf_counter()
     for _ in range(args.steps):
+        # a new state from the host, its face traces (Solver::initialize), one update, read back
         abi.check(lib.hexed_gpu_write_state(ctx.handle, abi.ctypes.cast(host_in.data_ptr(), abi.P_double)))
+        initialize(ctx)
         ctx.update(p, read_dt=False)
         abi.check(lib.hexed_gpu_read_state(ctx.handle, abi.ctypes.cast(host_out.data_ptr(), abi.P_double)))
     f1.record(stream)
