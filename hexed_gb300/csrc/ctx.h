@@ -48,6 +48,7 @@ struct OpsTable {
   void (*admissible)(Ctx&, int* d_record);
   void (*compute_jacobian)(Ctx&, const double* d_vert_pos, double* d_fn, double* d_vtss);
   void (*fix_admis_coef)(Ctx&, const int* d_record, bool swap_only);
+  void (*ref_terms)(Ctx&);
 };
 
 // A captured multi-update sequence and the inputs it was captured for.
@@ -95,6 +96,9 @@ struct Ctx {
   // mean conserved state of the initial state)
   float* face_f; float* rcache_f; float* nrm_f; float* face_nrml_f; float* def_con_nrml_f; float* bc_nrml_f;
   double* ref_state;
+  // its terms in float for the offset fluxes (RefState: state, velocity, |v|^2, enthalpy),
+  // [n_elem][2 nd + 4], refreshed whenever ref_state changes
+  float* ref_terms;
   int* record;           // per-element admissibility records [cap elements] (allocated at creation)
   // launch shape: volume-kernel variant (elements per CTA, see Runner::epb_of) and threads
   // per CTA of the face kernels

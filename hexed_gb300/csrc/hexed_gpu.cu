@@ -207,6 +207,7 @@ int refresh_metric_copies(Ctx* c, int which, long offset, long count)
   if (which == HEXED_ARRAY_BC_NRML) narrow(c->bc_nrml, c->bc_nrml_f);
   if (which == HEXED_ARRAY_FACE_NRML) narrow(c->face_nrml, c->face_nrml_f);
   if (which == HEXED_ARRAY_DEF_CON_NRML) narrow(c->def_con_nrml, c->def_con_nrml_f);
+  if (which == HEXED_ARRAY_REF_STATE) c->ops->ref_terms(*c);
   if (which == HEXED_ARRAY_JAC) {
     narrow(c->jac, c->nrm_f);
     if (c->n_def)
@@ -421,6 +422,9 @@ int hexed_gpu_create(const hexed_mesh_desc* d, int precision, hexed_gpu_ctx** ou
     for (size_t e = 0; e < n_elem; ++e)
       for (size_t v = 0; v < nv_; ++v) refs[e*nv_ + v] = mean[v];
     if (!st) st = upload_array(&c->ref_state, refs.data(), refs.size(), "reference state");
+    if (!st && cudaMalloc((void**)&c->ref_terms, n_elem*(2*nd + 4)*sizeof(float)) != cudaSuccess)
+      st = fail(HEXED_ERR_ALLOC, "reference-term allocation failed");
+    if (!st) c->ops->ref_terms(*c);
   }
   if (!st && c->n_def) {
     if (cudaMalloc((void**)&c->inv_det, (size_t)c->n_def*c->nq*sizeof(double)) != cudaSuccess) {
@@ -458,7 +462,7 @@ int hexed_gpu_destroy(hexed_gpu_ctx* c)
                   c->def_con, c->def_con_nrml, c->bc_con, c->bc_nrml, c->bc_cache, c->ref_face, c->bc_spec,
                   c->scalars, c->partials, c->status, c->d_norm, c->vert_id, c->uncert, c->vmax,
                   c->seg_table, c->seg_out, c->inv_det, c->face_f, c->rcache_f, c->nrm_f, c->face_nrml_f,
-                  c->def_con_nrml_f, c->bc_nrml_f, c->ref_state, c->record};
+                  c->def_con_nrml_f, c->bc_nrml_f, c->ref_state, c->ref_terms, c->record};
   for (void* p : ptrs) if (p) cudaFree(p);
   if (c->graph) {
     if (c->graph->exec) cudaGraphExecDestroy(c->graph->exec);
@@ -676,6 +680,8 @@ int hexed_gpu_set_reference_state(hexed_gpu_ctx* c, const double* state)
   for (size_t e = 0; e < n; ++e)
     for (size_t v = 0; v < c->nv; ++v) refs[e*c->nv + v] = state[v];
   HX_CUDA(cudaMemcpyAsync(c->ref_state, refs.data(), refs.size()*sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  c->ops->ref_terms(*c);
+  HX_LAUNCHED();
   HX_CUDA(cudaStreamSynchronize(c->stream));
   return HEXED_OK;
 }

@@ -70,6 +70,7 @@ struct Dev {
   // Mixed form: reference state of each element [n_elem][nv]; its face traces, and the
   // fluxes its kernels form, are differences from it (see RefState). Null in the FP64 form.
   const double* ref;
+  const float* ref_terms;   // mixed form: RefState<ND, float> of each element
   double* scalars;       // [0] dt of the current stage, [1] raw max_dt, ...
   double* partials;      // per-block reduction scratch
   int* status;           // device-side error flags
@@ -222,6 +223,14 @@ struct RefState {
     h = s[ND + 1] + R(heat_rat - 1.)*(s[ND + 1] - R(.5)*s[ND]*v_sq);
   }
 };
+
+// RefState<ND, float> of every element from its double reference state
+template <int ND>
+__global__ void k_ref_terms(const double* ref, int n_elem, RefState<ND, float>* out)
+{
+  for (int e = blockIdx.x*blockDim.x + threadIdx.x; e < n_elem; e += gridDim.x*blockDim.x)
+    out[e].set(ref + (size_t)e*(ND + 2));
+}
 
 // f(u).n - f(u_ref).n of the convective flux (pde.hpp:108-122) from the offset state
 // d = u - u_ref, with c the Conv of the full state u. Every term is an offset times a bounded
@@ -1196,7 +1205,7 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
     const double dp = ee < e_end ? m.nom_size[ee] : 1.;
     s_idp[threadIdx.x] = split ? R(1)/to_R<R>(dp) : R(1./dp);
     // the element's reference state in the compute type, formed once instead of per point
-    if constexpr (split) if (ee < e_end) s_ref[threadIdx.x].set(m.ref + (size_t)ee*nv);
+    if constexpr (split) if (ee < e_end) s_ref[threadIdx.x] = reinterpret_cast<const RefState<ND, R>*>(m.ref_terms)[ee];
   }
   __syncthreads();
   if (bulk && threadIdx.x == 0) {
@@ -1698,7 +1707,7 @@ __device__ __forceinline__ void neighbor_point(const Dev<FaceT>& m, int slot0, i
   if constexpr (split) {
     const int n_elem_slots = m.n_elem*2*ND;
     e_ref = slot0 < n_elem_slots ? slot0/(2*ND) : slot1 < n_elem_slots ? slot1/(2*ND) : 0;
-    rs.set(m.ref + (size_t)e_ref*nv);
+    rs = reinterpret_cast<const RefState<ND, R>*>(m.ref_terms)[e_ref];
   }
   const bool deformed = nrml != nullptr;
   int sign0 = 1, sign1 = 1;

@@ -40,10 +40,12 @@ struct Runner
       m.rcache = c.rcache; m.face = c.face; m.nrm = c.jac; m.face_nrml = c.face_nrml;
       m.def_con_nrml = c.def_con_nrml; m.bc_nrml_t = c.bc_nrml;
       m.ref = nullptr;
+      m.ref_terms = nullptr;
     } else {
       m.rcache = c.rcache_f; m.face = c.face_f; m.nrm = c.nrm_f; m.face_nrml = c.face_nrml_f;
       m.def_con_nrml = c.def_con_nrml_f; m.bc_nrml_t = c.bc_nrml_f;
       m.ref = c.ref_state;
+      m.ref_terms = c.ref_terms;
     }
     return m;
   }
@@ -352,6 +354,14 @@ struct Runner
     k_swap_av<ND, RS><<<grid_for((long)n_elem*S::nq, 256), 256, 0, c.stream>>>(c.elem, n_elem);
   }
 
+  // RefState terms of every element, after the reference state changed (mixed form)
+  static void ref_terms(Ctx& c)
+  {
+    const int n = c.cap_car + c.n_def;
+    if (c.ref_state && c.ref_terms && n > 0)
+      k_ref_terms<ND><<<grid_for(n, 256), 256, 0, c.stream>>>(c.ref_state, n, reinterpret_cast<RefState<ND, float>*>(c.ref_terms));
+  }
+
   static void segment_residual_norms(Ctx& c, int n_seg, const int* d_begin, const int* d_count, double* d_out)
   {
     ProfScope ps(c, "segment_residual");
@@ -363,7 +373,7 @@ struct Runner
     static const OpsTable t = {
       compute_euler, compute_navier_stokes, max_dt, refine, write_face, bc_state, bc_flux, residual_norm,
       set_art_visc_admis, segment_residual_norms, local_elems_per_cta, admissible, compute_jacobian,
-      fix_admis_coef,
+      fix_admis_coef, ref_terms,
     };
     return &t;
   }
