@@ -564,8 +564,6 @@ __device__ __forceinline__ void write_faces_points(const Dev<FaceT>& m, const ST
   }
 }
 
-// ------------------------------------------------------------------- Local
-// Spatial::Local (include/Spatial.hpp:326-509) fused with the stage update and Write_face.
 // ------------------------------------------------------------------- bulk async copies
 // One-dimensional bulk copy (TMA) of `bytes` contiguous bytes from global to shared memory,
 // completing on an mbarrier, and the bounded wait for it. Both addresses and `bytes` must be
@@ -631,6 +629,8 @@ __device__ __forceinline__ void prefetch_element_arrays(const Dev<FaceT>& m, int
 // read global memory instead
 constexpr int flag_bulk_wait = 1;
 
+// ------------------------------------------------------------------- Local
+// Spatial::Local (include/Spatial.hpp:326-509) fused with the stage update and Write_face.
 template <int ND, int RS, typename R, bool DEF, bool VISC, int EPB = Shape<ND, RS>::epb>
 struct LocalSmemPoints {
   using S = Shape<ND, RS>;

@@ -133,17 +133,23 @@ def rotated_pair_case(nd, rs, direction, kind=abi.BC_RIEMANN, seed=0):
 
 def planted_inadmissible(kind):
     """An admissible flow with a dip of negative energy at a few points of one element, its
-    face traces written: "cartesian" (2D vortex, Riemann boundaries) or "deformed" (3D
-    Taylor-Green, walls)."""
+    face traces (and hanging-face mortars) written: "cartesian" (2D vortex, Riemann
+    boundaries), "deformed" (3D Taylor-Green, walls) or "tree" (3D pulse on a tree mesh with
+    hanging faces)."""
     import oracle
     from hexed_gb300 import problems
     if kind == "cartesian":
         ar = problems.vortex_2d(n_per_side=6, row_size=4)
         e = 14
+    elif kind == "tree":
+        ar = problems.pulse_tree_3d(n_base=2, row_size=3, levels=1)
+        e = 5
     else:
         ar = problems.taylor_green_3d(n_per_side=3, row_size=3)
         e = 13
     energy = ar.elem[e, ar.nv - 1]
     energy[:3] = -0.05*np.abs(energy).mean()
-    oracle.Oracle(ar).write_face()
+    o = oracle.Oracle(ar)
+    o.write_face()
+    o.prolong()
     return ar

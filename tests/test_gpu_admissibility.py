@@ -51,7 +51,7 @@ def test_hanging_face_mortars_checked():
         assert c.is_admissible()
 
 
-@pytest.mark.parametrize("kind", ["cartesian", "deformed"])
+@pytest.mark.parametrize("kind", ["cartesian", "deformed", "tree"])
 def test_fix_admissibility_matches_oracle(kind):
     """The Fix_therm_admis diffusion loop: same iteration count as the oracle and the same
     state (and artificial-viscosity rows, which the loop rewrites) to the FP64 bar."""

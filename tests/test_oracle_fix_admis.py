@@ -37,7 +37,7 @@ def admissible(ar):
     return bool((ar.elem[:, nd] > 0).all() and (ar.elem[:, nd + 1] > 0).all())
 
 
-@pytest.mark.parametrize("kind", ["cartesian", "deformed"])
+@pytest.mark.parametrize("kind", ["cartesian", "deformed", "tree"])
 def test_fix_restores_admissibility(kind):
     ar = planted(kind)
     assert not admissible(ar)
