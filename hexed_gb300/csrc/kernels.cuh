@@ -466,17 +466,16 @@ __device__ __forceinline__ void bound_dot(const RowTab<RS, R>& t, const R (&x)[R
 }
 
 // (D.x)_i + lift_i.(b0, b1): Derivative::operator() at node i, with b_s the face value minus
-// the extrapolated row (include/Derivative.hpp:56-60)
+// the extrapolated row (include/Derivative.hpp:56-60). One FMA chain, lift terms first: the
+// row-task body is the float form's, whose sums need not follow the reference's order.
 template <int RS, typename R>
 __device__ __forceinline__ R row_deriv(const RowTab<RS, R>& t, const R (&x)[RS], int i, R b0, R b1)
 {
-  R acc = 0;
+  R acc = t.lift[i*2]*b0;
+  acc += t.lift[i*2 + 1]*b1;
   #pragma unroll
   for (int k = 0; k < RS; ++k) acc += t.diff[i*RS + k]*x[k];
-  R l = 0;
-  l += t.lift[i*2]*b0;
-  l += t.lift[i*2 + 1]*b1;
-  return acc + l;
+  return acc;
 }
 
 // Calls f(std::integral_constant<int, I>()) for I = 0 .. N-1 in order.
@@ -1153,7 +1152,8 @@ __device__ __forceinline__ void local_body_points(Dev<FaceT> m, const Tab<RS>& t
 
 // Spatial::Local (include/Spatial.hpp:326-509). Point work (state, fluxes, stage update) runs
 // one thread per quadrature point; the line contractions run as row tasks over the CTA's
-// shared-memory fields. The arithmetic of every output is that of Derivative, in its order.
+// shared-memory fields. Every output is Derivative's, each contraction one FMA chain
+// (row_deriv).
 template <int ND, int RS, typename R, bool DEF, bool VISC, typename FaceT, int EPB>
 __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab, const RowTab<RS, R>& rt,
                                                 int e_begin, int e_end, int stage, int compute_residual, int use_filter,
