@@ -545,8 +545,18 @@ def main():
         mprof = mctx.profile_read()
         mctx.close()
         mvalue = dofs_per_update(ar) * args.steps / (mms / 1e3) / 1e9
+        # HBM roofline of the mixed form's dominant kernel, as for the headline
+        mtop, (mlaunches, mtop_ms) = max(mprof.items(), key=lambda kv: kv[1][1])
+        mlaunch_ms = mtop_ms / max(mlaunches, 1)
+        mbytes = kernel_bytes(mtop, ar, "mixed")
+        machieved = mbytes / (mlaunch_ms * 1e-3) / 1e9 if mbytes else None
+        mper_elem = NCU_DRAM_BYTES_PER_ELEM.get((mtop, "mixed", wl.rs)) if wl.kind == "tgv" else None
+        mroof = {"bound": "hbm", "kernel": mtop, "achieved": machieved, "peak": hbm_peak, "unit": "GB/s",
+                 "frac": machieved / hbm_peak if machieved else None, "algorithmic_bytes_per_launch": mbytes,
+                 "launch_ms": mlaunch_ms,
+                 "traffic": mper_elem * (ar.n_def if "def" in mtop else ar.n_car) if mper_elem else None}
         mixed = {"value": mvalue, "unit": "GDOF/s", "ms_per_step": mms / args.steps, "speedup_vs_fp64": mvalue / value,
-                 "dtype": "f32/f64",
+                 "dtype": "f32/f64", "roofline": mroof,
                  "kernels": {k: {"launches": v[0], "total_ms": round(v[1], 4)}
                              for k, v in sorted(mprof.items(), key=lambda kv: -kv[1][1])},
                  "error_vs_fp64": mixed_vs_fp64(wl, args.err_steps) if args.err_steps > 0 else None}

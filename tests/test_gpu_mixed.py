@@ -57,6 +57,18 @@ def test_mixed_euler_and_bcs(deformed):
         check(ar, abi.update_params(max_safety=0.5), 20, 1e-6)
 
 
+@pytest.mark.parametrize("nd,rs", [(2, 2), (2, 5), (2, 8), (3, 2), (3, 3), (3, 5), (3, 7), (3, 8)])
+def test_mixed_row_sizes(nd, rs):
+    """Every row size's float kernels (odd point counts take the unaligned-copy paths) on a
+    deformed mesh, viscous: the state after 5 updates against FP64."""
+    from helpers import air_transport
+    ar = deformed_case(nd, rs, 2 if nd == 3 else 3, abi.BC_NONPENETRATION)
+    rng = np.random.default_rng(rs)
+    ar.elem[:, ar.nv + 2] = rng.uniform(0, 1e-3, size=ar.elem[:, 0].shape)   # Laplacian AV
+    visc, cond = air_transport()
+    check(ar, abi.update_params(max_safety=0.5, visc=visc, cond=cond), 5, 1e-6)
+
+
 def test_mixed_rotated_connections():
     for d in list(all_directions(3))[::5]:
         ar = rotated_pair_case(3, 3, d)

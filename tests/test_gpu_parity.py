@@ -10,6 +10,13 @@ from helpers import FP64_TOL, air_transport, cartesian_case, compare_arenas, def
 
 pytestmark = pytest.mark.gpu
 
+# After several viscous updates the LDG face slots hold Neighbor_reconcile outputs,
+# sign*avg - own flux: differences of nearly equal viscous fluxes, whose relative error
+# is the roundoff of the fluxes amplified by the cancellation (FMA contraction on the GPU
+# vs none in the oracle). The quantities the solver reports -- state, time step and
+# residual norms -- stay at the 1e-12 bar; the face/cache scratch gets 1e-10.
+SCRATCH_TOL = 1e-10
+
 
 def run_pair(ar, op_oracle, op_gpu, precision=abi.FP64):
     a = ar.copy()
@@ -53,7 +60,8 @@ def test_boundary_conditions(kind, deformed):
     assert_close(a, b)
 
 
-@pytest.mark.parametrize("nd,rs,n", [(2, 4, 5), (2, 6, 4), (3, 3, 3), (3, 4, 2), (3, 6, 2)])
+@pytest.mark.parametrize("nd,rs,n", [(2, 4, 5), (2, 6, 4), (2, 7, 3), (3, 3, 3), (3, 4, 2), (3, 5, 2), (3, 6, 2),
+                                     (3, 8, 1)])
 @pytest.mark.parametrize("deformed", [False, True])
 @pytest.mark.parametrize("stage", [0, 1])
 @pytest.mark.parametrize("use_filter", [False, True])
@@ -76,7 +84,8 @@ def test_compute_euler(nd, rs, n, deformed, stage, use_filter):
     assert_close(a, b)
 
 
-@pytest.mark.parametrize("nd,rs,n", [(2, 4, 4), (3, 3, 3), (3, 4, 2), (3, 6, 2)])
+@pytest.mark.parametrize("nd,rs,n", [(2, 4, 4), (2, 8, 3), (3, 3, 3), (3, 4, 2), (3, 5, 2), (3, 6, 2), (3, 7, 1),
+                                     (3, 8, 1)])
 @pytest.mark.parametrize("deformed", [False, True])
 @pytest.mark.parametrize("residual", [False, True])
 def test_compute_navier_stokes(nd, rs, n, deformed, residual):
@@ -96,7 +105,18 @@ def test_compute_navier_stokes(nd, rs, n, deformed, residual):
         c.apply_state_bcs()
         c.compute_navier_stokes(1e-6, 0, visc, cond, residual)
     a, b, _ = run_pair(ar, o_op, g_op)
-    assert_close(a, b)
+    if rs <= 6:
+        assert_close(a, b)
+    else:
+        # Row sizes 7 and 8: the LDG face slots and the boundary flux cache hold the viscous
+        # flux extrapolated from gradients whose 1-D operators have entries up to ~50, so
+        # FMA-contraction roundoff there reaches ~1e-12 (see SCRATCH_TOL below); the state,
+        # time step, residual cache and traces stay at the FP64 bar.
+        errs, bad = compare_arenas(a, b, FP64_TOL, what=("elem", "rcache"))
+        assert not bad, errs
+        errs, bad = compare_arenas(a, b, SCRATCH_TOL)
+        assert not bad, errs
+        assert errs["face"] <= FP64_TOL, errs
 
 
 @pytest.mark.parametrize("viscous", [False, True])
@@ -137,14 +157,6 @@ def test_update_vortex_2d():
     assert_close(a, b)
     np.testing.assert_allclose(dts["g"], dts["o"], rtol=FP64_TOL)
     np.testing.assert_allclose(dts["gn"], dts["on"], rtol=1e-11)
-
-
-# After several viscous updates the LDG face slots hold Neighbor_reconcile outputs,
-# sign*avg - own flux: differences of nearly equal viscous fluxes, whose relative error
-# is the roundoff of the fluxes amplified by the cancellation (FMA contraction on the GPU
-# vs none in the oracle). The quantities the solver reports -- state, time step and
-# residual norms -- stay at the 1e-12 bar; the face/cache scratch gets 1e-10.
-SCRATCH_TOL = 1e-10
 
 
 def test_update_taylor_green_small():
