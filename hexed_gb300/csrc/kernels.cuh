@@ -1607,18 +1607,11 @@ k_reconcile_ldg(Dev<FaceT> m, Tab<RS> tab, RowTab<RS, R> rt, int e_begin, int e_
   R tr[nv];
   #pragma unroll
   for (int v = 0; v < nv; ++v) tr[v] = 0;
-  int node_of[ND], base_of[ND];
-  #pragma unroll
-  for (int d = 0; d < ND; ++d) {
-    const int stride = S::stride(d);
-    node_of[d] = (q/stride)%RS;
-    base_of[d] = q - node_of[d]*stride;
-  }
   if (active) {
     #pragma unroll
     for (int d = 0; d < ND; ++d) {
       const int stride = S::stride(d);
-      const int i = node_of[d];
+      const int i = (q/stride)%RS;
       const int r = (q/(stride*RS))*stride + q%stride;
       const FaceT* fl = m.face + (size_t)(e*2*ND + 2*d)*S::slot_dof + nv*nfq + r;
       #pragma unroll
@@ -1642,11 +1635,14 @@ k_reconcile_ldg(Dev<FaceT> m, Tab<RS> tab, RowTab<RS, R> rt, int e_begin, int e_
       }
       __syncthreads();
       if (active) {
+        // the node and row start of this thread's point along d, formed here: arrays of them
+        // indexed by this loop's d would sit in local memory
         const int stride = S::stride(d);
-        const int i = node_of[d];
+        const int i = (q/stride)%RS;
+        const int base = q - i*stride;
         #pragma unroll
         for (int v = 0; v < nv; ++v) {
-          const R* row = my_t + v*nq + base_of[d];
+          const R* row = my_t + v*nq + base;
           R acc = 0;
           #pragma unroll
           for (int j = 0; j < RS; ++j) acc += st.filter[i*RS + j]*row[j*stride];
@@ -2542,61 +2538,97 @@ static __global__ void k_fp64_fma(double* out, int iters, double a)
 
 // ------------------------------------------------------------------- artificial viscosity
 // Stab_art_visc (src/stabilizing_art_visc.cpp:26-60): per-element smoothness indicator of the
-// specific volume. One thread per quadrature point: each forms its term of the norm and,
-// for the first nd*nfq points, the squared projection of one row onto the highest Legendre
-// mode; the element's threads then reduce both sums as a tree in shared memory (the
-// reference sums in sequence: the two orders differ in the last bits).
-template <int ND, int RS>
-__global__ void __launch_bounds__(Shape<ND, RS>::threads)
-k_av_uncert(const double* elem, const double* nom_size, int n_elem, Tab<RS> tab, double char_speed, double* uncert)
+// specific volume. One warp per element, with no block-wide barrier past the tables: each lane
+// takes the points lane, lane + 32, ..., stores their specific volumes in the warp's shared row
+// and sums their terms of the norm; after a warp barrier the lanes take the nd*nfq rows the same
+// way, each row's squared projection onto the highest Legendre mode; the warp then reduces both
+// sums by shuffles
+// (the reference sums in sequence: the two orders differ in the last bits). R is the type of the
+// terms and sums: double in the FP64 form, float in the mixed form, whose coefficient only has to
+// hold the mixed form's tolerance.
+constexpr int av_warps = 8;   // elements per CTA of k_av_uncert
+
+// The basis values the artificial-viscosity kernels use, already in their type R (rounded to
+// nearest on the host for the mixed form), so that no conversion runs per point or per row:
+// w = quadrature weights, ow = highest orthonormal Legendre mode times the weight, node = nodes.
+template <int RS, typename R>
+struct AvTab { R w[RS]; R ow[RS]; R node[RS]; };
+
+// The indicator's ramp in log10 of the non-smoothness (src/stabilizing_art_visc.cpp:47-55):
+// centre -4.25 log10(row_size - 1), half width 0.5; lo and hi are 10^(centre -+ half width),
+// the ratio's bounds below and above which the indicator is 0 and 1.
+struct AvRamp { double center, half_width, lo, hi; };
+
+template <int ND, int RS, typename R>
+__global__ void __launch_bounds__(av_warps*32)
+k_av_uncert(const double* elem, const double* nom_size, int n_elem, AvTab<RS, R> tab, double char_speed, AvRamp ramp,
+            double* uncert)
 {
   using S = Shape<ND, RS>;
-  constexpr int nq = S::nq, nfq = S::nfq, nv = S::nv, EPB = S::epb;
-  __shared__ double s_iv[EPB*nq];
-  __shared__ double s_norm[EPB*nq];
-  __shared__ double s_rough[EPB*nq];
-  const int le = threadIdx.x/nq, q = threadIdx.x%nq;
-  const int e = blockIdx.x*EPB + le;
-  const bool in_cta = threadIdx.x < EPB*nq;
-  const bool active = in_cta && e < n_elem;
-  if (in_cta) s_iv[le*nq + q] = active ? 1./elem[(size_t)e*(nv + 3)*nq + ND*nq + q] : 0.;
-  __syncthreads();
-  const double* iv = s_iv + le*nq;
-  double tn = 0., tr = 0.;
-  if (active) {
-    double w = 1.;
-    for (int d = 0; d < ND; ++d) w *= tab.weight[(q/ipow(RS, ND - 1 - d))%RS];
-    tn = iv[q]*iv[q]*w;
-    if (q < ND*nfq) {
-      const int d = q/nfq, r = q%nfq;
-      const int stride = S::stride(d);
-      const double* row = iv + (r/stride)*stride*RS + r%stride;
-      double dot = 0.;
-      for (int i = 0; i < RS; ++i) dot += row[i*stride]*(tab.ortho_last[i]*tab.weight[i]);
-      double fw = 1.;
-      for (int k = 0; k < ND - 1; ++k) fw *= tab.weight[(r/ipow(RS, ND - 2 - k))%RS];
-      tr = dot*dot*fw;
-    }
+  constexpr int nq = S::nq, nfq = S::nfq, nv = S::nv;
+  constexpr int ppl = (nq + 31)/32;   // points per lane
+  __shared__ R s_iv[av_warps][nq];
+  __shared__ R s_w[RS], s_ow[RS];
+  // the tables go to shared memory by constant indices: indexing the parameter by a lane's
+  // point would copy it to local memory in every thread
+  if (threadIdx.x == 0) {
+    #pragma unroll
+    for (int i = 0; i < RS; ++i) { s_w[i] = tab.w[i]; s_ow[i] = tab.ow[i]; }
   }
-  if (in_cta) { s_norm[le*nq + q] = tn; s_rough[le*nq + q] = tr; }
-  __syncthreads();
-  constexpr int top = nq <= 1 ? 1 : 1 << (32 - __builtin_clz(nq - 1));   // power of two >= nq
-  for (int h = top/2; h > 0; h >>= 1) {
-    if (in_cta && q < h && q + h < nq) {
-      s_norm[le*nq + q] += s_norm[le*nq + q + h];
-      s_rough[le*nq + q] += s_rough[le*nq + q + h];
-    }
-    __syncthreads();
+  __syncthreads();   // the only block-wide barrier
+  const int warp = threadIdx.x/32, lane = threadIdx.x%32;
+  const int e = blockIdx.x*av_warps + warp;
+  if (e >= n_elem) return;   // whole warps leave
+  const double* rho = elem + (size_t)e*(nv + 3)*nq + ND*nq;
+  R* iv = s_iv[warp];
+  double r[ppl];
+  #pragma unroll
+  for (int k = 0; k < ppl; ++k) r[k] = lane + 32*k < nq ? rho[lane + 32*k] : 1.;
+  R sn = 0;
+  #pragma unroll
+  for (int k = 0; k < ppl; ++k) {
+    const int q = lane + 32*k;
+    if (q >= nq) break;
+    const R v = std::is_same<R, double>::value ? R(1./r[k]) : R(1)/to_R<R>(r[k]);
+    iv[q] = v;
+    R w = 1;
+    #pragma unroll
+    for (int d = 0; d < ND; ++d) w *= s_w[(q/ipow(RS, ND - 1 - d))%RS];
+    sn += v*v*w;
   }
-  if (!active || q != 0) return;
-  const double nonsmooth = s_rough[le*nq]/(s_norm[le*nq]*ND);
-  const double ramp_center = -4.25*log(double(RS - 1))/log(10.);
-  const double half_width = 0.5;
-  double indicator = log(nonsmooth)/log(10.);
-  if (indicator <= ramp_center - half_width) indicator = 0;
-  else if (indicator < ramp_center + half_width)
-    indicator = .5*(1 + sin(3.14159265358979323846*(indicator - ramp_center)/2/half_width));
-  else indicator = 1;
+  __syncwarp();
+  R sr = 0;
+  for (int t = lane; t < ND*nfq; t += 32) {
+    const int d = t/nfq, rr = t%nfq;
+    const int stride = S::stride(d);
+    const R* row = iv + (rr/stride)*stride*RS + rr%stride;
+    R dot = 0;
+    #pragma unroll
+    for (int i = 0; i < RS; ++i) dot += row[i*stride]*s_ow[i];
+    R fw = 1;
+    #pragma unroll
+    for (int k = 0; k < ND - 1; ++k) fw *= s_w[(rr/ipow(RS, ND - 2 - k))%RS];
+    sr += dot*dot*fw;
+  }
+  #pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    sn += __shfl_xor_sync(0xffffffffu, sn, o);
+    sr += __shfl_xor_sync(0xffffffffu, sr, o);
+  }
+  if (lane) return;
+  // below and above the ramp by the thresholds on the ratio itself, without the division and the
+  // logarithm; the ramp (and a NaN) as the reference forms it
+  const double num = double(sr), den = double(sn)*ND;
+  double indicator;
+  if (den > 0 && num <= ramp.lo*den) indicator = 0;
+  else if (den > 0 && num >= ramp.hi*den) indicator = 1;
+  else {
+    indicator = log(num/den)/log(10.);
+    if (indicator <= ramp.center - ramp.half_width) indicator = 0;
+    else if (indicator < ramp.center + ramp.half_width)
+      indicator = .5*(1 + sin(3.14159265358979323846*(indicator - ramp.center)/2/ramp.half_width));
+    else indicator = 1;
+  }
   uncert[e] = (RS - 1)*char_speed*nom_size[e]*indicator;
 }
 
@@ -2648,27 +2680,48 @@ __global__ void k_swap_av(double* elem, int n_elem)
 }
 
 // Multilinear interpolation of the vertex values to the qpoints (Gauss_lobatto(2).interpolate
-// + math::hypercube_matvec, src/Solver.cpp:648-656): last reference dimension first.
-template <int ND, int RS>
-__global__ void k_av_interp(double* elem, const int* vert_id, int n_elem, Tab<RS> tab, const double* vmax)
+// + math::hypercube_matvec, src/Solver.cpp:648-656): last reference dimension first, as a
+// tensor product. A CTA takes tiles of EPB elements; stage m (m = 1..nd) interpolates along
+// dimension nd - m the (nvert >> (m-1)) x RS^(m-1) values of the previous stage to
+// (nvert >> m) x RS^m, in shared memory, so each point's value comes out of the same operations
+// as interpolating its nvert vertex values one point at a time, with the partial results shared
+// (312 instead of 1512 interpolations per element at row size 6 in 3D). R as in k_av_uncert.
+template <int ND, int RS, typename R>
+__global__ void __launch_bounds__(Shape<ND, RS>::threads)
+k_av_interp(double* elem, const int* vert_id, int n_elem, AvTab<RS, R> tab, const double* vmax)
 {
   using S = Shape<ND, RS>;
-  constexpr int nq = S::nq, nv = S::nv, nvert = S::nvert;
-  const long total = (long)n_elem*nq;
-  for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
-    const int e = int(t/nq), q = int(t%nq);
-    double vals[nvert];
+  constexpr int nq = S::nq, nv = S::nv, nvert = S::nvert, EPB = S::epb;
+  __shared__ R s_buf[2][EPB*nq];
+  __shared__ R s_node[RS];
+  if (threadIdx.x == 0) {   // constant indices, as in k_av_uncert; the tile loop's barrier follows
     #pragma unroll
-    for (int v = 0; v < nvert; ++v) vals[v] = vmax[vert_id[e*nvert + v]];
-    int n = nvert;
+    for (int i = 0; i < RS; ++i) s_node[i] = tab.node[i];
+  }
+  const int n_tiles = (n_elem + EPB - 1)/EPB;
+  for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    const int e0 = tile*EPB;
+    __syncthreads();   // the previous tile's last stage is read
+    for (int i = threadIdx.x; i < EPB*nvert; i += blockDim.x)
+      s_buf[0][i] = e0 + i/nvert < n_elem ? to_R<R>(vmax[vert_id[(size_t)e0*nvert + i]]) : R(0);
     #pragma unroll
-    for (int d = ND - 1; d >= 0; --d) {
-      const double x = tab.node[(q/ipow(RS, ND - 1 - d))%RS];
-      #pragma unroll
-      for (int i = 0; i < (nvert >> (ND - d)); ++i) vals[i] = (1. - x)*vals[2*i] + x*vals[2*i + 1];
-      n /= 2;
+    for (int m = 1; m <= ND; ++m) {
+      __syncthreads();
+      const int sub = ipow(RS, m - 1);
+      const int n_in = (nvert >> (m - 1))*sub, n_out = (nvert >> m)*sub*RS;
+      const R* in = s_buf[(m - 1)%2];
+      R* out = s_buf[m%2];
+      for (int t = threadIdx.x; t < EPB*n_out; t += blockDim.x) {
+        const int le = t/n_out, o = t%n_out;
+        const int i = o/(sub*RS), p = o%(sub*RS);
+        const int rest = p%sub;
+        const R x = s_node[p/sub];
+        const R* a = in + le*n_in + 2*i*sub + rest;
+        const R v = (R(1) - x)*a[0] + x*a[sub];
+        if (m < ND) out[le*n_out + o] = v;
+        else if (e0 + le < n_elem) elem[(size_t)(e0 + le)*(nv + 3)*nq + (nv + 2)*nq + p] = double(v);
+      }
     }
-    elem[(size_t)e*(nv + 3)*nq + (nv + 2)*nq + q] = vals[0];
   }
 }
 

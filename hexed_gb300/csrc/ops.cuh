@@ -69,6 +69,28 @@ struct Runner
     return t;
   }
 
+  static AvRamp av_ramp()
+  {
+    AvRamp r;
+    r.center = -4.25*std::log(double(RS - 1))/std::log(10.);
+    r.half_width = 0.5;
+    r.lo = std::pow(10., r.center - r.half_width);
+    r.hi = std::pow(10., r.center + r.half_width);
+    return r;
+  }
+
+  static AvTab<RS, R> av_tab(const Ctx& c)
+  {
+    const Tab<RS> t = tab(c);
+    AvTab<RS, R> a;
+    for (int i = 0; i < RS; ++i) {
+      a.w[i] = R(t.weight[i]);
+      a.ow[i] = R(t.ortho_last[i]*t.weight[i]);
+      a.node[i] = R(t.node[i]);
+    }
+    return a;
+  }
+
   // Elements per CTA of the volume kernel for launch-shape variant v: 0 the default
   // (256/nq), 1 half of it, 2 twice it. The 2D Cartesian kernels (the serving path) are
   // compiled in all three shapes; other kernels only in the default.
@@ -321,8 +343,8 @@ struct Runner
     const int n_elem = c.n_car + c.n_def;
     {
       ProfScope ps(c, "av_uncert");
-      k_av_uncert<ND, RS><<<(n_elem + S::epb - 1)/S::epb, S::threads, 0, c.stream>>>(c.elem, c.nom_size, n_elem, tab(c),
-                                                                                  char_speed, c.uncert);
+      k_av_uncert<ND, RS, R><<<(n_elem + av_warps - 1)/av_warps, av_warps*32, 0, c.stream>>>(c.elem, c.nom_size, n_elem, av_tab(c),
+                                                                                  char_speed, av_ramp(), c.uncert);
     }
     cudaMemsetAsync(c.vmax, 0, sizeof(double)*c.n_vert, c.stream);
     {
@@ -330,7 +352,7 @@ struct Runner
       k_av_vertex_max<ND><<<grid_for((long)n_elem*S::nvert, 256), 256, 0, c.stream>>>(c.vert_id, n_elem, c.uncert, c.vmax);
     }
     ProfScope ps(c, "av_interp");
-    k_av_interp<ND, RS><<<grid_for((long)n_elem*S::nq, 256), 256, 0, c.stream>>>(c.elem, c.vert_id, n_elem, tab(c), c.vmax);
+    k_av_interp<ND, RS, R><<<grid_for((n_elem + S::epb - 1)/S::epb, 1), S::threads, 0, c.stream>>>(c.elem, c.vert_id, n_elem, av_tab(c), c.vmax);
   }
 
   // Solver::fix_admissibility's coefficient set-up (src/Solver.cpp:990-1039): the elements'
@@ -349,7 +371,7 @@ struct Runner
       k_elem_vertex_max<ND><<<grid_for(n_elem, 256), 256, 0, c.stream>>>(c.vert_id, n_elem, c.vmax, c.uncert);
       cudaMemsetAsync(c.vmax, 0, sizeof(double)*c.n_vert, c.stream);
       k_av_vertex_max<ND><<<grid_for((long)n_elem*S::nvert, 256), 256, 0, c.stream>>>(c.vert_id, n_elem, c.uncert, c.vmax);
-      k_av_interp<ND, RS><<<grid_for((long)n_elem*S::nq, 256), 256, 0, c.stream>>>(c.elem, c.vert_id, n_elem, tab(c), c.vmax);
+      k_av_interp<ND, RS, R><<<grid_for((n_elem + S::epb - 1)/S::epb, 1), S::threads, 0, c.stream>>>(c.elem, c.vert_id, n_elem, av_tab(c), c.vmax);
     }
     k_swap_av<ND, RS><<<grid_for((long)n_elem*S::nq, 256), 256, 0, c.stream>>>(c.elem, n_elem);
   }
