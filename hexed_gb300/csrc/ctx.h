@@ -78,6 +78,7 @@ struct Ctx {
   double* partials;      // reduction partials, max_partials doubles
   int max_partials;
   int* status;
+  unsigned* dt_ticket;   // CTAs of k_max_dt done; the last one takes the minimum and resets it
   double* d_norm;        // residual norm output [3]
   double* h_pinned;      // pinned host staging for scalars [8]
   Profiler* prof;

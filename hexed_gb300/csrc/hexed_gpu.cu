@@ -442,6 +442,7 @@ int hexed_gpu_create(const hexed_mesh_desc* d, int precision, hexed_gpu_ctx** ou
       cudaMalloc((void**)&c->record, n_elem*sizeof(int)) != cudaSuccess ||
       cudaMalloc((void**)&c->scalars, hx::SC_N*sizeof(double)) != cudaSuccess ||
       cudaMalloc((void**)&c->status, 4*sizeof(int)) != cudaSuccess ||
+      cudaMalloc((void**)&c->dt_ticket, sizeof(unsigned)) != cudaSuccess ||
       cudaMalloc((void**)&c->d_norm, 4*sizeof(double)) != cudaSuccess ||
       cudaMallocHost((void**)&c->h_pinned, 8*sizeof(double)) != cudaSuccess) {
     hexed_gpu_destroy(c);
@@ -449,6 +450,7 @@ int hexed_gpu_create(const hexed_mesh_desc* d, int precision, hexed_gpu_ctx** ou
   }
   cudaMemset(c->scalars, 0, hx::SC_N*sizeof(double));
   cudaMemset(c->status, 0, 4*sizeof(int));
+  cudaMemset(c->dt_ticket, 0, sizeof(unsigned));
   HX_CUDA(cudaDeviceSynchronize());
   *out = c;
   return HEXED_OK;
@@ -460,7 +462,7 @@ int hexed_gpu_destroy(hexed_gpu_ctx* c)
   if (c->stream) cudaStreamSynchronize(c->stream);
   void* ptrs[] = {c->elem, c->rcache, c->face, c->nom_size, c->vert_tss, c->jac, c->face_nrml, c->car_con,
                   c->def_con, c->def_con_nrml, c->bc_con, c->bc_nrml, c->bc_cache, c->ref_face, c->bc_spec,
-                  c->scalars, c->partials, c->status, c->d_norm, c->vert_id, c->uncert, c->vmax,
+                  c->scalars, c->partials, c->status, c->dt_ticket, c->d_norm, c->vert_id, c->uncert, c->vmax,
                   c->seg_table, c->seg_out, c->inv_det, c->face_f, c->rcache_f, c->nrm_f, c->face_nrml_f,
                   c->def_con_nrml_f, c->bc_nrml_f, c->ref_state, c->ref_terms, c->record};
   for (void* p : ptrs) if (p) cudaFree(p);
@@ -796,7 +798,7 @@ int fix_admissibility(Ctx* c, const hexed_update_params* p, double stability_rat
 
 // Enqueues one Solver::update (src/Solver.cpp:834-886) on the context's stream. With local
 // time stepping and no diffusion the step is known on the host (the global part is 1, times
-// max_time_step and the Chebyshev factor, as k_finalize_dt would give): the first stage's
+// max_time_step and the Chebyshev factor, as k_max_dt's last CTA would give): the first stage's
 // volume kernel then computes each point's time-step scale itself (LocalDt mode 1) instead
 // of a separate Max_dt pass, with the same arithmetic, and *host_dt receives the step.
 // Otherwise *host_dt is NaN and the step stays on the device.

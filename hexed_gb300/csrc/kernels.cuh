@@ -2358,10 +2358,14 @@ __global__ void k_write_face(Dev<FaceT> m, Tab<RS> tab, int e_begin, int n_elem)
 // Spatial::Max_dt (include/Spatial.hpp:784-828); global minimum through per-CTA partials.
 // R is the compute type: double for the FP64 form; float for the mixed form, whose time
 // step is a CFL limit with a safety factor and needs no more than float accuracy.
+// Each CTA writes its minimum to partials and takes a ticket; the CTA that takes the last one
+// (all partials written and fenced before it) forms the minimum over the partials, the
+// stage's step dt = min(max_dt, max_time_step)*cheby (src/Solver.cpp:843-846; max_dt is 1
+// under local time stepping) into scalars, and resets the ticket. No CTA waits on another.
 template <int ND, int RS, typename R, bool VISC, typename FaceT>
 __global__ void __launch_bounds__(256)
 k_max_dt(Dev<FaceT> m, Tab<RS> tab, R inv_cfl_c, R inv_cfl_d, int local_time, TmT<R> visc, TmT<R> cond,
-         double* partials)
+         double* partials, unsigned* ticket, double max_time_step, double cheby)
 {
   using S = Shape<ND, RS>;
   constexpr int nq = S::nq, nv = S::nv;
@@ -2398,39 +2402,35 @@ k_max_dt(Dev<FaceT> m, Tab<RS> tab, R inv_cfl_c, R inv_cfl_d, int local_time, Tm
   for (int o = 16; o > 0; o >>= 1) dt = fmin(dt, __shfl_xor_sync(0xffffffffu, dt, o));
   if ((threadIdx.x & 31) == 0) s_min[threadIdx.x >> 5] = dt;
   __syncthreads();
+  __shared__ bool s_last;
   if (threadIdx.x < 32) {
     double x = threadIdx.x < (blockDim.x + 31)/32 ? s_min[threadIdx.x] : 1.7976931348623157e308;
     for (int o = 16; o > 0; o >>= 1) x = fmin(x, __shfl_xor_sync(0xffffffffu, x, o));
-    if (threadIdx.x == 0) partials[blockIdx.x] = x;
+    if (threadIdx.x == 0) {
+      partials[blockIdx.x] = x;
+      __threadfence();
+      s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
   }
-}
-
-// Minimum over the CTA partials -> scalars[SC_MAXDT]; then the stage step
-// dt = min(max_dt, max_time_step)*cheby (src/Solver.cpp:843-846) -> scalars[SC_DT].
-static __global__ void k_finalize_dt(double* scalars, const double* partials, int n_part, int local_time,
-                              double max_time_step, double cheby)
-{
-  // four independent running minima per thread, so the partials' loads overlap
-  double x = 1.7976931348623157e308, x1 = x, x2 = x, x3 = x;
-  int i = threadIdx.x;
-  for (; i + 3*(int)blockDim.x < n_part; i += 4*blockDim.x) {
-    x = fmin(x, partials[i]);
-    x1 = fmin(x1, partials[i + blockDim.x]);
-    x2 = fmin(x2, partials[i + 2*blockDim.x]);
-    x3 = fmin(x3, partials[i + 3*blockDim.x]);
-  }
-  for (; i < n_part; i += blockDim.x) x = fmin(x, partials[i]);
-  x = fmin(fmin(x, x1), fmin(x2, x3));
-  __shared__ double s_min[32];
-  for (int o = 16; o > 0; o >>= 1) x = fmin(x, __shfl_xor_sync(0xffffffffu, x, o));
-  if ((threadIdx.x & 31) == 0) s_min[threadIdx.x >> 5] = x;
+  __syncthreads();
+  if (!s_last) return;
+  // the last CTA: minimum over every CTA's partial (read past L1), in any order (fmin is exact)
+  __threadfence();
+  // one running minimum, the loop unrolled so that its loads overlap (a wider tail would raise
+  // the register count of the whole kernel)
+  double y = 1.7976931348623157e308;
+  #pragma unroll 4
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) y = fmin(y, __ldcg(partials + i));
+  for (int o = 16; o > 0; o >>= 1) y = fmin(y, __shfl_xor_sync(0xffffffffu, y, o));
+  if ((threadIdx.x & 31) == 0) s_min[threadIdx.x >> 5] = y;   // warp 0 read s_min before the barrier
   __syncthreads();
   if (threadIdx.x == 0) {
     double r = 1.7976931348623157e308;
     for (int i = 0; i < (int)(blockDim.x + 31)/32; ++i) r = fmin(r, s_min[i]);
     if (local_time) r = 1.;
-    scalars[SC_MAXDT] = r;
-    scalars[SC_DT] = fmin(r, max_time_step)*cheby;
+    m.scalars[SC_MAXDT] = r;
+    m.scalars[SC_DT] = fmin(r, max_time_step)*cheby;
+    *ticket = 0u;
   }
 }
 

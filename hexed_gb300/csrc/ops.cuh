@@ -310,11 +310,9 @@ struct Runner
     {
       ProfScope ps(c, "max_dt");
       const R icc = R(inv_cfl_conv(c, msc)), icd = R(inv_cfl_diff(c, msd));
-      if (viscous) k_max_dt<ND, RS, R, true, FaceT><<<grid, 256, 0, c.stream>>>(dev(c), tab(c), icc, icd, local_time, make_tm<R>(visc), make_tm<R>(cond), c.partials);
-      else k_max_dt<ND, RS, R, false, FaceT><<<grid, 256, 0, c.stream>>>(dev(c), tab(c), icc, icd, local_time, make_tm<R>(visc), make_tm<R>(cond), c.partials);
+      if (viscous) k_max_dt<ND, RS, R, true, FaceT><<<grid, 256, 0, c.stream>>>(dev(c), tab(c), icc, icd, local_time, make_tm<R>(visc), make_tm<R>(cond), c.partials, c.dt_ticket, max_time_step, cheby);
+      else k_max_dt<ND, RS, R, false, FaceT><<<grid, 256, 0, c.stream>>>(dev(c), tab(c), icc, icd, local_time, make_tm<R>(visc), make_tm<R>(cond), c.partials, c.dt_ticket, max_time_step, cheby);
     }
-    ProfScope ps(c, "finalize_dt");
-    k_finalize_dt<<<1, 1024, 0, c.stream>>>(c.scalars, c.partials, grid, local_time, max_time_step, cheby);
   }
 
   static void write_face(Ctx& c, int e_begin, int n_elem)
