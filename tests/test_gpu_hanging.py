@@ -111,3 +111,61 @@ def test_art_visc_admis(n):
     errs, bad = compare_arenas(a, g, what=("elem",))
     assert not bad, errs
     np.testing.assert_allclose(res["g"], res["o"], rtol=FP64_TOL)
+
+
+def ramp_arena(row_size=4, n=4):
+    """The Mach-2 arena with each element's specific volume carrying the highest Legendre mode
+    along the first reference dimension, amplitudes log-spaced over the elements, so that the
+    smoothness indicator (src/stabilizing_art_visc.cpp:47-55) falls below its ramp, inside it
+    and above it. Returns the arena and each element's log10 non-smoothness, restated here."""
+    ar = problems.mach2_jump_3d(n_per_side=n, row_size=row_size)
+    b = Basis(row_size)
+    rs, nq, nd = row_size, ar.nq, ar.n_dim
+    mode = b.orthogonal(rs - 1)
+    node0 = (np.arange(nq) // rs ** (nd - 1)) % rs      # node index along the first dimension
+    amps = np.logspace(-3.5, 0., ar.n_elem)
+    vel = ar.freestream[0] / ar.freestream[nd]
+    log_ns = np.empty(ar.n_elem)
+    w = b.node_weights
+    qw = np.prod([w[(np.arange(nq) // rs ** (nd - 1 - d)) % rs] for d in range(nd)], axis=0)
+    for e in range(ar.n_elem):
+        iv = (1. + 0.5 * amps[e] * mode[node0]) / 1.2
+        rho = 1. / iv
+        ar.elem[e, 0] = rho * vel
+        ar.elem[e, 1:nd] = 0.
+        ar.elem[e, nd] = rho
+        ar.elem[e, nd + 1] = 1e5 / (problems.HEAT_RAT - 1) + 0.5 * rho * vel * vel
+        # rows along the first dimension carry the mode; the other rows project to zero
+        rows = iv.reshape(rs, -1)
+        fw = np.prod([w[(np.arange(nq // rs) // rs ** (nd - 2 - d)) % rs] for d in range(nd - 1)], axis=0)
+        dots = (mode * w) @ rows
+        log_ns[e] = np.log10(np.sum(dots ** 2 * fw) / (np.sum(iv * iv * qw) * nd))
+    return ar, log_ns
+
+
+@pytest.mark.parametrize("precision", [abi.FP64, abi.MIXED])
+def test_art_visc_ramp_regimes(precision):
+    """Elements below, inside and above the indicator's ramp: the device classifies the outer
+    two by thresholds on the ratio and evaluates the ramp as the reference does; the AV row
+    must match the oracle's in every regime (FP64 to 1e-12; the mixed form's float sums to
+    1e-5 of the largest coefficient)."""
+    rs = 4
+    ar, log_ns = ramp_arena(rs)
+    center = -4.25 * np.log10(rs - 1)
+    assert (log_ns < center - 0.5).sum() >= 3
+    assert ((log_ns > center - 0.5) & (log_ns < center + 0.5)).sum() >= 3
+    assert (log_ns > center + 0.5).sum() >= 3
+    oracle.Oracle(ar).write_face()
+    cs = ar.av_char_speed
+    a = ar.copy()
+    oracle.Oracle(a).set_art_visc_admis(cs)
+    g = ar.copy()
+    with Context(g, precision) as ctx:
+        ctx.set_art_visc_admis(cs)
+        ctx.download_all()
+    ref = a.elem[:, a.nv + 2]
+    assert ref.max() > 0 and ref.min() == 0
+    if precision == abi.FP64:
+        np.testing.assert_allclose(g.elem[:, g.nv + 2], ref, rtol=1e-12, atol=1e-12 * ref.max())
+    else:
+        np.testing.assert_allclose(g.elem[:, g.nv + 2], ref, rtol=0, atol=1e-5 * ref.max())
