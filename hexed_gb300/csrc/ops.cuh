@@ -339,6 +339,7 @@ struct Runner
   static void set_art_visc_admis(Ctx& c, double char_speed)
   {
     const int n_elem = c.n_car + c.n_def;
+    if (n_elem == 0) return;   // k_av_uncert's grid would be empty
     {
       ProfScope ps(c, "av_uncert");
       k_av_uncert<ND, RS, R><<<(n_elem + av_warps - 1)/av_warps, av_warps*32, 0, c.stream>>>(c.elem, c.nom_size, n_elem, av_tab(c),
