@@ -265,6 +265,9 @@ def share_vertex_max(values, vert_ids):
 def structured_mesh(n_dim, row_size, n_per_dim, lo, hi, deformed=False, displacement=None, bcs=None):
     """Uniform structured mesh of n_per_dim^n_dim elements on [lo, hi]^n_dim.
 
+    n_per_dim may also be a sequence of per-dimension counts: the elements keep the size
+    (hi - lo)/n_per_dim[0], so dimension d spans lo + [0, n_per_dim[d]*size].
+
     deformed: make every element a Deformed_element (connections are deformed
       connections with direction {{d,d},{1,0}}, include/connection.hpp:35).
     displacement: fn(vertex positions [N][nd], on_boundary [N][nd] bool) -> displacement [N][nd]
@@ -272,24 +275,23 @@ def structured_mesh(n_dim, row_size, n_per_dim, lo, hi, deformed=False, displace
     bcs: dict {(i_dim, face_sign): BcSpec} for the 2*n_dim domain boundaries.
     """
     basis = Basis(row_size)
-    n = n_per_dim
-    E = n ** n_dim
-    h = (hi - lo) / n
+    counts = tuple(int(c) for c in n_per_dim) if np.ndim(n_per_dim) else (int(n_per_dim),) * n_dim
+    E = int(np.prod(counts))
+    h = (hi - lo) / counts[0]
     ar = Arena(n_dim, row_size, 0 if deformed else E, E if deformed else 0)
-    idx = np.array(list(itertools.product(range(n), repeat=n_dim)))   # [E][nd], dim 0 outermost
+    idx = np.array(list(itertools.product(*[range(c) for c in counts])))   # [E][nd], dim 0 outermost
     ar.nom_size[:] = h
     # global vertex grid
-    nvg = n + 1
     vbits = np.array(list(itertools.product(range(2), repeat=n_dim)))  # [nvert][nd], dim 0 most significant
     vidx = idx[:, None, :] + vbits[None]                               # [E][nvert][nd]
     vert_ids = np.zeros(vidx.shape[:2], dtype=np.int64)
     for d in range(n_dim):
-        vert_ids = vert_ids * nvg + vidx[:, :, d]
+        vert_ids = vert_ids * (counts[d] + 1) + vidx[:, :, d]
     ar.vert_ids = vert_ids
-    gv = np.array(list(itertools.product(range(nvg), repeat=n_dim)))   # global vertices, same ordering
+    gv = np.array(list(itertools.product(*[range(c + 1) for c in counts])))   # global vertices, same ordering
     gpos = lo + gv * h
     if deformed and displacement is not None:
-        on_b = (gv == 0) | (gv == n)
+        on_b = (gv == 0) | (gv == np.array(counts))
         gpos = gpos + displacement(gpos.copy(), on_b)
     vert_pos = gpos[vert_ids]                                           # [E][nvert][nd]
     ar.vert_pos = vert_pos
@@ -304,7 +306,7 @@ def structured_mesh(n_dim, row_size, n_per_dim, lo, hi, deformed=False, displace
         elem_face_nrml = None
     ar.vert_tss[:] = share_vertex_min(vtss, vert_ids)
     nd, nfq = n_dim, ar.nfq
-    strides = np.array([n ** (n_dim - 1 - d) for d in range(n_dim)])
+    strides = np.array([int(np.prod(counts[d + 1:])) for d in range(n_dim)])
     cons, con_nrml, bcons, bnrml = [], [], [], []
     face_nrml = np.zeros((E if deformed else 0, 2 * nd, nd, nfq))
     bcs = bcs or {}
@@ -315,7 +317,7 @@ def structured_mesh(n_dim, row_size, n_per_dim, lo, hi, deformed=False, displace
     next_slot = E * 2 * nd
     for e in range(E):
         for d in range(nd):
-            if idx[e, d] + 1 < n:
+            if idx[e, d] + 1 < counts[d]:
                 b = e + strides[d]
                 s0, s1 = ar.slot_of(e, 2 * d + 1), ar.slot_of(b, 2 * d)
                 if deformed:
@@ -329,7 +331,7 @@ def structured_mesh(n_dim, row_size, n_per_dim, lo, hi, deformed=False, displace
                 else:
                     cons.append((s0, s1, d))
             for sign in range(2):
-                at_b = (idx[e, d] == 0) if sign == 0 else (idx[e, d] == n - 1)
+                at_b = (idx[e, d] == 0) if sign == 0 else (idx[e, d] == counts[d] - 1)
                 if not at_b:
                     continue
                 if (d, sign) not in spec_index:

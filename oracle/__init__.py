@@ -9,6 +9,8 @@ import ctypes
 import os
 import subprocess
 
+import numpy as np
+
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "hexed_oracle.cpp")
 LIB = os.path.join(HERE, "_build", "libhexed_oracle.so")
@@ -58,6 +60,8 @@ def load():
             "oracle_derivative": [c_int, P, P, P],
             "oracle_perm_index": [c_int, c_int, c_int, c_int],
             "oracle_characteristics": [c_int, P, P, P, P, P],
+            "oracle_sav_slot_dof": [c_int, c_int],
+            "oracle_update_art_visc_smoothness": [D, P, P, ctypes.POINTER(SavParams), P],
         }
         for name, args in sig.items():
             fn = getattr(lib, name)
@@ -65,6 +69,53 @@ def load():
             fn.restype = c_int
         _lib = lib
     return _lib
+
+
+class SavParams(ctypes.Structure):
+    """oracle_sav_params: Solver::update_art_visc_smoothness's settings, the reference's
+    defaults (src/Solver.cpp:154-163) unless given."""
+    _fields_ = [("advect_length", ctypes.c_double), ("advect_iters", ctypes.c_int),
+                ("diff_iters", ctypes.c_int), ("n_cheby", ctypes.c_int), ("av_row_size", ctypes.c_int),
+                ("advect_safety", ctypes.c_double), ("diff_safety", ctypes.c_double),
+                ("diff_ratio", ctypes.c_double), ("visc_mult", ctypes.c_double),
+                ("unscaled_max", ctypes.c_double), ("freestream_mass", ctypes.c_double),
+                ("freestream_energy", ctypes.c_double)]
+
+
+def sav_params(advect_length, row_size, freestream_mass, freestream_energy, advect_iters=1, diff_iters=1,
+               n_cheby=1, av_row_size=None, advect_safety=0.7, diff_safety=0.7, diff_ratio=0.3,
+               visc_mult=1e2, unscaled_max=5.):
+    return SavParams(advect_length, advect_iters, diff_iters, n_cheby, av_row_size or row_size, advect_safety,
+                     diff_safety, diff_ratio, visc_mult, unscaled_max, freestream_mass, freestream_energy)
+
+
+class SavStorage:
+    """Storage of the smoothness-based AV beside an arena: `aux` [n_elem][4 + 2*row_size][nq]
+    (forcing rows at 0, the advection state at 1 as Solver's constructor sets it
+    (src/Solver.cpp:201-211), its residual cache) and the face slots [n_slot][slot_dof]."""
+
+    def __init__(self, arena):
+        rs, nq = arena.row_size, arena.nq
+        self.aux = np.zeros((arena.n_elem, 4 + 2 * rs, nq))
+        self.aux[:, 4:4 + rs] = 1.
+        slot_dof = load().oracle_sav_slot_dof(arena.n_dim, rs)
+        self.face = np.zeros((arena.n_slot, slot_dof))
+
+    @property
+    def forcing(self):
+        return self.aux[:, :4]
+
+    @property
+    def advection(self):
+        n = (self.aux.shape[1] - 4) // 2
+        return self.aux[:, 4:4 + n]
+
+
+def _inplace(a):
+    """Pointer to an array the oracle updates in place (no copy is made)."""
+    if a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise ValueError("in-place oracle storage must be C-contiguous float64")
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
 
 def _dp(a):
@@ -165,6 +216,15 @@ class Oracle:
 
     def set_art_visc_admis(self, char_speed):
         self._chk(self.lib.oracle_set_art_visc_admis(ctypes.byref(self.desc), char_speed))
+
+    def update_art_visc_smoothness(self, storage, params):
+        """Solver::update_art_visc_smoothness (src/Solver.cpp:457-582) on a conforming mesh:
+        writes the bulk AV row of the arena; returns art_visc_residual."""
+        out = ctypes.c_double()
+        self._chk(self.lib.oracle_update_art_visc_smoothness(ctypes.byref(self.desc), _inplace(storage.aux),
+                                                             _inplace(storage.face), ctypes.byref(params),
+                                                             ctypes.byref(out)))
+        return out.value
 
     def residual_norm(self):
         out = (ctypes.c_double * 3)()

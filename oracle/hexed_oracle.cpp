@@ -27,6 +27,24 @@
 #include "../include/hexed_gpu.h"
 #include "../hexed_gb300/csrc/basis_tables.h"
 
+// Parameters of Solver::update_art_visc_smoothness (src/Solver.cpp:457-582) and
+// Solver::diffuse_art_visc (src/Solver.cpp:428-455); the reference's defaults
+// (src/Solver.cpp:154-163) in brackets.
+struct oracle_sav_params {
+  double advect_length;      // the `advect_length` argument (Case: art_visc_width)
+  int advect_iters;          // av_advect_iters [1]
+  int diff_iters;            // av_diff_iters [1]
+  int n_cheby;               // n_cheby_av [1]
+  int av_row_size;           // av_rs: degree + 1 of the projected Legendre mode [row_size]
+  double advect_safety;      // av_advect_max_safety [0.7]
+  double diff_safety;        // av_diff_max_safety [0.7]
+  double diff_ratio;         // av_diff_ratio [0.3]
+  double visc_mult;          // av_visc_mult [100]
+  double unscaled_max;       // av_unscaled_max [5]
+  double freestream_mass;    // freestream{n_dim}
+  double freestream_energy;  // freestream{n_dim + 1}
+};
+
 namespace {
 
 constexpr double heat_rat = 1.4;                 // include/pde.hpp:51
@@ -62,6 +80,7 @@ inline double transport_coef(const hexed_transport& t, double sqrt_temp)
 template <int ND, int RS>
 struct K
 {
+  static constexpr int n_dim = ND, row_size = RS;
   static constexpr int nq = ipow(RS, ND);
   static constexpr int nfq = nq/RS;
   static constexpr int nv = ND + 2;
@@ -1294,6 +1313,626 @@ double chebyshev_step(int n_steps, int i_step)
   return 1/(1 - std::cos((n_steps - i_step - 0.5)*M_PI/n_steps));
 }
 
+// ---------------------------------------------------------------- smoothness-based AV
+// Solver::update_art_visc_smoothness (src/Solver.cpp:457-582): the Spatial kernels applied to
+// pde::Advection and pde::Smooth_art_visc (include/pde.hpp:265-431) on conforming meshes.
+// Storage beside the arena:
+//  * aux  [n_elem][4 + 2*row_size][nq]: the art_visc_forcing rows (Storage_params::n_forcing
+//    = 4), the advection state (row_size rows) and its residual cache (row_size rows: the
+//    element's residual_cache, which the reference sizes for max(n_var, row_size) rows);
+//  * face [n_slot][max(2*nv, nd + row_size)*nfq]: one face slot per arena slot, the size of a
+//    Face_connection face (include/connection.hpp:58-66); the LDG half starts at nv*nfq as
+//    in Element::face (src/Element.cpp:189). The reference keeps these traces in the flow's
+//    face storage; the flow's update rewrites every trace it reads before reading it.
+// The flow state is used in place: the momentum rows are divided by sqrt(2 rho E) for the
+// advection velocity and multiplied back at the end (the reference does the same, so the
+// momentum keeps the same last bits); the time-step-scale row is overwritten by the
+// pseudo-time steps; the bulk AV row receives the coefficient.
+template <int ND, int RS>
+struct Sav
+{
+  using KK = K<ND, RS>;
+  static constexpr int nq = KK::nq, nfq = KK::nfq, nv = KK::nv, nvert = KK::nvert;
+  static constexpr int n_forcing = 4;
+  static constexpr int n_adv = RS;                       // Storage_params::n_advection
+  static constexpr int n_aux = n_forcing + 2*n_adv;
+  static constexpr int n_adv_extrap = ND + n_adv;        // pde::Advection::n_extrap
+  static constexpr int n_sav = 3;                        // pde::Smooth_art_visc::n_extrap, n_update
+  static constexpr int slot_dof = (2*nv > n_adv_extrap ? 2*nv : n_adv_extrap)*nfq;
+
+  const KK& k;
+  const hexed_mesh_desc& m;
+  double* aux;
+  double* sf;
+  const oracle_sav_params& p;
+  double adv_node[RS];   // pde::Advection::_nodes = 2*(Gauss-Legendre nodes) - 1 (pde.hpp:281)
+
+  Sav(const KK& kk, double* aux_, double* face_, const oracle_sav_params& par)
+  : k{kk}, m{kk.m}, aux{aux_}, sf{face_}, p{par}
+  {
+    for (int i = 0; i < RS; ++i) adv_node[i] = 2*k.t.node[i] - 1.;
+  }
+
+  double* forcing(int e) const { return aux + (size_t)e*n_aux*nq; }
+  double* adv(int e) const { return forcing(e) + n_forcing*nq; }
+  double* adv_cache(int e) const { return adv(e) + n_adv*nq; }
+  double* slot(int s, bool ldg) const { return sf + (size_t)s*slot_dof + ldg*nv*nfq; }
+  double* face(int e, int i, bool ldg) const { return slot(e*2*ND + i, ldg); }
+  int n_elem() const { return k.n_elem(); }
+  const double* jac(int e) const { return m.jac + (size_t)(e - m.n_car_elem)*(ND*ND + 1)*nq; }
+
+  // mesh spacing at a qpoint: math::interp of the vertex time-step scales (include/math.hpp:207-218)
+  double spacing(int e, int q) const
+  {
+    const double* vt = m.vert_tss + (size_t)e*nvert;
+    double vals[nvert];
+    for (int i = 0; i < nvert; ++i) vals[i] = vt[i];
+    int stride = nvert;
+    for (int d = 0; d < ND; ++d) {
+      double coord = k.t.node[(q/ipow(RS, ND - 1 - d))%RS];
+      stride /= 2;
+      for (int i = 0; i < stride; ++i) vals[i] += coord*(vals[i + stride] - vals[i]);
+    }
+    return vals[0];
+  }
+
+  // Spatial<pde::Advection>::Max_dt with local time stepping (include/Spatial.hpp:784-828):
+  // char_speed = max(1, |velocity|) (pde.hpp:343-346), no diffusion
+  void max_dt_advection() const
+  {
+    const double max_cfl_c = k.t.max_cfl*p.advect_safety;
+    #pragma omp parallel for
+    for (int e = 0; e < n_elem(); ++e) {
+      double* state = k.elem(e);
+      for (int q = 0; q < nq; ++q) {
+        double sq = 0.;
+        for (int d = 0; d < ND; ++d) sq += state[d*nq + q]*state[d*nq + q];
+        double cs = std::max(1., std::sqrt(sq));
+        double scale = 0;
+        scale += cs/max_cfl_c/spacing(e, q);
+        state[nv*nq + q] = 1./scale;
+      }
+    }
+  }
+
+  // Spatial<pde::Smooth_art_visc>::Max_dt with local time stepping: diffusivity 1, no convection
+  void max_dt_smooth_av() const
+  {
+    const double max_cfl_d = -2/k.t.min_eig_diffusion*p.diff_safety;
+    #pragma omp parallel for
+    for (int e = 0; e < n_elem(); ++e) {
+      double* state = k.elem(e);
+      for (int q = 0; q < nq; ++q) {
+        double sp = spacing(e, q);
+        double scale = 0;
+        scale += 1./max_cfl_d/sp/sp;
+        state[nv*nq + q] = 1./scale;
+      }
+    }
+  }
+
+  // Spatial::Write_face (include/Spatial.hpp:41-57) of n_var rows of `rows` into the element's faces
+  void write_face_rows(int e, const double* const* rows, int n_var) const
+  {
+    for (int d = 0; d < ND; ++d) {
+      for (int i_fq = 0; i_fq < nfq; ++i_fq) {
+        for (int v = 0; v < n_var; ++v) {
+          for (int s = 0; s < 2; ++s) {
+            double acc = 0.;
+            for (int i = 0; i < RS; ++i) acc += k.t.bound[s*RS + i]*rows[v][KK::row_qpoint(d, i_fq, i)];
+            face(e, 2*d + s, false)[v*nfq + i_fq] = acc;
+          }
+        }
+      }
+    }
+  }
+  // pde::Advection::fetch_extrap (pde.hpp:284-290): the velocity rows, then the advection state
+  void write_face_advection(int e) const
+  {
+    const double* rows[n_adv_extrap];
+    for (int d = 0; d < ND; ++d) rows[d] = k.elem(e) + d*nq;
+    for (int a = 0; a < n_adv; ++a) rows[ND + a] = adv(e) + a*nq;
+    write_face_rows(e, rows, n_adv_extrap);
+  }
+  // pde::Smooth_art_visc::fetch_extrap (pde.hpp:372-377): forcing rows 1-3
+  void write_face_smooth_av(int e) const
+  {
+    const double* rows[n_sav];
+    for (int v = 0; v < n_sav; ++v) rows[v] = forcing(e) + (1 + v)*nq;
+    write_face_rows(e, rows, n_sav);
+  }
+
+  // Flow_bc::apply_advection and its overrides (src/Boundary_condition.cpp:24-41, 346-368,
+  // 429-448, 460-463)
+  void apply_advection_bc(int i) const
+  {
+    const int* c = m.bc_con + 4*i;
+    const hexed_bc_spec& b = m.bc_spec[c[3]];
+    double* in = slot(c[0], false);
+    double* gh = slot(c[1], false);
+    switch (b.kind) {
+      case HEXED_BC_NONPENETRATION: {
+        const double* nrml = m.bc_nrml + (size_t)i*ND*nfq;
+        for (int q = 0; q < nfq; ++q) {
+          double dot = 0., nsq = 0.;
+          for (int d = 0; d < ND; ++d) {
+            double n = nrml[d*nfq + q];
+            dot += in[d*nfq + q]*n;
+            nsq += n*n;
+          }
+          for (int d = 0; d < ND; ++d) gh[d*nfq + q] = in[d*nfq + q] - 2*dot*nrml[d*nfq + q]/nsq;
+          for (int a = 0; a < n_adv; ++a) gh[(ND + a)*nfq + q] = in[(ND + a)*nfq + q];
+        }
+        break;
+      }
+      case HEXED_BC_NO_SLIP:
+        for (int k2 = 0; k2 < ND*nfq; ++k2) gh[k2] = -in[k2];
+        for (int k2 = ND*nfq; k2 < n_adv_extrap*nfq; ++k2) gh[k2] = in[k2];
+        break;
+      case HEXED_BC_COPY:
+        // copy_state (src/Boundary_condition.cpp:12-22): both halves of the face, n_var*nfq each
+        for (int k2 = 0; k2 < 2*nv*nfq; ++k2) gh[k2] = in[k2];
+        break;
+      default:
+        // velocity as inside; advected scalars mirrored about 1
+        for (int k2 = 0; k2 < ND*nfq; ++k2) gh[k2] = in[k2];
+        for (int k2 = 0; k2 < n_adv*nfq; ++k2) gh[ND*nfq + k2] = 2. - in[ND*nfq + k2];
+    }
+  }
+
+  // the three connection lists with the direction encoding of K::neighbor
+  template <typename F>
+  void for_connections(F&& f) const
+  {
+    #pragma omp parallel for
+    for (int i = 0; i < m.n_car_con; ++i) {
+      const int* c = m.car_con + 3*i;
+      f(c[0], c[1], c[2] | (c[2] << 2) | (1 << 4), (const double*)nullptr);
+    }
+    #pragma omp parallel for
+    for (int i = 0; i < m.n_def_con; ++i) {
+      const int* c = m.def_con + 3*i;
+      f(c[0], c[1], c[2], (const double*)(m.def_con_nrml + (size_t)i*ND*nfq));
+    }
+    #pragma omp parallel for
+    for (int i = 0; i < m.n_bc_con; ++i) {
+      const int* c = m.bc_con + 4*i;
+      int d = c[2] & 3, ifs = (c[2] >> 2) & 1;
+      f(c[0], c[1], d | (d << 2) | (ifs << 4) | ((!ifs) << 5), (const double*)(m.bc_nrml + (size_t)i*ND*nfq));
+    }
+  }
+
+  static void signs(int dir, bool deformed, int* sign)
+  {
+    sign[0] = sign[1] = 1;
+    if (deformed) {
+      bool s0 = (dir >> 4) & 1, s1 = (dir >> 5) & 1;
+      sign[0] = 1 - 2*(s0 == 0);
+      sign[1] = 1 - 2*(s1 == 1);
+    }
+  }
+
+  // Spatial<pde::Advection>::Neighbor (include/Spatial.hpp:613-705): local Lax-Friedrichs flux
+  // of the advected scalars, written over the first row_size face variables of both sides
+  void neighbor_advection_con(int slot0, int slot1, int dir, const double* nrml) const
+  {
+    const bool deformed = nrml != nullptr;
+    int sign[2];
+    signs(dir, deformed, sign);
+    double* f0 = slot(slot0, false);
+    double* f1 = slot(slot1, false);
+    double out0[n_adv*nfq], out1[n_adv*nfq];
+    for (int q = 0; q < nfq; ++q) {
+      const int q1 = deformed ? KK::perm_index(dir, q) : q;
+      double n[ND];
+      if (deformed) for (int d = 0; d < ND; ++d) n[d] = sign[0]*nrml[d*nfq + q];
+      else for (int d = 0; d < ND; ++d) n[d] = (d == (dir & 3)) ? 1. : 0.;
+      double u[2][n_adv_extrap], fl[2][n_adv], cs[2];
+      for (int v = 0; v < n_adv_extrap; ++v) { u[0][v] = f0[v*nfq + q]; u[1][v] = f1[v*nfq + q1]; }
+      for (int side = 0; side < 2; ++side) {
+        double nrml_veloc = 0, sq = 0.;
+        for (int d = 0; d < ND; ++d) nrml_veloc += u[side][d]*n[d];
+        for (int a = 0; a < n_adv; ++a) fl[side][a] = adv_node[a]*nrml_veloc*u[side][ND + a];
+        for (int d = 0; d < ND; ++d) sq += u[side][d]*u[side][d];
+        cs[side] = std::max(1., std::sqrt(sq));
+      }
+      double nn = 0.;
+      for (int d = 0; d < ND; ++d) nn += n[d]*n[d];
+      double mult = std::max(cs[0], cs[1])*std::sqrt(nn);
+      for (int a = 0; a < n_adv; ++a) {
+        double flux = .5*(fl[0][a] + fl[1][a] + mult*(u[0][ND + a] - u[1][ND + a]));
+        out0[a*nfq + q] = sign[0]*flux;
+        out1[a*nfq + q1] = sign[1]*flux;
+      }
+    }
+    std::memcpy(f0, out0, sizeof(out0));
+    std::memcpy(f1, out1, sizeof(out1));
+  }
+
+  // Spatial<pde::Advection>::Local (include/Spatial.hpp:326-509) for one element: convective
+  // flux nodes_i*(v.n)*a_i, the source 2/advect_length in the first stage, and
+  // Advection::write_update (pde.hpp:292-300): pseudo = 1 + 2*tss/advect_length, the first
+  // stage sets a = (a + update)/pseudo, the second adds update/pseudo.
+  void local_advection_elem(int e, bool deformed, int stage) const
+  {
+    double* state = k.elem(e);
+    double* tss = state + nv*nq;
+    double* a_st = adv(e);
+    double* ref_state = adv_cache(e);
+    const double d_pos = m.nom_size[e];
+    const double* nrml = deformed ? jac(e) : nullptr;
+    const double* det = deformed ? jac(e) + ND*ND*nq : nullptr;
+    static thread_local std::vector<double> buf;
+    buf.assign((size_t)(2*n_adv*nq + ND*n_adv*nq), 0.);
+    double (*time_rate)[n_adv][nq] = reinterpret_cast<double (*)[n_adv][nq]>(buf.data());
+    double (*flux)[n_adv][nq] = reinterpret_cast<double (*)[n_adv][nq]>(buf.data() + 2*n_adv*nq);
+    for (int q = 0; q < nq; ++q) {
+      for (int i = 0; i < ND; ++i) {
+        double nrml_veloc = 0;
+        for (int j = 0; j < ND; ++j)
+          nrml_veloc += state[j*nq + q]*(deformed ? nrml[(i*ND + j)*nq + q] : (i == j ? 1. : 0.));
+        for (int a = 0; a < n_adv; ++a) flux[i][a][q] = adv_node[a]*nrml_veloc*a_st[a*nq + q];
+      }
+      if (!stage) {
+        double mult = d_pos;
+        if (deformed) mult *= det[q];
+        for (int a = 0; a < n_adv; ++a) time_rate[1][a][q] = mult*(2/p.advect_length);
+      }
+    }
+    for (int d = 0; d < ND; ++d) {
+      for (int i_fq = 0; i_fq < nfq; ++i_fq) {
+        for (int a = 0; a < n_adv; ++a) {
+          double row_f[RS], face_f[2], der[RS];
+          for (int i = 0; i < RS; ++i) row_f[i] = flux[d][a][KK::row_qpoint(d, i_fq, i)];
+          for (int s = 0; s < 2; ++s) face_f[s] = face(e, 2*d + s, false)[a*nfq + i_fq];
+          k.derivative(row_f, face_f, der);
+          for (int i = 0; i < RS; ++i) {
+            double& x = time_rate[0][a][KK::row_qpoint(d, i_fq, i)];
+            x = 1.*x + -der[i];
+          }
+        }
+      }
+    }
+    const double update_coef = stage ? 1.*k.t.step_ratio : 1.;
+    for (int q = 0; q < nq; ++q) {
+      double mult = update_coef*tss[q]/d_pos;
+      if (deformed) mult /= det[q];
+      const double pseudo = 1 + tss[q]*2/p.advect_length;
+      for (int a = 0; a < n_adv; ++a) {
+        double u = time_rate[0][a][q];
+        if (stage) u -= ref_state[a*nq + q];
+        else {
+          ref_state[a*nq + q] = u;
+          u += time_rate[1][a][q];
+        }
+        u *= mult;
+        double& x = a_st[a*nq + q];
+        if (!stage) x = (x + u)/pseudo;
+        else x += u/pseudo;
+      }
+    }
+    write_face_advection(e);
+  }
+
+  // compute_advection (src/kernels_convective.cpp:8-19) on a conforming mesh, dt = 1
+  void compute_advection(int stage) const
+  {
+    for_connections([&](int s0, int s1, int dir, const double* nrml) { neighbor_advection_con(s0, s1, dir, nrml); });
+    #pragma omp parallel for
+    for (int e = 0; e < m.n_car_elem; ++e) local_advection_elem(e, false, stage);
+    #pragma omp parallel for
+    for (int e = m.n_car_elem; e < n_elem(); ++e) local_advection_elem(e, true, stage);
+  }
+
+  // Spatial<pde::Smooth_art_visc>::Neighbor: the LDG average of the three traces on both sides
+  void neighbor_smooth_av_con(int slot0, int slot1, int dir, const double* nrml) const
+  {
+    const bool deformed = nrml != nullptr;
+    const double* f0 = slot(slot0, false);
+    const double* f1 = slot(slot1, false);
+    double* l0 = slot(slot0, true);
+    double* l1 = slot(slot1, true);
+    for (int q = 0; q < nfq; ++q) {
+      const int q1 = deformed ? KK::perm_index(dir, q) : q;
+      for (int v = 0; v < n_sav; ++v) {
+        double avg = .5*(f0[v*nfq + q] + f1[v*nfq + q1]);
+        l0[v*nfq + q] = avg;
+        l1[v*nfq + q1] = avg;
+      }
+    }
+  }
+
+  // Spatial<pde::Smooth_art_visc>::Local (include/Spatial.hpp:326-509), first stage, for one
+  // element. The unknowns are forcing rows 1-3; their flux is -gradient.normal, diffusivity 1;
+  // the source of unknown i is f(forcing row i)/diff_time with f = |x| for rows 0 and 2 and
+  // sqrt|x| for row 1 (pde.hpp:422-429); write_update adds (pde.hpp:379-387, not critical).
+  void local_smooth_av_elem(int e, bool deformed, double dt, double diff_time) const
+  {
+    double* state = k.elem(e);
+    double* tss = state + nv*nq;
+    double* fc = forcing(e);
+    const double d_pos = m.nom_size[e];
+    const double* nrml = deformed ? jac(e) : nullptr;
+    const double* det = deformed ? jac(e) + ND*ND*nq : nullptr;
+    const double* face_nrml[6] = {};
+    if (deformed) {
+      const int ed = e - m.n_car_elem;
+      for (int i = 0; i < 2*ND; ++i) face_nrml[i] = m.face_nrml + ((size_t)ed*2*ND + i)*ND*nfq;
+    }
+    double time_rate[2][n_sav][nq];
+    double visc_storage[ND][n_sav][nq];
+    for (int v = 0; v < n_sav; ++v) for (int q = 0; q < nq; ++q) {
+      time_rate[0][v][q] = time_rate[1][v][q] = 0.;
+      for (int d = 0; d < ND; ++d) visc_storage[d][v][q] = 0.;
+    }
+    // gradient times the Jacobian determinant (Spatial.hpp:371-402)
+    for (int v = 0; v < n_sav; ++v) for (int q = 0; q < nq; ++q) time_rate[0][v][q] = fc[(1 + v)*nq + q];
+    for (int d = 0; d < ND; ++d) {
+      for (int i_fq = 0; i_fq < nfq; ++i_fq) {
+        double row_r[n_sav][RS], fs[n_sav][2];
+        for (int v = 0; v < n_sav; ++v) {
+          for (int i = 0; i < RS; ++i) row_r[v][i] = time_rate[0][v][KK::row_qpoint(d, i_fq, i)];
+          for (int s = 0; s < 2; ++s) fs[v][s] = face(e, 2*d + s, true)[v*nfq + i_fq];
+        }
+        if (deformed) {
+          for (int j = 0; j < ND; ++j) {
+            double row_n[RS], face_n[2];
+            for (int i = 0; i < RS; ++i) row_n[i] = nrml[(d*ND + j)*nq + KK::row_qpoint(d, i_fq, i)];
+            for (int s = 0; s < 2; ++s) face_n[s] = face_nrml[2*d + s][j*nfq + i_fq];
+            for (int v = 0; v < n_sav; ++v) {
+              double row[RS], bound[2], der[RS];
+              for (int i = 0; i < RS; ++i) row[i] = row_n[i]*row_r[v][i];
+              for (int s = 0; s < 2; ++s) bound[s] = face_n[s]*fs[v][s];
+              k.derivative(row, bound, der);
+              for (int i = 0; i < RS; ++i) {
+                double& x = visc_storage[j][v][KK::row_qpoint(d, i_fq, i)];
+                x = 1.*x + der[i]/d_pos;
+              }
+            }
+          }
+        } else {
+          for (int v = 0; v < n_sav; ++v) {
+            double der[RS];
+            k.derivative(row_r[v], fs[v], der);
+            for (int i = 0; i < RS; ++i) {
+              double& x = visc_storage[d][v][KK::row_qpoint(d, i_fq, i)];
+              x = 0*x + der[i]/d_pos;
+            }
+          }
+        }
+      }
+    }
+    for (int v = 0; v < n_sav; ++v) for (int q = 0; q < nq; ++q) { time_rate[0][v][q] = 0; time_rate[1][v][q] = 0; }
+    // flux and source (Spatial.hpp:405-442)
+    for (int q = 0; q < nq; ++q) {
+      double g[n_sav][ND];
+      for (int d = 0; d < ND; ++d) for (int v = 0; v < n_sav; ++v) g[v][d] = visc_storage[d][v][q];
+      if (deformed) for (int v = 0; v < n_sav; ++v) for (int d = 0; d < ND; ++d) g[v][d] /= det[q];
+      for (int v = 0; v < n_sav; ++v) for (int i = 0; i < ND; ++i) {
+        double acc = 0.;
+        for (int j = 0; j < ND; ++j) acc += -g[v][j]*(deformed ? nrml[(i*ND + j)*nq + q] : (i == j ? 1. : 0.));
+        visc_storage[i][v][q] = acc;
+      }
+      double mult = d_pos;
+      if (deformed) mult *= det[q];
+      for (int v = 0; v < n_sav; ++v) {
+        double f = std::abs(fc[v*nq + q]);
+        time_rate[1][v][q] = mult*(((v == 1) ? std::sqrt(f) : f)/diff_time);
+      }
+    }
+    // residual (Spatial.hpp:445-470): interior divergence of the flux; the flux's face values
+    // go to the LDG faces
+    for (int d = 0; d < ND; ++d) {
+      for (int i_fq = 0; i_fq < nfq; ++i_fq) {
+        for (int v = 0; v < n_sav; ++v) {
+          double row_f[RS], der[RS];
+          for (int i = 0; i < RS; ++i) row_f[i] = visc_storage[d][v][KK::row_qpoint(d, i_fq, i)];
+          for (int s = 0; s < 2; ++s) {
+            double acc = 0.;
+            for (int i = 0; i < RS; ++i) acc += k.t.bound[s*RS + i]*row_f[i];
+            face(e, 2*d + s, true)[v*nfq + i_fq] = acc;
+          }
+          k.derivative_interior(row_f, der);
+          for (int i = 0; i < RS; ++i) {
+            double& x = time_rate[1][v][KK::row_qpoint(d, i_fq, i)];
+            x = 1.*x + -der[i];
+          }
+        }
+      }
+    }
+    for (int q = 0; q < nq; ++q) {
+      double mult = dt*tss[q]/d_pos;
+      if (deformed) mult /= det[q];
+      for (int v = 0; v < n_sav; ++v) {
+        double u = time_rate[0][v][q];
+        u += time_rate[1][v][q];
+        u *= mult;
+        fc[(1 + v)*nq + q] += u;
+      }
+    }
+  }
+
+  // Spatial::Neighbor_reconcile (include/Spatial.hpp:716-759) over the three LDG fluxes
+  void neighbor_reconcile_smooth_av_con(int slot0, int slot1, int dir, const double* nrml) const
+  {
+    const bool deformed = nrml != nullptr;
+    int sign[2];
+    signs(dir, deformed, sign);
+    double* l0 = slot(slot0, true);
+    double* l1 = slot(slot1, true);
+    double out0[n_sav*nfq], out1[n_sav*nfq];
+    for (int q = 0; q < nfq; ++q) {
+      const int q1 = deformed ? KK::perm_index(dir, q) : q;
+      for (int v = 0; v < n_sav; ++v) {
+        double a = l0[v*nfq + q], b = l1[v*nfq + q1];
+        double avg = 0;
+        avg += .5*sign[0]*a;
+        avg += .5*sign[1]*b;
+        out0[v*nfq + q] = sign[0]*avg - a;
+        out1[v*nfq + q1] = sign[1]*avg - b;
+      }
+    }
+    std::memcpy(l0, out0, sizeof(out0));
+    std::memcpy(l1, out1, sizeof(out1));
+  }
+
+  // Spatial<pde::Smooth_art_visc>::Reconcile_ldg_flux (include/Spatial.hpp:543-594): lift of
+  // the flux differences, then the critical write_update: add, then divide by
+  // pseudo = 1 + tss*chebyshev_step/diff_time (pde.hpp:379-387); the traces are re-extrapolated
+  void reconcile_smooth_av_elem(int e, bool deformed, double dt, double diff_time, double cheby) const
+  {
+    double* state = k.elem(e);
+    double* tss = state + nv*nq;
+    double* fc = forcing(e);
+    const double d_pos = m.nom_size[e];
+    const double* det = deformed ? jac(e) + ND*ND*nq : nullptr;
+    double time_rate[n_sav][nq];
+    for (int v = 0; v < n_sav; ++v) for (int q = 0; q < nq; ++q) time_rate[v][q] = 0.;
+    for (int d = 0; d < ND; ++d) {
+      for (int i_fq = 0; i_fq < nfq; ++i_fq) {
+        for (int v = 0; v < n_sav; ++v) {
+          double b0 = face(e, 2*d, true)[v*nfq + i_fq];
+          double b1 = face(e, 2*d + 1, true)[v*nfq + i_fq];
+          for (int i = 0; i < RS; ++i) {
+            double l = 0.;
+            l += k.lift[i][0]*b0;
+            l += k.lift[i][1]*b1;
+            double& x = time_rate[v][KK::row_qpoint(d, i_fq, i)];
+            x = 1.*x + -l;
+          }
+        }
+      }
+    }
+    for (int q = 0; q < nq; ++q) {
+      double mult = dt*tss[q]/d_pos;
+      if (deformed) mult /= det[q];
+      const double pseudo = 1 + tss[q]*cheby/diff_time;
+      for (int v = 0; v < n_sav; ++v) {
+        double& x = fc[(1 + v)*nq + q];
+        x += time_rate[v][q]*mult;
+        x /= pseudo;
+      }
+    }
+    write_face_smooth_av(e);
+  }
+
+  // compute_smooth_av (src/kernels_diffusive.cpp:8-30) on a conforming mesh, first stage
+  void compute_smooth_av(double dt, double diff_time, double cheby) const
+  {
+    for_connections([&](int s0, int s1, int dir, const double* nrml) { neighbor_smooth_av_con(s0, s1, dir, nrml); });
+    #pragma omp parallel for
+    for (int e = 0; e < m.n_car_elem; ++e) local_smooth_av_elem(e, false, dt, diff_time);
+    #pragma omp parallel for
+    for (int e = m.n_car_elem; e < n_elem(); ++e) local_smooth_av_elem(e, true, dt, diff_time);
+    // Solver::apply_avc_diff_flux_bcs -> Flow_bc::flux_diffusion (src/Boundary_condition.cpp:54-60)
+    #pragma omp parallel for
+    for (int i = 0; i < m.n_bc_con; ++i) {
+      const int* c = m.bc_con + 4*i;
+      const double* in = slot(c[0], true);
+      double* gh = slot(c[1], true);
+      for (int k2 = 0; k2 < nv*nfq; ++k2) gh[k2] = -in[k2];
+    }
+    for_connections([&](int s0, int s1, int dir, const double* nrml) {
+      neighbor_reconcile_smooth_av_con(s0, s1, dir, nrml);
+    });
+    #pragma omp parallel for
+    for (int e = 0; e < m.n_car_elem; ++e) reconcile_smooth_av_elem(e, false, dt, diff_time, cheby);
+    #pragma omp parallel for
+    for (int e = m.n_car_elem; e < n_elem(); ++e) reconcile_smooth_av_elem(e, true, dt, diff_time, cheby);
+  }
+
+  // Solver::diffuse_art_visc (src/Solver.cpp:428-455)
+  void diffuse_art_visc(double diff_time) const
+  {
+    max_dt_smooth_av();
+    #pragma omp parallel for
+    for (int e = 0; e < n_elem(); ++e) write_face_smooth_av(e);
+    for (int i_iter = 0; i_iter < p.diff_iters; ++i_iter) {
+      for (int i_cheby = 0; i_cheby < p.n_cheby; ++i_cheby) {
+        const double s = chebyshev_step(p.n_cheby, i_cheby);
+        // Solver::apply_avc_diff_bcs -> Flow_bc::apply_diffusion (src/Boundary_condition.cpp:43-52)
+        #pragma omp parallel for
+        for (int i = 0; i < m.n_bc_con; ++i) {
+          const int* c = m.bc_con + 4*i;
+          const double* in = slot(c[0], false);
+          double* gh = slot(c[1], false);
+          for (int k2 = 0; k2 < nv*nfq; ++k2) gh[k2] = in[k2];
+        }
+        compute_smooth_av(s, diff_time, s);
+      }
+    }
+  }
+
+  // Solver::update_art_visc_smoothness (src/Solver.cpp:457-582); returns art_visc_residual
+  double update() const
+  {
+    const double L = p.advect_length;
+    // advection velocity: momentum / sqrt(2 rho E) (Solver.cpp:468-478)
+    #pragma omp parallel for
+    for (int e = 0; e < n_elem(); ++e) {
+      double* state = k.elem(e);
+      for (int q = 0; q < nq; ++q) {
+        double scale = std::sqrt(2*state[ND*nq + q]*state[(ND + 1)*nq + q]);
+        for (int d = 0; d < ND; ++d) state[d*nq + q] /= scale;
+      }
+    }
+    max_dt_advection();
+    for (int iter = 0; iter < p.advect_iters; ++iter) {
+      #pragma omp parallel for
+      for (int e = 0; e < n_elem(); ++e) write_face_advection(e);
+      for (int i = 0; i < 2; ++i) {
+        #pragma omp parallel for
+        for (int j = 0; j < m.n_bc_con; ++j) apply_advection_bc(j);
+        compute_advection(i);
+      }
+    }
+    // projection onto the Legendre mode of degree av_rs - 1 (Solver.cpp:527-542)
+    const double* orth = k.t.ortho + (size_t)(p.av_row_size - 1)*RS;
+    #pragma omp parallel for
+    for (int e = 0; e < n_elem(); ++e) {
+      double* fc = forcing(e);
+      const double* a_st = adv(e);
+      const double* state = k.elem(e);
+      for (int q = 0; q < nq; ++q) {
+        double proj = 0;
+        for (int i = 0; i < RS; ++i) proj += a_st[i*nq + q]*k.t.weight[i]*orth[i];
+        fc[q] = proj*proj*2*state[(ND + 1)*nq + q]/state[ND*nq + q];
+      }
+    }
+    // root-smear-square (Solver.cpp:544-550)
+    const int n_real = n_forcing - 1;
+    diffuse_art_visc(p.diff_ratio*L*L/n_real);
+    // coefficient, residual and the momentum put back (Solver.cpp:552-575)
+    const double mult = p.visc_mult*L;
+    const double us_max = L*p.unscaled_max*std::sqrt(2*p.freestream_energy/p.freestream_mass);
+    double qw[nq];
+    for (int q = 0; q < nq; ++q) {
+      double w = 1.;
+      for (int d = 0; d < ND; ++d) w *= k.t.weight[(q/ipow(RS, ND - 1 - d))%RS];
+      qw[q] = w;
+    }
+    double resid = 0;
+    for (int e = 0; e < n_elem(); ++e) {
+      double* state = k.elem(e);
+      double* av = state + (nv + 1)*nq;
+      const double* fc = forcing(e);
+      double volume = 1.;
+      for (int d = 0; d < ND; ++d) volume *= m.nom_size[e];
+      for (int q = 0; q < nq; ++q) {
+        double f = mult*fc[n_real*nq + q];
+        double new_av = us_max*f/(us_max + f);
+        double diff = av[q] - new_av;
+        resid += diff*diff*qw[q]*volume;
+        av[q] = new_av;
+        double scale = std::sqrt(2*state[ND*nq + q]*state[(ND + 1)*nq + q]);
+        for (int d = 0; d < ND; ++d) state[d*nq + q] *= scale;
+      }
+    }
+    k.write_face();   // compute_write_face (Solver.cpp:577)
+    return std::sqrt(resid);
+  }
+};
+
 } // namespace
 
 extern "C" {
@@ -1401,6 +2040,34 @@ int oracle_fix_admissibility(const hexed_mesh_desc* m, const hexed_update_params
     else *iterations = it;
   });
   return st != HEXED_OK ? st : ds;
+}
+
+// Face-slot size (doubles) of the smoothness-AV face storage: max(2*nv, nd + row_size)*nfq
+int oracle_sav_slot_dof(int nd, int rs)
+{
+  int r = -1;
+  hexed_mesh_desc m{};
+  m.n_dim = nd; m.row_size = rs;
+  dispatch(&m, [&](auto& k) {
+    using KT = std::remove_reference_t<decltype(k)>;
+    r = Sav<KT::n_dim, KT::row_size>::slot_dof;
+  });
+  return r;
+}
+
+// Solver::update_art_visc_smoothness (src/Solver.cpp:457-582) on a conforming mesh. `aux` is
+// [n_elem][4 + 2*row_size][nq] (forcing, advection state, its residual cache), `face`
+// [n_slot][oracle_sav_slot_dof]; *residual receives art_visc_residual.
+int oracle_update_art_visc_smoothness(const hexed_mesh_desc* m, double* aux, double* face,
+                                      const oracle_sav_params* p, double* residual)
+{
+  if (!m || !aux || !face || !p || !residual || m->n_ref_face > 0 || !m->vert_tss) return HEXED_ERR_INVALID;
+  if (p->av_row_size < 2 || p->av_row_size > m->row_size || !(p->advect_length > 0)) return HEXED_ERR_INVALID;
+  return dispatch(m, [&](auto& k) {
+    using KT = std::remove_reference_t<decltype(k)>;
+    Sav<KT::n_dim, KT::row_size> s(k, aux, face, *p);
+    *residual = s.update();
+  });
 }
 
 // Solver::compute_residual (src/Solver.cpp:899-913)
