@@ -218,7 +218,7 @@ class Oracle:
         self._chk(self.lib.oracle_set_art_visc_admis(ctypes.byref(self.desc), char_speed))
 
     def update_art_visc_smoothness(self, storage, params):
-        """Solver::update_art_visc_smoothness (src/Solver.cpp:457-582) on a conforming mesh:
+        """Solver::update_art_visc_smoothness (src/Solver.cpp:457-582):
         writes the bulk AV row of the arena; returns art_visc_residual."""
         out = ctypes.c_double()
         self._chk(self.lib.oracle_update_art_visc_smoothness(ctypes.byref(self.desc), _inplace(storage.aux),

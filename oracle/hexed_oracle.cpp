@@ -655,18 +655,25 @@ struct K
   // Spatial::Prolong_refined / Restrict_refined (include/Spatial.hpp:153-206, 230-285)
   void refine(bool prolong, bool scale, bool offset) const
   {
+    refine_slots(m.face, n_slot_dof, nv, prolong, scale, offset);
+  }
+
+  // the same over face slots of `slot_stride` doubles from `base` and the first n_var face
+  // variables (the Pde's n_extrap, Spatial.hpp:141, 218); the LDG half starts at nv*nfq
+  void refine_slots(double* base, size_t slot_stride, int n_var, bool prolong, bool scale, bool offset) const
+  {
     const int n_face = 1 << (ND - 1);
     #pragma omp parallel for
     for (int i_ref = 0; i_ref < m.n_ref_face; ++i_ref) {
       const int* rf = m.ref_face + 7*i_ref;
       bool str[2] = {rf[5] != 0, rf[6] != 0};
-      double* coarse = slot(rf[0], false) + offset*nv*nfq;
-      if (!prolong) for (int i = 0; i < nv*nfq; ++i) coarse[i] = 0.;
+      double* coarse = base + (size_t)rf[0]*slot_stride + offset*nv*nfq;
+      if (!prolong) for (int i = 0; i < n_var*nfq; ++i) coarse[i] = 0.;
       int nf = n_face;
       for (int d = 0; d < ND - 1; ++d) nf /= 1 + str[d];
       for (int i_face = 0; i_face < nf; ++i_face) {
-        double* fine = slot(rf[1 + i_face], false) + offset*nv*nfq;
-        for (int v = 0; v < nv; ++v) {
+        double* fine = base + (size_t)rf[1 + i_face]*slot_stride + offset*nv*nfq;
+        for (int v = 0; v < n_var; ++v) {
           double* var_face = fine + v*nfq;
           if (prolong) for (int q = 0; q < nfq; ++q) var_face[q] = coarse[v*nfq + q];
           for (int d = 0; d < ND - 1; ++d) {
@@ -1315,7 +1322,7 @@ double chebyshev_step(int n_steps, int i_step)
 
 // ---------------------------------------------------------------- smoothness-based AV
 // Solver::update_art_visc_smoothness (src/Solver.cpp:457-582): the Spatial kernels applied to
-// pde::Advection and pde::Smooth_art_visc (include/pde.hpp:265-431) on conforming meshes.
+// pde::Advection and pde::Smooth_art_visc (include/pde.hpp:265-431), hanging faces included.
 // Storage beside the arena:
 //  * aux  [n_elem][4 + 2*row_size][nq]: the art_visc_forcing rows (Storage_params::n_forcing
 //    = 4), the advection state (row_size rows) and its residual cache (row_size rows: the
@@ -1359,6 +1366,11 @@ struct Sav
   double* slot(int s, bool ldg) const { return sf + (size_t)s*slot_dof + ldg*nv*nfq; }
   double* face(int e, int i, bool ldg) const { return slot(e*2*ND + i, ldg); }
   int n_elem() const { return k.n_elem(); }
+  // Prolong_refined / Restrict_refined of the Pde's n_extrap face variables on these slots
+  void refine(int n_var, bool prolong, bool scale, bool offset) const
+  {
+    k.refine_slots(sf, slot_dof, n_var, prolong, scale, offset);
+  }
   const double* jac(int e) const { return m.jac + (size_t)(e - m.n_car_elem)*(ND*ND + 1)*nq; }
 
   // mesh spacing at a qpoint: math::interp of the vertex time-step scales (include/math.hpp:207-218)
@@ -1614,14 +1626,16 @@ struct Sav
     write_face_advection(e);
   }
 
-  // compute_advection (src/kernels_convective.cpp:8-19) on a conforming mesh, dt = 1
+  // compute_advection (src/kernels_convective.cpp:8-19), dt = 1
   void compute_advection(int stage) const
   {
     for_connections([&](int s0, int s1, int dir, const double* nrml) { neighbor_advection_con(s0, s1, dir, nrml); });
+    refine(n_adv_extrap, false, true, false);
     #pragma omp parallel for
     for (int e = 0; e < m.n_car_elem; ++e) local_advection_elem(e, false, stage);
     #pragma omp parallel for
     for (int e = m.n_car_elem; e < n_elem(); ++e) local_advection_elem(e, true, stage);
+    refine(n_adv_extrap, true, false, false);
   }
 
   // Spatial<pde::Smooth_art_visc>::Neighbor: the LDG average of the three traces on both sides
@@ -1816,14 +1830,17 @@ struct Sav
     write_face_smooth_av(e);
   }
 
-  // compute_smooth_av (src/kernels_diffusive.cpp:8-30) on a conforming mesh, first stage
+  // compute_smooth_av (src/kernels_diffusive.cpp:8-30), first stage
   void compute_smooth_av(double dt, double diff_time, double cheby) const
   {
     for_connections([&](int s0, int s1, int dir, const double* nrml) { neighbor_smooth_av_con(s0, s1, dir, nrml); });
+    refine(n_sav, false, true, false);
+    refine(n_sav, false, false, true);
     #pragma omp parallel for
     for (int e = 0; e < m.n_car_elem; ++e) local_smooth_av_elem(e, false, dt, diff_time);
     #pragma omp parallel for
     for (int e = m.n_car_elem; e < n_elem(); ++e) local_smooth_av_elem(e, true, dt, diff_time);
+    refine(n_sav, true, true, true);
     // Solver::apply_avc_diff_flux_bcs -> Flow_bc::flux_diffusion (src/Boundary_condition.cpp:54-60)
     #pragma omp parallel for
     for (int i = 0; i < m.n_bc_con; ++i) {
@@ -1835,10 +1852,12 @@ struct Sav
     for_connections([&](int s0, int s1, int dir, const double* nrml) {
       neighbor_reconcile_smooth_av_con(s0, s1, dir, nrml);
     });
+    refine(n_sav, false, true, true);
     #pragma omp parallel for
     for (int e = 0; e < m.n_car_elem; ++e) reconcile_smooth_av_elem(e, false, dt, diff_time, cheby);
     #pragma omp parallel for
     for (int e = m.n_car_elem; e < n_elem(); ++e) reconcile_smooth_av_elem(e, true, dt, diff_time, cheby);
+    refine(n_sav, true, false, false);
   }
 
   // Solver::diffuse_art_visc (src/Solver.cpp:428-455)
@@ -1847,6 +1866,7 @@ struct Sav
     max_dt_smooth_av();
     #pragma omp parallel for
     for (int e = 0; e < n_elem(); ++e) write_face_smooth_av(e);
+    refine(nv, true, false, false);   // compute_prolong: the flow's n_extrap = nv variables
     for (int i_iter = 0; i_iter < p.diff_iters; ++i_iter) {
       for (int i_cheby = 0; i_cheby < p.n_cheby; ++i_cheby) {
         const double s = chebyshev_step(p.n_cheby, i_cheby);
@@ -1880,6 +1900,7 @@ struct Sav
     for (int iter = 0; iter < p.advect_iters; ++iter) {
       #pragma omp parallel for
       for (int e = 0; e < n_elem(); ++e) write_face_advection(e);
+      refine(n_adv_extrap, true, false, false);   // compute_prolong_advection
       for (int i = 0; i < 2; ++i) {
         #pragma omp parallel for
         for (int j = 0; j < m.n_bc_con; ++j) apply_advection_bc(j);
@@ -1928,7 +1949,8 @@ struct Sav
         for (int d = 0; d < ND; ++d) state[d*nq + q] *= scale;
       }
     }
-    k.write_face();   // compute_write_face (Solver.cpp:577)
+    k.write_face();   // compute_write_face and compute_prolong (Solver.cpp:577-578)
+    k.refine(true, false, false);
     return std::sqrt(resid);
   }
 };
@@ -2055,13 +2077,13 @@ int oracle_sav_slot_dof(int nd, int rs)
   return r;
 }
 
-// Solver::update_art_visc_smoothness (src/Solver.cpp:457-582) on a conforming mesh. `aux` is
+// Solver::update_art_visc_smoothness (src/Solver.cpp:457-582). `aux` is
 // [n_elem][4 + 2*row_size][nq] (forcing, advection state, its residual cache), `face`
 // [n_slot][oracle_sav_slot_dof]; *residual receives art_visc_residual.
 int oracle_update_art_visc_smoothness(const hexed_mesh_desc* m, double* aux, double* face,
                                       const oracle_sav_params* p, double* residual)
 {
-  if (!m || !aux || !face || !p || !residual || m->n_ref_face > 0 || !m->vert_tss) return HEXED_ERR_INVALID;
+  if (!m || !aux || !face || !p || !residual || !m->vert_tss) return HEXED_ERR_INVALID;
   if (p->av_row_size < 2 || p->av_row_size > m->row_size || !(p->advect_length > 0)) return HEXED_ERR_INVALID;
   return dispatch(m, [&](auto& k) {
     using KT = std::remove_reference_t<decltype(k)>;

@@ -149,14 +149,21 @@ def test_invalid_arguments():
         o.update_art_visc_smoothness(st, oracle.sav_params(0.1, 4, 1., 1.5))
 
 
-def test_hanging_faces_refused():
-    """The restatement covers conforming meshes; a mesh with refined faces is refused."""
+@pytest.mark.parametrize("nd", [2, 3])
+def test_hanging_faces_uniform_flow(nd):
+    """On a tree mesh with hanging faces, a uniform flow keeps the advected scalars at 1 and
+    the coefficient at zero: prolongation is exact for constants and the coarse face's flux is
+    the restriction of the fine fluxes (Spatial.hpp:138-285)."""
     from hexed_gb300 import problems
     from hexed_gb300.tree import tree_mesh
-    fs = problems.freestream_state(2, 0.3, 0., 1.2, 1e5)
+    fs = problems.freestream_state(nd, 0.3, 20., 1.2, 1e5)
     spec = bc_spec(abi.BC_FREESTREAM, freestream=fs)
-    ar = tree_mesh(2, 4, 2, 2, problems.sphere_refinement(2, 0.3), {(d, s): spec for d in range(2) for s in range(2)})
+    ar = tree_mesh(nd, 4, 2, 2, problems.sphere_refinement(nd, 0.3), {(d, s): spec for d in range(nd) for s in range(2)})
     assert len(ar.ref_face) > 0
-    ar.set_state(lambda pos: np.stack([fs[0] + 0 * pos[0], 0 * pos[0], fs[2] + 0 * pos[0], fs[3] + 0 * pos[0]]))
-    with pytest.raises(RuntimeError):
-        oracle.Oracle(ar).update_art_visc_smoothness(oracle.SavStorage(ar), oracle.sav_params(0.1, 4, fs[2], fs[3]))
+    ar.set_state(lambda pos: np.stack([fs[v] + 0 * pos[0] for v in range(nd + 2)]))
+    st = oracle.SavStorage(ar)
+    p = oracle.sav_params(0.2, 4, fs[nd], fs[nd + 1], advect_iters=40, diff_iters=20)
+    resid = oracle.Oracle(ar).update_art_visc_smoothness(st, p)
+    assert np.isfinite(resid)
+    np.testing.assert_allclose(st.advection, 1., rtol=0, atol=1e-12)
+    assert np.abs(ar.elem[:, ar.nv + 1]).max() < 1e-12
