@@ -167,3 +167,23 @@ def test_hanging_faces_uniform_flow(nd):
     assert np.isfinite(resid)
     np.testing.assert_allclose(st.advection, 1., rtol=0, atol=1e-12)
     assert np.abs(ar.elem[:, ar.nv + 1]).max() < 1e-12
+
+
+@pytest.mark.parametrize("nd", [2, 3])
+def test_curved_mesh_uniform_flow(nd):
+    """Deformed elements with a smooth non-affine mapping (reference-level normals and
+    determinants that vary over the element): a uniform flow keeps the advected scalars at 1
+    and the coefficient at roundoff, i.e. the advection operator preserves a uniform state
+    through the metric terms."""
+    from hexed_gb300 import problems
+    fs = problems.freestream_state(nd, 0.3, 20., 1.2, 1e5)
+    spec = bc_spec(abi.BC_FREESTREAM, freestream=fs)
+    ar = structured_mesh(nd, 4, 4, 0., 1., deformed=True,
+                         displacement=problems.sinusoid_displacement(1. / 4, 0.1, 0, n_dim=nd),
+                         bcs={(d, s): spec for d in range(nd) for s in range(2)})
+    ar.set_state(lambda pos: np.stack([fs[v] + 0 * pos[0] for v in range(nd + 2)]))
+    st = oracle.SavStorage(ar)
+    p = oracle.sav_params(0.2, 4, fs[nd], fs[nd + 1], advect_iters=40, diff_iters=20)
+    oracle.Oracle(ar).update_art_visc_smoothness(st, p)
+    np.testing.assert_allclose(st.advection, 1., rtol=0, atol=1e-12)
+    assert np.abs(ar.elem[:, ar.nv + 1]).max() < 1e-10
