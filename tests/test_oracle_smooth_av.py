@@ -187,3 +187,17 @@ def test_curved_mesh_uniform_flow(nd):
     oracle.Oracle(ar).update_art_visc_smoothness(st, p)
     np.testing.assert_allclose(st.advection, 1., rtol=0, atol=1e-12)
     assert np.abs(ar.elem[:, ar.nv + 1]).max() < 1e-10
+
+
+def test_chebyshev_substeps_same_steady_state():
+    """n_cheby_av > 1 splits each diffusion iteration into Chebyshev sub-steps
+    (src/Solver.cpp:447-454); the pseudo-time steady state does not depend on the split, so
+    converged coefficients agree."""
+    out = []
+    for n_cheby, iters in ((1, 2400), (3, 800)):
+        ar = strip(4, (10, 2))
+        tanh_state(ar, 0.1)
+        av, _ = run(ar, oracle.SavStorage(ar), 0.1, advect_iters=2000, diff_iters=iters, n_cheby=n_cheby)
+        out.append(av)
+    assert out[0].max() > 0
+    np.testing.assert_allclose(out[1], out[0], rtol=0, atol=1e-10 * out[0].max())
