@@ -7,8 +7,9 @@ generated C++ file. This script runs that generator unmodified from a temporary 
 the emitted ``Gauss_legendre.cpp`` and stores every table as JSON, in the reference's
 storage order (column-major for square matrices, ``[side][node]`` for ``boundary``).
 
-It needs the reference checkout and sympy, so it runs only in the build container:
-    python tests/golden/make_basis_golden.py [/path/to/reference]
+It needs the reference checkout and sympy. Give the checkout's root as the argument or in
+HEXED_REFERENCE_ROOT:
+    python tests/golden/make_basis_golden.py /path/to/hexed
 """
 import json
 import os
@@ -23,7 +24,10 @@ OUT = os.path.join(HERE, "gauss_legendre_ref.json")
 MAX_ROW_SIZE = 8
 
 
-def main(ref_root="/root/reference"):
+def main(ref_root=None):
+    ref_root = ref_root or os.environ.get("HEXED_REFERENCE_ROOT")
+    if not ref_root:
+        sys.exit("usage: make_basis_golden.py /path/to/hexed (or set HEXED_REFERENCE_ROOT)")
     with tempfile.TemporaryDirectory() as tmp:
         script = os.path.join(tmp, "script")
         shutil.copytree(os.path.join(ref_root, "script"), script)

@@ -70,6 +70,44 @@ def group_rel(x, y, nv, axis):
     return float(out)
 
 
+def _quantity_scales(y, nv, norm):
+    """Scale of each variable's conserved quantity (rows of y, variable axis first): for a
+    momentum component the norm of the momentum vector (all its components together), for
+    density and energy their own norm, for rows beyond nv (time-step scale, AV) their own."""
+    own = [norm(yv) for yv in y]
+    mom = norm(y[:nv - 2]) if nv else 0.
+    return [mom if v < nv - 2 else own[v] for v in range(len(y))], own
+
+
+def per_variable_rel(x, y, axis=1, nv=None):
+    """Max-norm error of each variable on its own (every momentum component separately):
+    max |x_v - y_v| over S_v. With nv given, S_v is the scale of the variable's conserved
+    quantity (_quantity_scales: a momentum component against the momentum vector's largest
+    magnitude); without, S_v = max |y_v|. A variable whose scale is zero reports its absolute
+    error."""
+    x = np.moveaxis(np.asarray(x), axis, 0)
+    y = np.moveaxis(np.asarray(y), axis, 0)
+    scales, _ = _quantity_scales(y, nv, lambda a: float(np.abs(a).max())) if nv else \
+        ([float(np.abs(yv).max()) for yv in y], None)
+    out = []
+    for xv, yv, sc in zip(x, y, scales):
+        diff = float(np.abs(xv - yv).max())
+        out.append(diff / sc if sc > 0 else diff)
+    return out
+
+
+def l2_per_variable(x, y, axis=1, nv=None):
+    """L2 error of each variable on its own, relative to the L2 norm of its scale (as in
+    per_variable_rel: the momentum vector's for a momentum component when nv is given, else
+    the variable's own)."""
+    x = np.moveaxis(np.asarray(x), axis, 0)
+    y = np.moveaxis(np.asarray(y), axis, 0)
+    scales, _ = _quantity_scales(y, nv, lambda a: float(np.linalg.norm(a))) if nv else \
+        ([float(np.linalg.norm(yv)) for yv in y], None)
+    return [float(np.linalg.norm(xv - yv) / sc) if sc > 0 else float(np.linalg.norm(xv - yv))
+            for xv, yv, sc in zip(x, y, scales)]
+
+
 def compare_arenas(a, b, tol=FP64_TOL, what=("elem", "rcache", "face", "bc_cache")):
     """Relative errors of GPU arena `b` against oracle arena `a` (see group_rel)."""
     errs = {}
