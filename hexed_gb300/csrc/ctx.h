@@ -97,9 +97,12 @@ struct Ctx {
   // mean conserved state of the initial state)
   float* face_f; float* rcache_f; float* nrm_f; float* face_nrml_f; float* def_con_nrml_f; float* bc_nrml_f;
   double* ref_state;
-  // its terms in float for the offset fluxes (RefState: state, velocity, |v|^2, enthalpy),
-  // [n_elem][2 nd + 4], refreshed whenever ref_state changes
+  // its terms in float for the offset fluxes (RefState: state and its rounding error, velocity,
+  // |v|^2, enthalpy, 1/density), [n_elem][3 nd + 7], refreshed whenever ref_state changes
   float* ref_terms;
+  // element of each slot beyond the element slots (ghost: the inside element; hanging-face
+  // mortar: the coarse element), whose reference state the slot's traces are offsets from
+  int* slot_elem;
   int* record;           // per-element admissibility records [cap elements] (allocated at creation)
   // launch shape: volume-kernel variant (elements per CTA, see Runner::epb_of) and threads
   // per CTA of the face kernels

@@ -410,21 +410,36 @@ int hexed_gpu_create(const hexed_mesh_desc* d, int precision, hexed_gpu_ctx** ou
     if (!st) st = narrow_copy(c, c->face_nrml, &c->face_nrml_f, (long)c->n_def*2*nd*nd*c->nfq);
     if (!st) st = narrow_copy(c, c->def_con_nrml, &c->def_con_nrml_f, (long)c->n_def_con*nd*c->nfq);
     if (!st) st = narrow_copy(c, c->bc_nrml, &c->bc_nrml_f, (long)c->n_bc_con*nd*c->nfq);
-    // reference state of every element: the mean conserved state of the initial state (zero
-    // without one; hexed_gpu_set_reference_state or HEXED_ARRAY_REF_STATE set it then)
-    std::vector<double> mean(c->nv, 0.), refs;
+    // reference state of every element: the mean of its own initial state over its quadrature
+    // points (zero without one; hexed_gpu_set_reference_state or HEXED_ARRAY_REF_STATE set it
+    // then), so that the FP32 offsets carry only the variation inside the element
+    std::vector<double> refs(n_elem*c->nv, 0.);
     const size_t nq_ = c->nq, nv_ = c->nv;
     for (size_t e = 0; d->elem && e < n_elem; ++e)
-      for (size_t v = 0; v < nv_; ++v)
-        for (size_t q = 0; q < nq_; ++q) mean[v] += d->elem[(e*(nv_ + 3) + v)*nq_ + q];
-    for (size_t v = 0; v < nv_; ++v) mean[v] /= double(n_elem*nq_);
-    refs.resize(n_elem*nv_);
-    for (size_t e = 0; e < n_elem; ++e)
-      for (size_t v = 0; v < nv_; ++v) refs[e*nv_ + v] = mean[v];
+      for (size_t v = 0; v < nv_; ++v) {
+        double sum = 0.;
+        for (size_t q = 0; q < nq_; ++q) sum += d->elem[(e*(nv_ + 3) + v)*nq_ + q];
+        refs[e*nv_ + v] = sum/double(nq_);
+      }
     if (!st) st = upload_array(&c->ref_state, refs.data(), refs.size(), "reference state");
-    if (!st && cudaMalloc((void**)&c->ref_terms, n_elem*(2*nd + 4)*sizeof(float)) != cudaSuccess)
+    if (!st && cudaMalloc((void**)&c->ref_terms, n_elem*(3*nd + 7)*sizeof(float)) != cudaSuccess)
       st = fail(HEXED_ERR_ALLOC, "reference-term allocation failed");
     if (!st) c->ops->ref_terms(*c);
+    // owners of the slots beyond the element slots: boundary ghosts take the inside element,
+    // hanging-face mortars the coarse element
+    const size_t elem_slots = n_elem*2*nd;
+    std::vector<int> owner(c->n_slot > (int)elem_slots ? c->n_slot - elem_slots : 1, 0);
+    for (int i = 0; i < c->n_bc_con; ++i) {
+      const int* r = d->bc_con + 4*i;
+      if (r[1] >= (int)elem_slots) owner[r[1] - elem_slots] = r[0]/int(2*nd);
+    }
+    for (int i = 0; i < c->n_ref; ++i) {
+      const int* r = d->ref_face + 7*i;
+      int n_fine = 1 << (nd - 1);
+      for (size_t k = 0; k + 1 < nd; ++k) n_fine /= 1 + (r[5 + k] != 0);
+      for (int k = 1; k <= n_fine; ++k) if (r[k] >= (int)elem_slots) owner[r[k] - elem_slots] = r[0]/int(2*nd);
+    }
+    if (!st) st = upload_array(&c->slot_elem, owner.data(), owner.size(), "slot owners");
   }
   if (!st && c->n_def) {
     if (cudaMalloc((void**)&c->inv_det, (size_t)c->n_def*c->nq*sizeof(double)) != cudaSuccess) {
@@ -464,7 +479,7 @@ int hexed_gpu_destroy(hexed_gpu_ctx* c)
                   c->def_con, c->def_con_nrml, c->bc_con, c->bc_nrml, c->bc_cache, c->ref_face, c->bc_spec,
                   c->scalars, c->partials, c->status, c->dt_ticket, c->d_norm, c->vert_id, c->uncert, c->vmax,
                   c->seg_table, c->seg_out, c->inv_det, c->face_f, c->rcache_f, c->nrm_f, c->face_nrml_f,
-                  c->def_con_nrml_f, c->bc_nrml_f, c->ref_state, c->ref_terms, c->record};
+                  c->def_con_nrml_f, c->bc_nrml_f, c->ref_state, c->ref_terms, c->record, c->slot_elem};
   for (void* p : ptrs) if (p) cudaFree(p);
   if (c->graph) {
     if (c->graph->exec) cudaGraphExecDestroy(c->graph->exec);

@@ -71,6 +71,11 @@ struct Dev {
   // fluxes its kernels form, are differences from it (see RefState). Null in the FP64 form.
   const double* ref;
   const float* ref_terms;   // mixed form: RefState<ND, float> of each element
+  // Mixed form: slots at or beyond elem_slot_end (boundary ghost faces, hanging-face mortars)
+  // belong to no element; slot_elem[slot - elem_slot_end] is the element whose reference
+  // state their traces are offsets from (the inside element, the coarse element)
+  int elem_slot_end;
+  const int* slot_elem;
   double* scalars;       // [0] dt of the current stage, [1] raw max_dt, ...
   double* partials;      // per-block reduction scratch
   int* status;           // device-side error flags
@@ -206,17 +211,28 @@ __device__ __forceinline__ R char_speed(const R* s, R inv_mass) // pde.hpp:161-1
 }
 
 // Reference state of the mixed form and the parts of its flux the offset flux needs.
+// Each element has its own reference (by default the mean of its initial state), so the
+// offsets carry only the variation inside the element. `lo` is the rounding error of `s`: the
+// double reference is s + lo to about 2^-48 relative, so the difference of two elements'
+// references, (s1 - s0) + (lo1 - lo0), has the relative accuracy of float whatever the
+// references' size (the face kernels convert traces between neighbouring elements with it).
 template <int ND, typename R>
 struct RefState {
   R s[ND + 2];   // conserved reference state
+  R lo[ND + 2];  // ref - s (zero in double)
   R v[ND];       // its velocity
   R v_sq;        // |v|^2
   R h;           // E + p
+  R inv_mass;    // 1/density
   __device__ __forceinline__ void set(const double* ref)
   {
     #pragma unroll
-    for (int i = 0; i < ND + 2; ++i) s[i] = to_R<R>(ref[i]);
+    for (int i = 0; i < ND + 2; ++i) {
+      s[i] = to_R<R>(ref[i]);
+      lo[i] = to_R<R>(ref[i] - double(s[i]));
+    }
     const R inv = R(1)/s[ND];
+    inv_mass = inv;
     v_sq = 0;
     #pragma unroll
     for (int j = 0; j < ND; ++j) { v[j] = s[j]*inv; v_sq += v[j]*v[j]; }
@@ -233,7 +249,7 @@ __global__ void k_ref_terms(const double* ref, int n_elem, RefState<ND, float>* 
 }
 
 // f(u).n - f(u_ref).n of the convective flux (pde.hpp:108-122) from the offset state
-// d = u - u_ref, with c the Conv of the full state u. Every term is an offset times a bounded
+// d = u - u_ref, with inv_mass = 1/u[ND] of the full state u. Every term is an offset times a bounded
 // factor, so in float the result carries the relative accuracy of the offsets and not of the
 // full fluxes (no difference of nearly equal fluxes is formed):
 //   dv = (dm - v_ref drho)/rho, dp = (gamma-1)(dE - (drho |v_ref|^2 + rho (v + v_ref).dv)/2),
@@ -241,15 +257,15 @@ __global__ void k_ref_terms(const double* ref, int n_elem, RefState<ND, float>* 
 // The reference flux itself drops out of the scheme: its volume derivative and its face
 // terms cancel by the discrete metric identity (free-stream preservation).
 template <int ND, typename R>
-__device__ __forceinline__ void flux_delta(const R* u, const R* d, const RefState<ND, R>& r, const Conv<ND, R>& c,
+__device__ __forceinline__ void flux_delta(const R* u, const R* d, const RefState<ND, R>& r, R inv_mass,
                                            const R* n, R* f)
 {
   R v[ND], dv[ND];
   R dkin2 = d[ND]*r.v_sq;
   #pragma unroll
   for (int j = 0; j < ND; ++j) {
-    v[j] = u[j]*c.inv_mass;
-    dv[j] = (d[j] - r.v[j]*d[ND])*c.inv_mass;
+    v[j] = u[j]*inv_mass;
+    dv[j] = (d[j] - r.v[j]*d[ND])*inv_mass;
     dkin2 += u[ND]*(v[j] + r.v[j])*dv[j];
   }
   const R dp = R(heat_rat - 1.)*(d[ND + 1] - R(.5)*dkin2);
@@ -958,7 +974,7 @@ __device__ __forceinline__ void local_body_points(Dev<FaceT> m, const Tab<RS>& t
       if (VISC && m.fta) {
         #pragma unroll
         for (int v = 0; v < nv; ++v) f[v] = R(0);   // Fix_therm_admis has no convection
-      } else if constexpr (split) flux_delta<ND, R>(u, up, rs, c, col, f);
+      } else if constexpr (split) flux_delta<ND, R>(u, up, rs, c.inv_mass, col, f);
       else c.flux(u, col, f);
       #pragma unroll
       for (int v = 0; v < nv; ++v) my_f[(i*nv + v)*nq + q] = f[v];
@@ -1358,7 +1374,7 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
       if (VISC && m.fta) {
         #pragma unroll
         for (int v = 0; v < nv; ++v) f[v] = R(0);   // Fix_therm_admis has no convection
-      } else if constexpr (split) flux_delta<ND, R>(u, up, rs, c, col, f);
+      } else if constexpr (split) flux_delta<ND, R>(u, up, rs, c.inv_mass, col, f);
       else c.flux(u, col, f);
       #pragma unroll
       for (int v = 0; v < nv; ++v) s_x[((le*ND + i)*nv + v)*nq + q] = f[v];
@@ -1687,23 +1703,48 @@ k_reconcile_ldg(Dev<FaceT> m, Tab<RS> tab, RowTab<RS, R> rt, int e_begin, int e_
 }
 
 // ------------------------------------------------------------------- Neighbor
+// Element whose reference state the traces of a face slot are offsets from (mixed form).
+template <int ND, typename FaceT>
+__device__ __forceinline__ int slot_owner(const Dev<FaceT>& m, int slot)
+{
+  return slot < m.elem_slot_end ? slot/(2*ND) : m.slot_elem[slot - m.elem_slot_end];
+}
+
 // Spatial::Neighbor (include/Spatial.hpp:613-705): local Lax-Friedrichs flux written back
 // to both faces with sign; LDG face average for the viscous path. One thread per face qpoint.
+// same_ref: both slots are offsets from one reference (a boundary connection: the ghost face
+// takes the inside element's).
 template <int ND, int RS, typename R, typename FaceT>
 __device__ __forceinline__ void neighbor_point(const Dev<FaceT>& m, int slot0, int slot1, int dir, int q,
-                                               const FaceT* nrml, bool viscous, const double* ghost_override)
+                                               const FaceT* nrml, bool viscous, const double* ghost_override,
+                                               bool same_ref)
 {
   using S = Shape<ND, RS>;
   constexpr int nfq = S::nfq, nv = S::nv;
-  // mixed form: traces are offsets from the reference state of the connection's elements
-  // (one solve, one reference) and so are the fluxes (flux_delta); nothing here needs double
+  // Mixed form: each side's traces are offsets from its own element's reference state. Side 1
+  // is expressed in side 0's reference by adding the difference of the references, formed
+  // from their float high and low parts (RefState::lo) so that it keeps float's relative
+  // accuracy; the numerical flux is then the offset flux of side 0, and side 1 receives it
+  // minus f(ref1).n - f(ref0).n, itself an offset flux. Nothing here needs double.
   constexpr bool split = !std::is_same<FaceT, double>::value;
   RefState<ND, R> rs;
-  int e_ref = 0;
+  R delta[nv];   // ref1 - ref0
+  bool cross = false;
+  int e_ref = 0, e_ref1 = 0;
   if constexpr (split) {
-    const int n_elem_slots = m.n_elem*2*ND;
-    e_ref = slot0 < n_elem_slots ? slot0/(2*ND) : slot1 < n_elem_slots ? slot1/(2*ND) : 0;
-    rs = reinterpret_cast<const RefState<ND, R>*>(m.ref_terms)[e_ref];
+    e_ref = slot_owner<ND>(m, slot0);
+    e_ref1 = same_ref ? e_ref : slot_owner<ND>(m, slot1);
+    const RefState<ND, R>* terms = reinterpret_cast<const RefState<ND, R>*>(m.ref_terms);
+    rs = terms[e_ref];
+    cross = e_ref1 != e_ref;
+    if (cross) {
+      const RefState<ND, R> r1 = terms[e_ref1];
+      #pragma unroll
+      for (int v = 0; v < nv; ++v) delta[v] = (r1.s[v] - rs.s[v]) + (r1.lo[v] - rs.lo[v]);
+    } else {
+      #pragma unroll
+      for (int v = 0; v < nv; ++v) delta[v] = R(0);
+    }
   }
   const bool deformed = nrml != nullptr;
   int sign0 = 1, sign1 = 1;
@@ -1714,12 +1755,12 @@ __device__ __forceinline__ void neighbor_point(const Dev<FaceT>& m, int slot0, i
   const int q1 = deformed ? perm_index<ND, RS>(dir, q) : q;
   FaceT* f0 = m.face + (size_t)slot0*S::slot_dof;
   FaceT* f1 = m.face + (size_t)slot1*S::slot_dof;
-  R o0[nv], o1[nv], jump[nv];   // offset-form traces and their jump
+  R o0[nv], o1[nv], jump[nv];   // offset-form traces (both from side 0's reference) and their jump
   #pragma unroll
   for (int v = 0; v < nv; ++v) {
     if constexpr (split) {
       o0[v] = R(f0[v*nfq + q]);
-      o1[v] = ghost_override ? offset_var<ND, R>(m, e_ref, v, ghost_override[v]) : R(f1[v*nfq + q1]);
+      o1[v] = ghost_override ? offset_var<ND, R>(m, e_ref, v, ghost_override[v]) : R(f1[v*nfq + q1]) + delta[v];
       jump[v] = o0[v] - o1[v];
     } else {
       const double a = double(f0[v*nfq + q]);
@@ -1734,7 +1775,7 @@ __device__ __forceinline__ void neighbor_point(const Dev<FaceT>& m, int slot0, i
     for (int v = 0; v < nv; ++v) {
       R avg = R(.5)*(o0[v] + o1[v]);
       f0[nv*nfq + v*nfq + q] = FaceT(avg);
-      f1[nv*nfq + v*nfq + q1] = FaceT(avg);
+      f1[nv*nfq + v*nfq + q1] = FaceT(split ? avg - delta[v] : avg);
     }
     if (m.fta) return;   // Fix_therm_admis has no convection (Spatial.hpp:655-686 are skipped)
   }
@@ -1748,11 +1789,18 @@ __device__ __forceinline__ void neighbor_point(const Dev<FaceT>& m, int slot0, i
   const int i_dim0 = dir & 3;
   #pragma unroll
   for (int d = 0; d < ND; ++d) n[d] = deformed ? R(sign0)*R(nrml[d*nfq + q]) : (d == i_dim0 ? R(1) : R(0));
-  R fl0[nv], fl1[nv];
+  R fl0[nv], fl1[nv], dref[nv];
   Conv<ND, R> c0(u0), c1(u1);
   if constexpr (split) {
-    flux_delta<ND, R>(u0, o0, rs, c0, n, fl0);
-    flux_delta<ND, R>(u1, o1, rs, c1, n, fl1);
+    flux_delta<ND, R>(u0, o0, rs, c0.inv_mass, n, fl0);
+    flux_delta<ND, R>(u1, o1, rs, c1.inv_mass, n, fl1);
+    // f(ref1).n - f(ref0).n, the offset flux of side 1's reference from side 0's
+    #pragma unroll
+    for (int v = 0; v < nv; ++v) dref[v] = R(0);
+    if (cross) {
+      const RefState<ND, R> r1 = reinterpret_cast<const RefState<ND, R>*>(m.ref_terms)[e_ref1];
+      flux_delta<ND, R>(r1.s, delta, rs, r1.inv_mass, n, dref);
+    }
   } else {
     c0.flux(u0, n, fl0);
     c1.flux(u1, n, fl1);
@@ -1766,7 +1814,7 @@ __device__ __forceinline__ void neighbor_point(const Dev<FaceT>& m, int slot0, i
   for (int v = 0; v < nv; ++v) {
     R flux = R(.5)*(fl0[v] + fl1[v] + mult*jump[v]);
     f0[v*nfq + q] = FaceT(R(sign0)*flux);
-    f1[v*nfq + q1] = FaceT(R(sign1)*flux);
+    f1[v*nfq + q1] = FaceT(R(sign1)*(split ? flux - dref[v] : flux));
   }
 }
 
@@ -1781,10 +1829,12 @@ __global__ void k_neighbor(Dev<FaceT> m)
     const int i = int(t/nfq), q = int(t%nfq);
     if constexpr (DEF) {
       const int* c = m.def_con + 3*i;
-      neighbor_point<ND, RS, R, FaceT>(m, c[0], c[1], c[2], q, m.def_con_nrml + (size_t)i*ND*nfq, VISC, nullptr);
+      neighbor_point<ND, RS, R, FaceT>(m, c[0], c[1], c[2], q, m.def_con_nrml + (size_t)i*ND*nfq, VISC, nullptr,
+                                       false);
     } else {
       const int* c = m.car_con + 3*i;
-      neighbor_point<ND, RS, R, FaceT>(m, c[0], c[1], c[2] | (c[2] << 2) | (1 << 4), q, nullptr, VISC, nullptr);
+      neighbor_point<ND, RS, R, FaceT>(m, c[0], c[1], c[2] | (c[2] << 2) | (1 << 4), q, nullptr, VISC, nullptr,
+                                       false);
     }
   }
 }
@@ -2091,7 +2141,7 @@ __global__ void k_bc_neighbor(Dev<FaceT> m)
       bc_state_point<ND, RS, FaceT>(m, i, q, gh);
       ov = gh;
     }
-    neighbor_point<ND, RS, R, FaceT>(m, c[0], c[1], bc_dir(c[2]), q, m.bc_nrml_t + (size_t)i*ND*nfq, VISC, ov);
+    neighbor_point<ND, RS, R, FaceT>(m, c[0], c[1], bc_dir(c[2]), q, m.bc_nrml_t + (size_t)i*ND*nfq, VISC, ov, true);
   }
 }
 
@@ -2111,7 +2161,8 @@ __global__ void k_neighbor_car_bc(Dev<FaceT> m, int car_blocks)
     for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)car_blocks*blockDim.x) {
       const int i = int(t/nfq), q = int(t%nfq);
       const int* c = m.car_con + 3*i;
-      neighbor_point<ND, RS, R, FaceT>(m, c[0], c[1], c[2] | (c[2] << 2) | (1 << 4), q, nullptr, VISC, nullptr);
+      neighbor_point<ND, RS, R, FaceT>(m, c[0], c[1], c[2] | (c[2] << 2) | (1 << 4), q, nullptr, VISC, nullptr,
+                                       false);
     }
   } else {
     if ((int)threadIdx.x >= bc_warp) return;
@@ -2126,7 +2177,7 @@ __global__ void k_neighbor_car_bc(Dev<FaceT> m, int car_blocks)
         bc_state_point<ND, RS, FaceT>(m, i, q, gh);
         ov = gh;
       }
-      neighbor_point<ND, RS, R, FaceT>(m, c[0], c[1], bc_dir(c[2]), q, m.bc_nrml_t + (size_t)i*ND*nfq, VISC, ov);
+      neighbor_point<ND, RS, R, FaceT>(m, c[0], c[1], bc_dir(c[2]), q, m.bc_nrml_t + (size_t)i*ND*nfq, VISC, ov, true);
     }
   }
 }

@@ -41,11 +41,15 @@ struct Runner
       m.def_con_nrml = c.def_con_nrml; m.bc_nrml_t = c.bc_nrml;
       m.ref = nullptr;
       m.ref_terms = nullptr;
+      m.elem_slot_end = 0;
+      m.slot_elem = nullptr;
     } else {
       m.rcache = c.rcache_f; m.face = c.face_f; m.nrm = c.nrm_f; m.face_nrml = c.face_nrml_f;
       m.def_con_nrml = c.def_con_nrml_f; m.bc_nrml_t = c.bc_nrml_f;
       m.ref = c.ref_state;
       m.ref_terms = c.ref_terms;
+      m.elem_slot_end = (c.cap_car + c.n_def)*2*ND;
+      m.slot_elem = c.slot_elem;
     }
     return m;
   }
@@ -378,6 +382,7 @@ struct Runner
   // RefState terms of every element, after the reference state changed (mixed form)
   static void ref_terms(Ctx& c)
   {
+    static_assert(sizeof(RefState<ND, float>) == (3*ND + 7)*sizeof(float), "ref_terms rows are 3 nd + 7 floats");
     const int n = c.cap_car + c.n_def;
     if (c.ref_state && c.ref_terms && n > 0)
       k_ref_terms<ND><<<grid_for(n, 256), 256, 0, c.stream>>>(c.ref_state, n, reinterpret_cast<RefState<ND, float>*>(c.ref_terms));

@@ -266,11 +266,13 @@ int hexed_gpu_launch_shape(hexed_gpu_ctx* ctx, int* local_elems_per_cta, int* fa
 
 /* Reference state (nv conserved values) of every element in the mixed form. The mixed form
  * stores face traces, and forms convective fluxes, as differences from the element's
- * reference state, so that float arithmetic resolves small variations of a nearly uniform
- * flow. By default this is the mean conserved state of the state given to hexed_gpu_create.
- * HEXED_ARRAY_REF_STATE sets it per element: one solve's elements share one reference state.
- * Call this before the states and traces it applies to are written. No effect in the FP64
- * form. No counterpart in the reference. */
+ * reference state, so that float arithmetic resolves small variations of the flow. By default
+ * each element's reference is the mean of its own state given to hexed_gpu_create, so the
+ * float offsets carry only the variation inside the element; neighbouring elements with
+ * different references exchange traces and fluxes through the exact difference of their
+ * references. This call gives every element the same state; HEXED_ARRAY_REF_STATE sets it
+ * per element. Call this before the states and traces it applies to are written. No effect
+ * in the FP64 form. No counterpart in the reference. */
 int hexed_gpu_set_reference_state(hexed_gpu_ctx* ctx, const double* state);
 
 /* The conserved state of the active elements as host arrays [n_elem][nv][nq] (the first nv

@@ -1,21 +1,32 @@
 """Mixed precision (FP32 fluxes, derivatives and traces; FP64 state, update, metrics, time
-step): error of the mixed state against the FP64 GPU state on every mesh kind."""
+step): error of the mixed state against the FP64 GPU state on every mesh kind.
+
+The bar is 1e-6 on the L2 error of every conserved variable on its own (each momentum
+component separately), relative to the L2 norm of its conserved quantity in the FP64 state:
+the momentum vector's for a momentum component, its own for density and energy.
+
+Why not each momentum component against its own norm: a component that starts at zero
+(z-momentum in the Taylor-Green vortex and in the deformed test states, whose velocity lies in
+the x-y plane) is made only by the rates, and FP32 rates carry the relative roundoff of an
+FP32 line derivative of a smooth field, about |D| eps_32 ~ 20 x 6e-8 ~ 1e-6 at row size 6
+(|D| the largest row sum of the derivative operator's entries times the in-element variation
+over the derivative). After 200 Taylor-Green updates z-momentum is 1/150 of x-momentum; its L2
+error is 1.3e-6 of its own norm and 9e-9 of the momentum's. The report (below) carries both.
+
+Setting HEXED_PARITY_REPORT to a file path appends one JSON line of measured errors per case."""
+import json
+import os
+
 import numpy as np
 import pytest
 
-import oracle
 from hexed_gb300 import abi, problems
 from hexed_gb300.solver import Context
-from helpers import all_directions, cartesian_case, deformed_case, rotated_pair_case
+from helpers import all_directions, cartesian_case, deformed_case, l2_per_variable, rotated_pair_case
 
 pytestmark = pytest.mark.gpu
 
-
-def l2_by_quantity(a, b, nv):
-    out = {}
-    for name, sl in (("momentum", slice(0, nv - 2)), ("density", slice(nv - 2, nv - 1)), ("energy", slice(nv - 1, nv))):
-        out[name] = float(np.linalg.norm(a[:, sl] - b[:, sl]) / np.linalg.norm(b[:, sl]))
-    return out
+MIXED_TOL = 1e-6
 
 
 def run(ar, params, steps, precision, prolong=False):
@@ -29,32 +40,44 @@ def run(ar, params, steps, precision, prolong=False):
         return c.download(abi.ARRAY_ELEM)[:, :ar.nv]
 
 
-def check(ar, params, steps, tol, prolong=False):
+def check(ar, params, steps, tol=MIXED_TOL, prolong=False, name=None):
     s64 = run(ar, params, steps, abi.FP64, prolong)
     s32 = run(ar, params, steps, abi.MIXED, prolong)
     assert np.isfinite(s32).all()
-    err = l2_by_quantity(s32, s64, ar.nv)
-    assert max(err.values()) <= tol, err
+    err = l2_per_variable(s32, s64, nv=ar.nv)
+    path = os.environ.get("HEXED_PARITY_REPORT")
+    if path and name:
+        with open(path, "a") as fh:
+            fh.write(json.dumps({"case": name, "mixed_l2_per_variable": err,
+                                 "mixed_l2_per_variable_own": l2_per_variable(s32, s64), "steps": steps}) + "\n")
+    assert max(err) <= tol, err
     # the update really moved the state (the comparison is not vacuous)
     assert np.abs(s64 - ar.elem[:, :ar.nv]).max() > 0
     return err
 
 
 def test_mixed_vortex_2d():
-    ar = problems.vortex_2d(n_per_side=12, row_size=6)
-    check(ar, abi.update_params(max_safety=0.5), 50, 1e-6)
+    ar = problems.vortex_2d(n_per_side=32, row_size=6)
+    check(ar, abi.update_params(max_safety=0.5), 100, name="mixed_vortex_2d_32sq_rs6")
 
 
 def test_mixed_taylor_green():
     ar = problems.taylor_green_3d(n_per_side=4, row_size=4)
-    check(ar, abi.update_params(max_safety=0.5, visc=ar.visc, cond=ar.cond), 50, 1e-6)
+    check(ar, abi.update_params(max_safety=0.5, visc=ar.visc, cond=ar.cond), 50)
+
+
+def test_mixed_taylor_green_32cube_rs6_200_updates():
+    """The Taylor-Green workload at its benchmark size."""
+    ar = problems.taylor_green_3d(n_per_side=32, row_size=6)
+    check(ar, abi.update_params(max_safety=0.5, visc=ar.visc, cond=ar.cond), 200,
+          name="mixed_taylor_green_3d_ns_32cube_deformed_rs6")
 
 
 @pytest.mark.parametrize("deformed", [False, True])
 def test_mixed_euler_and_bcs(deformed):
     for kind in (abi.BC_RIEMANN, abi.BC_NONPENETRATION, abi.BC_FREESTREAM, abi.BC_PRESSURE_OUTFLOW):
         ar = deformed_case(3, 4, 3, kind) if deformed else cartesian_case(2, 4, 5, kind)
-        check(ar, abi.update_params(max_safety=0.5), 20, 1e-6)
+        check(ar, abi.update_params(max_safety=0.5), 20)
 
 
 @pytest.mark.parametrize("nd,rs", [(2, 2), (2, 5), (2, 8), (3, 2), (3, 3), (3, 5), (3, 7), (3, 8)])
@@ -66,23 +89,36 @@ def test_mixed_row_sizes(nd, rs):
     rng = np.random.default_rng(rs)
     ar.elem[:, ar.nv + 2] = rng.uniform(0, 1e-3, size=ar.elem[:, 0].shape)   # Laplacian AV
     visc, cond = air_transport()
-    check(ar, abi.update_params(max_safety=0.5, visc=visc, cond=cond), 5, 1e-6)
+    check(ar, abi.update_params(max_safety=0.5, visc=visc, cond=cond), 5)
 
 
 def test_mixed_rotated_connections():
     for d in list(all_directions(3))[::5]:
         ar = rotated_pair_case(3, 3, d)
-        check(ar, abi.update_params(max_safety=0.5), 10, 1e-6)
+        check(ar, abi.update_params(max_safety=0.5), 10)
 
 
 def test_mixed_hanging_faces():
     ar = problems.pulse_tree_3d(n_base=2, row_size=4, levels=1)
-    check(ar, abi.update_params(max_safety=0.5), 20, 1e-6, prolong=True)
+    check(ar, abi.update_params(max_safety=0.5), 20, prolong=True, name="mixed_pulse_tree_2base_1level_rs4")
 
 
 def test_mixed_artificial_viscosity():
     ar = problems.mach2_jump_3d(n_per_side=3, row_size=4)
-    check(ar, abi.update_params(max_safety=0.5, av_admis_char_speed=ar.av_char_speed), 10, 1e-5)
+    check(ar, abi.update_params(max_safety=0.5, av_admis_char_speed=ar.av_char_speed), 10,
+          name="mixed_mach2_jump_3cube_rs4")
+
+
+def test_mixed_artificial_viscosity_32cube_rs6():
+    ar = problems.mach2_jump_3d(n_per_side=32, row_size=6)
+    check(ar, abi.update_params(max_safety=0.5, av_admis_char_speed=ar.av_char_speed), 20,
+          name="mixed_mach2_jump_32cube_rs6")
+
+
+@pytest.mark.parametrize("rs", [4, 6])
+def test_mixed_pulse_tree_16base_2levels(rs):
+    ar = problems.pulse_tree_3d(n_base=16, row_size=rs, levels=2)
+    check(ar, abi.update_params(max_safety=0.5), 50, prolong=True, name=f"mixed_pulse_tree_16base_2levels_rs{rs}")
 
 
 def test_integer_conversions_match_hardware():
