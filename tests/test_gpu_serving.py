@@ -159,3 +159,41 @@ def test_diverged_solve_is_retired_without_touching_the_others():
     assert status_bad == {0: "converged", 1: "diverged", 2: "converged"}
     for rid in (0, 2):
         assert np.array_equal(got_bad[rid], got_ok[rid])
+
+
+@pytest.mark.parametrize("static_scratch", [False, True])
+def test_segment_norms_match_oracle(static_scratch):
+    """The segmented residual norms that retire solves, through both entry points (the one
+    that grows its buffers and the one with a fixed array), against the oracle: each solve's
+    segment equals the oracle's residual_norm of that solve alone. On the same pool, one
+    segment over every live element equals hexed_gpu_residual_norm, and the squared segment
+    norms sum to the squared whole-pool norm."""
+    reqs = [serving.Request(0, 6, 4, 0.6, 8., seed=21), serving.Request(1, 5, 4, 0.3, -4., seed=3),
+            serving.Request(2, 7, 4, 0.75, 2., seed=9)]
+    pool = serving.Pool(4, abi.FP64, capacity=512, max_cases=8, params=PARAMS, updates_per_batch=5)
+    try:
+        slots = [pool.admit(r) for r in reqs]
+        for _ in range(2):
+            pool.enqueue_batch()
+        c = pool.ctx
+        c.compute_residual(PARAMS)
+        begin = np.array([s.elem_begin for s in slots], np.int32)
+        count = np.array([s.n_elem for s in slots], np.int32)
+        seg = c.segment_residual_norms(begin, count, static_scratch=static_scratch)
+        end = int((begin + count).max())
+        whole = c.segment_residual_norms(np.array([0], np.int32), np.array([end], np.int32),
+                                         static_scratch=static_scratch)[0]
+        total = np.array(c.residual_norm())
+    finally:
+        pool.close()
+    # the pool's active prefix holds only these solves: the whole-pool norms are theirs
+    np.testing.assert_allclose(whole, total, rtol=1e-12)
+    np.testing.assert_allclose((seg ** 2).sum(axis=0), total ** 2, rtol=1e-12)
+    for req, got in zip(reqs, seg):
+        ar = plain_arena(req)
+        o = oracle.Oracle(ar)
+        o.write_face()
+        for _ in range(10):
+            o.update(PARAMS)
+        o.compute_residual(PARAMS)
+        np.testing.assert_allclose(got, o.residual_norm(), rtol=1e-11)
