@@ -10,8 +10,11 @@ A step is one Solver::update: max_dt, the viscous LDG stage 0 and the inviscid s
   python bench.py --serving [--solves S --rate R --max-side M --tol T --precision fp64|mixed]
 
 The default line reports the FP64 form (the headline) and, under "mixed", the mixed form of
-the same workload with its error against the FP64 state. --workload selects the other
-configurations (see Workload); --serving measures the serving loop (see run_serving).
+the same workload with its error against the FP64 state, and under "serving" a bounded
+sample of the serving stream (see serving_sample). The K timed updates replay one CUDA graph
+(hexed_gpu_update_n) captured in warm-up; the per-kernel table comes from a separate eager,
+profiled pass of K updates. --workload selects the other configurations (see Workload);
+--serving measures the serving loop alone (see run_serving).
 
 Multi-GPU: the path runs one independent replica per GPU (no data-path collective);
 value aggregates all replicas (weak scaling).
@@ -65,6 +68,13 @@ class Workload:
         self.rs = rs or self.DEFAULT_RS[kind]
 
     def arena(self):
+        """A fresh copy of the workload's arena (generated once: the 32^3 deformed meshes take
+        tens of seconds to set up on the host)."""
+        if getattr(self, "_arena", None) is None:
+            self._arena = self._make()
+        return self._arena.copy()
+
+    def _make(self):
         k, n, rs = self.kind, self.n, self.rs
         if k == "tgv":
             return problems.taylor_green_3d(n_per_side=n, row_size=rs)
@@ -132,9 +142,9 @@ def kernel_bytes(name, ar, precision="fp64"):
     return None
 
 
-# DRAM bytes per element and launch measured by ncu on smaller cases of the same kernels
-# (read + write; profiles/fp64_flops_tgv16_rs6.md: FP64 at 16^3; profiles/k_local_tgv_rs6.md:
-# mixed at 24^3 elements).
+# DRAM bytes per element and launch measured by ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum, one launch) on smaller Taylor-Green meshes of the same kernels: FP64
+# on the 16^3 mesh, mixed on the 24^3 mesh, row size 6.
 NCU_DRAM_BYTES_PER_ELEM = {
     ("local_def_ns", "fp64", 6): 73281.,
     ("local_def_euler", "fp64", 6): 69966.,
@@ -143,14 +153,14 @@ NCU_DRAM_BYTES_PER_ELEM = {
 }
 
 
-# Busiest pipe of the same kernels in those captures (% of peak sustained, active cycles).
+# Busiest pipe of the same kernels in those captures (fraction of peak sustained over active cycles).
 NCU_PIPE_FRAC = {
     ("local_def_ns", "fp64", 6): ("fp64", 0.919),
     ("local_def_euler", "fp64", 6): ("fp64", 0.879),
 }
 
-# FP64 flops per element of the FP64 kernels (2 x DFMA + DADD + DMUL thread instructions,
-# ncu on the 16^3 case; profiles/fp64_flops_tgv16_rs6.md): the compute roofline of the FP64
+# FP64 flops per element of the FP64 kernels (2 x DFMA + DADD + DMUL thread instructions
+# counted by ncu on the 16^3 Taylor-Green mesh, row size 6): the compute roofline of the FP64
 # form, against the FP64 FMA rate hexed_gpu_fp64_peak measures in the same run.
 NCU_FP64_FLOPS_PER_ELEM = {
     ("local_def_ns", 6): 455624.,
@@ -210,9 +220,46 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ CPU oracle timing
+def host_threads():
+    """OpenMP threads of the CPU baseline: OMP_NUM_THREADS when set, else the rule of the
+    reference's hexecute, all hardware threads but two (src/hexecute.cpp:7)."""
+    env = os.environ.get("OMP_NUM_THREADS")
+    if env and env.isdigit() and int(env) > 0:
+        return int(env)
+    return max(1, (os.cpu_count() or 1) - 2)
+
+
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the machine type)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as fh:
+            for line in fh:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
+
+
+def config_of(wl, ar, precision, world):
+    """The `config` object of both arms' lines."""
+    return {"workload": wl.name, "n_elem": ar.n_elem, "row_size": wl.rs, "precision": precision,
+            "parallelism": f"replicas{world}",
+            "l2": f"inputs larger than L2 (state alone {ar.elem.nbytes / 1e6:.0f} MB; L2 129 MB)"}
+
+
 def cpu_baseline(wl, steps=None, target_s=12.):
-    """Time the oracle port (OpenMP, all host threads) on the same workload."""
+    """Time the oracle port (OpenMP, host_threads() threads) on the same workload."""
     import oracle
+    threads = oracle.set_threads(host_threads())
     ar = wl.arena()
     o = oracle.Oracle(ar)
     initialize(o)
@@ -226,10 +273,9 @@ def cpu_baseline(wl, steps=None, target_s=12.):
     for _ in range(steps):
         o.update(p)
     t = time.perf_counter() - t0
-    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return {"value": dofs_per_update(ar) * steps / t / 1e9, "unit": "GDOF/s", "cores": cores, "kind": "port",
+    return {"value": dofs_per_update(ar) * steps / t / 1e9, "unit": "GDOF/s", "cores": threads, "kind": "port",
             "sample": f"{steps} Solver::update steps of the full {wl.name} workload on the CPU oracle "
-                      f"({t:.2f} s)", "seconds": t}
+                      f"({t:.2f} s)", "seconds": t, "cpu_model": cpu_model(), "host_threads": os.cpu_count()}
 
 
 def run_reference(args):
@@ -238,6 +284,7 @@ def run_reference(args):
         return 0
     import oracle
     oracle.build()
+    threads = oracle.set_threads(host_threads())
     wl = Workload(args.workload, args.n, args.rs)
     ar = wl.arena()
     o = oracle.Oracle(ar)
@@ -251,14 +298,13 @@ def run_reference(args):
         o.update(p)
     t = time.perf_counter() - t0
     value = dofs_per_update(ar) * args.steps / t / 1e9
-    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "GDOF/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": wl.name, "n_elem": ar.n_elem, "row_size": wl.rs,
-                                            "precision": "fp64"},
-            "cpu_baseline": {"value": value, "unit": "GDOF/s", "cores": cores, "kind": "port",
-                             "sample": f"{args.steps} Solver::update steps of the full workload on the CPU oracle"},
+            "data": "synthetic", "config": config_of(wl, ar, "fp64", world),
+            "cpu_baseline": {"value": value, "unit": "GDOF/s", "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} Solver::update steps of the full workload on the CPU oracle",
+                             "cpu_model": cpu_model(), "host_threads": os.cpu_count()},
             "e2e": {"value": value, "unit": "GDOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -266,12 +312,19 @@ def run_reference(args):
 
 def state_errors(a, b, nv):
     """L2 and Linf errors of state a against reference b: per variable (each relative to
-    that variable's own norm) and per conserved quantity (momentum vector, density, energy)."""
+    that variable's own norm, and relative to its conserved quantity's norm) and per conserved
+    quantity (momentum vector, density, energy)."""
     out = {"l2_rel": [], "linf_rel": []}
     for v in range(nv):
         d, r = a[:, v] - b[:, v], b[:, v]
         out["l2_rel"].append(float(np.linalg.norm(d) / max(np.linalg.norm(r), 1e-300)))
         out["linf_rel"].append(float(np.abs(d).max() / max(np.abs(r).max(), 1e-300)))
+    # each variable against the L2 norm of its conserved quantity: a momentum component against
+    # the momentum vector's (a component that starts at zero has no meaningful own scale)
+    mom = float(np.linalg.norm(b[:, :nv - 2]))
+    out["l2_rel_quantity_scaled"] = [
+        float(np.linalg.norm(a[:, v] - b[:, v]) / (mom if v < nv - 2 else np.linalg.norm(b[:, v])))
+        for v in range(nv)]
     groups = {"momentum": slice(0, nv - 2), "density": slice(nv - 2, nv - 1), "energy": slice(nv - 1, nv)}
     out["l2_rel_by_quantity"] = {k: float(np.linalg.norm(a[:, s] - b[:, s]) / np.linalg.norm(b[:, s]))
                                  for k, s in groups.items()}
@@ -376,6 +429,67 @@ def run_serving_probe(args):
 
 
 # ------------------------------------------------------------------ GPU arm
+def timed_updates(ctx, p, args, stream, barrier, local_rank):
+    """W eager warm-up updates, then one untimed hexed_gpu_update_n of K updates, which
+    captures them as a CUDA graph; the timed region replays that graph (K updates) between
+    CUDA events on the library's stream, with the clocks sampled meanwhile. Then an eager pass
+    of K updates under the library's per-kernel CUDA-event profiler gives the kernel table
+    (same launches as the graph; outside the timed region). Returns (ms, profile, clocks)."""
+    import torch
+    for _ in range(args.warmup):
+        ctx.update(p, read_dt=False)
+    ctx.update_n(p, args.steps, use_graph=True)
+    ctx.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clk:
+        e0.record(stream)
+        ctx.update_n(p, args.steps, use_graph=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    ctx.profile_enable(True)
+    for _ in range(args.steps):
+        ctx.update(p, read_dt=False)
+    prof = ctx.profile_read()
+    ctx.profile_enable(False)
+    return ms, prof, clk
+
+
+def serving_sample(args):
+    """A bounded sample of the serving stream (steady 2D Euler solves, Cartesian meshes of
+    sides uniform in [8, serving_max_side], row size 4 or 6, Mach U(0.2, 0.8), angle
+    U(-10, 10) degrees, 2% five-mode perturbation, local time stepping to a 1e-8 drop of the
+    normalized residual, Poisson arrivals): batched in the mixed form, batched in FP64, and
+    one solve at a time in FP64 (the same engine with one live solve), each with solves/s,
+    p50/p99 latency and the clocks seen."""
+    from hexed_gb300 import serving
+    params = abi.update_params(max_safety=0.5, local_time=True)
+    reqs = serving.request_stream(args.serving_solves, args.rate, seed=args.seed, sides=(8, args.serving_max_side))
+    k = {4: args.batch, 6: args.batch}
+    out = {"config": {"workload": "serving_2d_euler_stream_sample", "solves": args.serving_solves,
+                      "rate_per_s": args.rate, "sides": [8, args.serving_max_side], "row_sizes": [4, 6],
+                      "tol": args.tol, "seed": args.seed, "updates_per_batch": args.batch,
+                      "sample": "bounded sample of the 512-solve, sides 8-96 stream with the same distributions"}}
+    legs = (("batched_mixed", abi.MIXED, None), ("batched_fp64", abi.FP64, None), ("one_at_a_time_fp64", abi.FP64, 1))
+    for name, prec, max_live in legs:
+        with serving.Server(prec, tol=args.tol, updates_per_batch=k, params=params, max_live=max_live,
+                            max_updates=args.max_updates) as srv:
+            srv.run(reqs[:2])   # warm-up: kernels loaded, graphs of the first shapes
+            with ClockSampler(0) as clk:
+                summary = srv.run(reqs).summary()
+        out[name] = {k2: summary[k2] for k2 in ("solves", "converged", "solves_per_s", "p50_latency_s",
+                                                "p99_latency_s", "updates", "wall_s")}
+        out[name]["clocks"] = clk.summary()
+    out["speedup_batched_fp64_vs_one_at_a_time"] = (out["batched_fp64"]["solves_per_s"] /
+                                                     out["one_at_a_time_fp64"]["solves_per_s"])
+    out["speedup_batched_mixed_vs_one_at_a_time"] = (out["batched_mixed"]["solves_per_s"] /
+                                                      out["one_at_a_time_fp64"]["solves_per_s"])
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -400,6 +514,9 @@ def main():
     ap.add_argument("--max-updates", type=int, default=400_000)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-one-at-a-time", action="store_true")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving sample of the default line")
+    ap.add_argument("--serving-solves", type=int, default=24, help="solves in the default line's serving sample")
+    ap.add_argument("--serving-max-side", type=int, default=16)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -429,24 +546,8 @@ def main():
     initialize(ctx)
     p = wl.params(ar)
     stream = torch.cuda.ExternalStream(ctx.stream_ptr)
-    for _ in range(args.warmup):
-        ctx.update(p, read_dt=False)
-    ctx.synchronize()
-
-    # ---- timed region: inputs resident in HBM (arena ~2 GB >> 129 MB L2, no flush needed)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ctx.profile_enable(True)
-    barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(local_rank) as clk:
-        e0.record(stream)
-        for _ in range(args.steps):
-            ctx.update(p, read_dt=False)
-        e1.record(stream)
-        torch.cuda.synchronize()
-    barrier()
-    ms = e0.elapsed_time(e1)
-    prof = ctx.profile_read()
+    # timed region: inputs resident in HBM (arena ~2 GB >> 129 MB L2, no flush needed)
+    ms, prof, clk = timed_updates(ctx, p, args, stream, barrier, local_rank)
     ms = replicas.max_over_ranks(ms, device="cuda")
     value = replicas.job_rate(dofs_per_update(ar) * args.steps, world, ms) / 1e9
     launches = sum(v[0] for v in prof.values())
@@ -496,14 +597,15 @@ def main():
         traffic = per_elem * (ar.n_def if "def" in top_name else ar.n_car if "car" in top_name else ar.n_elem)
     roofline = {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved / hbm_peak if achieved else None, "traffic": traffic,
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a smaller case of the same "
-                                  "kernel, scaled by elements (profiles/k_local_tgv_rs6.md)" if traffic else None,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of the same "
+                                  "kernel on a smaller Taylor-Green mesh (16^3 FP64, 24^3 mixed), scaled by "
+                                  "elements" if traffic else None,
                 "algorithmic_bytes_per_launch": nbytes, "launch_ms": per_launch_ms,
                 "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
                 "fp64_peak_tflops_measured": fp64_peak}
     pipe = NCU_PIPE_FRAC.get((top_name, args.precision, wl.rs)) if wl.kind == "tgv" else None
     if pipe is not None:
-        # what bounds this kernel instead of HBM: the busiest pipe in ncu (profiles/k_local_tgv_rs6.md)
+        # what bounds this kernel instead of HBM: the busiest pipe in the same ncu capture
         roofline["compute_bound"] = {"pipe": pipe[0], "frac_of_peak_ncu": pipe[1]}
     flops = NCU_FP64_FLOPS_PER_ELEM.get((top_name, wl.rs)) if wl.kind in ("tgv", "mach2") else None
     if flops is not None and precision == abi.FP64 and fp64_peak:
@@ -513,8 +615,8 @@ def main():
         achieved_tf = flops * n / (per_launch_ms * 1e-3) / 1e12
         roofline["fp64"] = {"achieved": achieved_tf, "peak": fp64_peak, "unit": "TFLOP/s",
                             "frac": achieved_tf / fp64_peak, "flops_per_launch": flops * n,
-                            "flops_source": "ncu 2*dfma + dadd + dmul thread instructions per element of the "
-                                            "16^3 case, scaled by elements (profiles/fp64_flops_tgv16_rs6.md)",
+                            "flops_source": "ncu 2*dfma + dadd + dmul thread instructions per element of one "
+                                            "launch on the 16^3 Taylor-Green mesh, scaled by elements",
                             "peak_source": "hexed_gpu_fp64_peak, measured in this run"}
     kernels = {k: {"launches": v[0], "total_ms": round(v[1], 4), "share": round(v[1] / sum(x[1] for x in prof.values()), 4)}
                for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])}
@@ -531,18 +633,7 @@ def main():
         mctx = Context(wl.arena(), abi.MIXED)
         initialize(mctx)
         mstream = torch.cuda.ExternalStream(mctx.stream_ptr)
-        for _ in range(args.warmup):
-            mctx.update(p, read_dt=False)
-        mctx.profile_enable(True)
-        torch.cuda.synchronize()
-        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        g0.record(mstream)
-        for _ in range(args.steps):
-            mctx.update(p, read_dt=False)
-        g1.record(mstream)
-        torch.cuda.synchronize()
-        mms = g0.elapsed_time(g1)
-        mprof = mctx.profile_read()
+        mms, mprof, mclk = timed_updates(mctx, p, args, mstream, lambda: None, local_rank)
         mctx.close()
         mvalue = dofs_per_update(ar) * args.steps / (mms / 1e3) / 1e9
         # HBM roofline of the mixed form's dominant kernel, as for the headline
@@ -556,10 +647,15 @@ def main():
                  "launch_ms": mlaunch_ms,
                  "traffic": mper_elem * (ar.n_def if "def" in mtop else ar.n_car) if mper_elem else None}
         mixed = {"value": mvalue, "unit": "GDOF/s", "ms_per_step": mms / args.steps, "speedup_vs_fp64": mvalue / value,
-                 "dtype": "f32/f64", "roofline": mroof,
+                 "dtype": "f32/f64", "roofline": mroof, "clocks": mclk.summary(),
                  "kernels": {k: {"launches": v[0], "total_ms": round(v[1], 4)}
                              for k, v in sorted(mprof.items(), key=lambda kv: -kv[1][1])},
                  "error_vs_fp64": mixed_vs_fp64(wl, args.err_steps) if args.err_steps > 0 else None}
+
+    serving_line = None
+    if rank == 0 and world == 1 and not args.no_serving:
+        ctx.close()
+        serving_line = serving_sample(args)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -574,9 +670,8 @@ def main():
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64" if precision == abi.FP64 else "f32/f64",
                 "data": "synthetic",
-                "config": {"workload": wl.name, "n_elem": ar.n_elem, "row_size": wl.rs,
-                           "precision": args.precision, "parallelism": f"replicas{world}",
-                           "l2": f"inputs larger than L2 (state alone {ar.elem.nbytes / 1e6:.0f} MB; L2 129 MB)"},
+                "config": config_of(wl, ar, args.precision, world),
+                "timing": f"{args.steps} updates replayed as one CUDA graph captured in warm-up",
                 "e2e": {"value": e2e_value, "unit": "GDOF/s", "h2d_bytes_per_step": n_bytes,
                         "d2h_bytes_per_step": n_bytes},
                 "gpu_launches": launches,
@@ -588,6 +683,8 @@ def main():
             line["mixed_vs_fp64"] = mixed_err
         if mixed is not None:
             line["mixed"] = mixed
+        if serving_line is not None:
+            line["serving"] = serving_line
         print(json.dumps(line))
     if pg:
         pg.destroy_process_group()

@@ -62,6 +62,7 @@ def load():
             "oracle_characteristics": [c_int, P, P, P, P, P],
             "oracle_sav_slot_dof": [c_int, c_int],
             "oracle_update_art_visc_smoothness": [D, P, P, ctypes.POINTER(SavParams), P],
+            "oracle_set_threads": [c_int],
         }
         for name, args in sig.items():
             fn = getattr(lib, name)
@@ -135,6 +136,11 @@ def derivative(row_size, f, fb):
     po = out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
     assert lib.oracle_derivative(row_size, pf, pb, po) == 0
     return out
+
+
+def set_threads(n=0):
+    """OpenMP threads of the oracle (n <= 0: unchanged); returns the count in effect."""
+    return load().oracle_set_threads(int(n))
 
 
 def perm_index(n_dim, row_size, direction, q):

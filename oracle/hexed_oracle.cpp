@@ -24,6 +24,7 @@
 #include <limits>
 #include <vector>
 #include <type_traits>
+#include <omp.h>
 #include "../include/hexed_gpu.h"
 #include "../hexed_gb300/csrc/basis_tables.h"
 
@@ -1958,6 +1959,15 @@ struct Sav
 } // namespace
 
 extern "C" {
+
+// OpenMP threads of the oracle's parallel loops (the reference's hexecute runs
+// omp_get_max_threads() - 2, src/hexecute.cpp:7). n <= 0 leaves the count unchanged; returns
+// the count in effect.
+int oracle_set_threads(int n)
+{
+  if (n > 0) omp_set_num_threads(n);
+  return omp_get_max_threads();
+}
 
 int oracle_write_face(const hexed_mesh_desc* m) { return dispatch(m, [](auto& k) { k.write_face(); }); }
 int oracle_prolong(const hexed_mesh_desc* m, int scale, int offset)
