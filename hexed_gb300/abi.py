@@ -22,7 +22,7 @@ STATUS_NAMES = {0: "HEXED_OK", -1: "HEXED_ERR_INVALID", -2: "HEXED_ERR_CUDA", -3
 BC_FREESTREAM, BC_RIEMANN, BC_NONPENETRATION, BC_COPY, BC_OUTFLOW, BC_PRESSURE_OUTFLOW, BC_NO_SLIP = range(7)
 THERMAL_HEAT_FLUX, THERMAL_ENERGY, THERMAL_EQUILIBRIUM = range(3)
 ARRAY_ELEM, ARRAY_RCACHE, ARRAY_FACE, ARRAY_BC_CACHE, ARRAY_NOM_SIZE, ARRAY_VERT_TSS, ARRAY_BC_NRML, \
-    ARRAY_REF_STATE, ARRAY_JAC, ARRAY_FACE_NRML, ARRAY_DEF_CON_NRML = range(11)
+    ARRAY_REF_STATE, ARRAY_JAC, ARRAY_FACE_NRML, ARRAY_DEF_CON_NRML, ARRAY_SAV_AUX, ARRAY_SAV_FACE = range(13)
 INT_CAR_CON, INT_BC_CON = 0, 1
 FP64, MIXED = 0, 1
 
@@ -59,6 +59,23 @@ class UpdateParams(ctypes.Structure):
                 ("flow_iters", c_int), ("local_time", c_int), ("use_filter", c_int), ("use_ldg", c_int),
                 ("visc", Transport), ("cond", Transport), ("av_admis_char_speed", c_double),
                 ("fix_admis", c_int), ("fix_admis_max_safety", c_double)]
+
+
+class SavParams(ctypes.Structure):
+    """hexed_sav_params: the settings of Solver::update_art_visc_smoothness."""
+    _fields_ = [("advect_length", c_double), ("advect_iters", c_int), ("diff_iters", c_int), ("n_cheby", c_int),
+                ("av_row_size", c_int), ("advect_safety", c_double), ("diff_safety", c_double),
+                ("diff_ratio", c_double), ("visc_mult", c_double), ("unscaled_max", c_double),
+                ("freestream_mass", c_double), ("freestream_energy", c_double)]
+
+
+def sav_params(advect_length, row_size, freestream_mass, freestream_energy, advect_iters=1, diff_iters=1,
+               n_cheby=1, av_row_size=None, advect_safety=0.7, diff_safety=0.7, diff_ratio=0.3, visc_mult=1e2,
+               unscaled_max=5.):
+    """Settings of Solver::update_art_visc_smoothness; defaults of the Solver namespace
+    (src/Solver.cpp:154-163), av_row_size defaulting to the row size."""
+    return SavParams(advect_length, advect_iters, diff_iters, n_cheby, av_row_size or row_size, advect_safety,
+                     diff_safety, diff_ratio, visc_mult, unscaled_max, freestream_mass, freestream_energy)
 
 
 def transport_inviscid():
@@ -157,6 +174,7 @@ def load_library(path=LIB_PATH):
         "hexed_gpu_update_n": ([vp, ctypes.POINTER(UpdateParams), c_int, c_int], c_int),
         "hexed_gpu_segment_residual_norms_static": ([vp, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int),
                                                      P_double], c_int),
+        "hexed_gpu_update_art_visc_smoothness": ([vp, ctypes.POINTER(SavParams), P_double], c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -49,6 +49,8 @@ struct OpsTable {
   void (*compute_jacobian)(Ctx&, const double* d_vert_pos, double* d_fn, double* d_vtss);
   void (*fix_admis_coef)(Ctx&, const int* d_record, bool swap_only);
   void (*ref_terms)(Ctx&);
+  void (*update_art_visc_smoothness)(Ctx&, const hexed_sav_params&, double* d_residual);
+  int (*sav_slot_dof)();
 };
 
 // A captured multi-update sequence and the inputs it was captured for.
@@ -110,6 +112,9 @@ struct Ctx {
   int face_threads;
   // 1 while Solver::fix_admissibility's diffusion runs: the kernels compute pde::Fix_therm_admis
   int fta;
+  // smoothness-based AV storage (allocated on first use): [cap elements][4 + 2 rs][nq],
+  // [n_slot][sav slot_dof], and per-element residual partials [cap elements]
+  double* sav_aux; double* sav_face; double* sav_partials;
 };
 
 // Max_dt's CFL reciprocals for convective and diffusive safety factors (include/Spatial.hpp:

@@ -14,6 +14,7 @@
 #include <limits>
 #include "ctx.h"
 #include "kernels.cuh"
+#include "sav.cuh"
 #include "basis_tables.h"
 
 using hx::Ctx;
@@ -165,6 +166,8 @@ size_t array_count(const Ctx* c, int which)
     case HEXED_ARRAY_JAC: return (size_t)c->n_def*(c->nd*c->nd + 1)*c->nq;
     case HEXED_ARRAY_FACE_NRML: return (size_t)c->n_def*2*c->nd*c->nd*c->nfq;
     case HEXED_ARRAY_DEF_CON_NRML: return (size_t)c->n_def_con*c->nd*c->nfq;
+    case HEXED_ARRAY_SAV_AUX: return n_elem*(4 + 2*(size_t)c->rs)*c->nq;
+    case HEXED_ARRAY_SAV_FACE: return (size_t)c->n_slot*c->ops->sav_slot_dof();
   }
   return 0;
 }
@@ -183,8 +186,36 @@ double* array_ptr(Ctx* c, int which)
     case HEXED_ARRAY_JAC: return c->jac;
     case HEXED_ARRAY_FACE_NRML: return c->face_nrml;
     case HEXED_ARRAY_DEF_CON_NRML: return c->def_con_nrml;
+    case HEXED_ARRAY_SAV_AUX: return c->sav_aux;
+    case HEXED_ARRAY_SAV_FACE: return c->sav_face;
   }
   return nullptr;
+}
+
+// Storage of the smoothness-based AV, allocated on first use: forcing rows and residual cache
+// zero, advection state 1 (Solver's constructor, src/Solver.cpp:201-211), face slots zero.
+int ensure_sav(Ctx* c)
+{
+  if (c->sav_aux) return HEXED_OK;
+  const size_t n_elem = (size_t)c->cap_car + c->n_def;
+  const size_t n_aux = array_count(c, HEXED_ARRAY_SAV_AUX), n_face = array_count(c, HEXED_ARRAY_SAV_FACE);
+  double *aux = nullptr, *face = nullptr, *part = nullptr;
+  if (cudaMalloc((void**)&aux, n_aux*sizeof(double)) != cudaSuccess ||
+      cudaMalloc((void**)&face, n_face*sizeof(double)) != cudaSuccess ||
+      cudaMalloc((void**)&part, n_elem*sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    if (aux) cudaFree(aux);
+    if (face) cudaFree(face);
+    if (part) cudaFree(part);
+    return fail(HEXED_ERR_ALLOC, "smoothness-based AV storage allocation failed (%zu + %zu doubles)", n_aux, n_face);
+  }
+  HX_CUDA(cudaMemsetAsync(aux, 0, n_aux*sizeof(double), c->stream));
+  HX_CUDA(cudaMemsetAsync(face, 0, n_face*sizeof(double), c->stream));
+  const int n_rows = c->rs, grid = int(std::min<long>(((long)n_elem*n_rows*c->nq + 255)/256, 152*16));
+  if (n_elem) hx::k_sav_init<<<grid, 256, 0, c->stream>>>(aux, (long)n_elem, 4 + 2*c->rs, 4, n_rows, (int)c->nq);
+  c->sav_aux = aux; c->sav_face = face; c->sav_partials = part;
+  HX_LAUNCHED();
+  return HEXED_OK;
 }
 
 // FP32 device storage of an arena array in the mixed form (face traces, residual cache).
@@ -228,6 +259,10 @@ int transfer(Ctx* c, int which, long offset, long count, double* host, bool to_d
   if (offset < 0 || count < 0 || offset + count > n || (count && !host))
     return fail(HEXED_ERR_INVALID, "range [%ld, %ld) outside array %d of %ld entries", offset, offset + count, which, n);
   if (count == 0) return HEXED_OK;
+  if (which == HEXED_ARRAY_SAV_AUX || which == HEXED_ARRAY_SAV_FACE) {
+    if (int st = ensure_sav(c)) return st;
+    d = array_ptr(c, which);
+  }
   if (!d && !f) return fail(HEXED_ERR_INVALID, "array %d is not allocated", which);
   if (f) {
     double* tmp = nullptr;
@@ -479,7 +514,8 @@ int hexed_gpu_destroy(hexed_gpu_ctx* c)
                   c->def_con, c->def_con_nrml, c->bc_con, c->bc_nrml, c->bc_cache, c->ref_face, c->bc_spec,
                   c->scalars, c->partials, c->status, c->dt_ticket, c->d_norm, c->vert_id, c->uncert, c->vmax,
                   c->seg_table, c->seg_out, c->inv_det, c->face_f, c->rcache_f, c->nrm_f, c->face_nrml_f,
-                  c->def_con_nrml_f, c->bc_nrml_f, c->ref_state, c->ref_terms, c->record, c->slot_elem};
+                  c->def_con_nrml_f, c->bc_nrml_f, c->ref_state, c->ref_terms, c->record, c->slot_elem,
+                  c->sav_aux, c->sav_face, c->sav_partials};
   for (void* p : ptrs) if (p) cudaFree(p);
   if (c->graph) {
     if (c->graph->exec) cudaGraphExecDestroy(c->graph->exec);
@@ -719,6 +755,31 @@ int hexed_gpu_set_art_visc_admis(hexed_gpu_ctx* c, double char_speed)
   if (c->n_vert <= 0) return fail(HEXED_ERR_INVALID, "set_art_visc_admis needs the arena's vertex table");
   c->ops->set_art_visc_admis(*c, char_speed);
   HX_LAUNCHED();
+  return HEXED_OK;
+}
+
+int hexed_gpu_update_art_visc_smoothness(hexed_gpu_ctx* c, const hexed_sav_params* p, double* residual)
+{
+  if (int st = check_ctx(c)) return st;
+  if (!p) return fail(HEXED_ERR_INVALID, "null smoothness-AV parameters");
+  if (!(p->advect_length > 0) || !std::isfinite(p->advect_length))
+    return fail(HEXED_ERR_INVALID, "advect_length must be positive and finite");
+  if (p->advect_iters < 0 || p->diff_iters < 0 || p->n_cheby < 1)
+    return fail(HEXED_ERR_INVALID, "iteration counts must be >= 0 and n_cheby >= 1");
+  // Solver::set_art_visc_row_size (src/Solver.cpp:660-665)
+  if (p->av_row_size < 2 || p->av_row_size > c->rs)
+    return fail(HEXED_ERR_PRECONDITION, "`row_size` must be >= 2 and <= discretization row size");
+  if (!(p->advect_safety > 0) || !(p->diff_safety > 0) || !(p->diff_ratio > 0) || !(p->unscaled_max > 0) ||
+      !(p->freestream_mass > 0) || !(p->freestream_energy > 0))
+    return fail(HEXED_ERR_INVALID, "safety factors, diff_ratio, unscaled_max and the freestream must be positive");
+  if (int st = ensure_sav(c)) return st;
+  c->ops->update_art_visc_smoothness(*c, *p, c->d_norm + 3);
+  HX_LAUNCHED();
+  if (residual) {
+    HX_CUDA(cudaMemcpyAsync(c->h_pinned, c->d_norm + 3, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    HX_CUDA(cudaStreamSynchronize(c->stream));
+    *residual = c->h_pinned[0];
+  }
   return HEXED_OK;
 }
 

@@ -2307,37 +2307,39 @@ __global__ void k_bc_flux(Dev<FaceT> m)
 }
 
 // ------------------------------------------------------------------- hanging faces
-// Prolong_refined / Restrict_refined (include/Spatial.hpp:153-285). One CTA per refined face;
-// thread (fine face, var, qpoint). Row transforms go through shared memory one dimension at a time.
-template <int ND, int RS, bool PROLONG, typename FaceT>
-__global__ void k_refine(Dev<FaceT> m, Tab<RS> tab, int scale, int offset)
+// Prolong_refined / Restrict_refined (include/Spatial.hpp:153-285) of one refined face (the
+// calling CTA): NVAR face variables of the slots of `base` (slot_stride values per slot), the
+// LDG half starting ldg_offset values into a slot. Thread (fine face, var, qpoint); row
+// transforms go through shared memory one dimension at a time. The flow uses the arena's face
+// slots with its nv variables; the smoothness-based AV uses its own slots and variable counts.
+template <int ND, int RS, bool PROLONG, int NVAR, typename FaceT>
+__device__ __forceinline__ void refine_face(FaceT* base, size_t slot_stride, int ldg_offset, const int* rf,
+                                            const Tab<RS>& tab, int scale, int offset)
 {
   using S = Shape<ND, RS>;
-  constexpr int nfq = S::nfq, nv = S::nv;
+  constexpr int nfq = S::nfq;
   constexpr int n_face = 1 << (ND - 1);
-  __shared__ double s_face[n_face*nv*nfq];
+  __shared__ double s_face[n_face*NVAR*nfq];
   __shared__ double s_mat[2*RS*RS];
   for (int i = threadIdx.x; i < 2*RS*RS; i += blockDim.x) s_mat[i] = PROLONG ? tab.prolong[i] : tab.restrict_[i];
-  const int i_ref = blockIdx.x;
-  const int* rf = m.ref_face + 7*i_ref;
   const bool str[2] = {rf[5] != 0, rf[6] != 0};
   int nf = n_face;
   for (int d = 0; d < ND - 1; ++d) nf /= 1 + str[d];
-  FaceT* coarse = m.face + (size_t)rf[0]*S::slot_dof + offset*nv*nfq;
-  const int n_item = nf*nv*nfq;
+  FaceT* coarse = base + (size_t)rf[0]*slot_stride + offset*ldg_offset;
+  const int n_item = nf*NVAR*nfq;
   __syncthreads();
   for (int t = threadIdx.x; t < n_item; t += blockDim.x) {
-    const int i_face = t/(nv*nfq), k = t%(nv*nfq);
-    FaceT* fine = m.face + (size_t)rf[1 + i_face]*S::slot_dof + offset*nv*nfq;
+    const int i_face = t/(NVAR*nfq), k = t%(NVAR*nfq);
+    FaceT* fine = base + (size_t)rf[1 + i_face]*slot_stride + offset*ldg_offset;
     s_face[t] = PROLONG ? double(coarse[k]) : double(fine[k]);
   }
   #pragma unroll 1
   for (int d = 0; d < ND - 1; ++d) {
     __syncthreads();
-    double val[(n_face*nv*nfq + 63)/64 + 1];
+    double val[(n_face*NVAR*nfq + 63)/64 + 1];
     int cnt = 0;
     for (int t = threadIdx.x; t < n_item; t += blockDim.x, ++cnt) {
-      const int i_face = t/(nv*nfq), k = t%(nv*nfq);
+      const int i_face = t/(NVAR*nfq), k = t%(NVAR*nfq);
       const int qq = k%nfq;
       double x = s_face[t];
       if (str[d]) {
@@ -2348,11 +2350,11 @@ __global__ void k_refine(Dev<FaceT> m, Tab<RS> tab, int scale, int offset)
         const int qstride = ipow(RS, pw);
         const int i_half = (i_face/face_stride)%2;
         const int i = (qq/qstride)%RS;
-        const int base = t - i*qstride;
+        const int row0 = t - i*qstride;
         const double* mat = s_mat + i_half*RS*RS;
         double acc = 0.;
         #pragma unroll
-        for (int j = 0; j < RS; ++j) acc += mat[i*RS + j]*s_face[base + j*qstride];
+        for (int j = 0; j < RS; ++j) acc += mat[i*RS + j]*s_face[row0 + j*qstride];
         x = acc;
       }
       val[cnt] = x;
@@ -2362,24 +2364,27 @@ __global__ void k_refine(Dev<FaceT> m, Tab<RS> tab, int scale, int offset)
     for (int t = threadIdx.x; t < n_item; t += blockDim.x, ++cnt) s_face[t] = val[cnt];
   }
   __syncthreads();
-  if (PROLONG) {
-    for (int t = threadIdx.x; t < n_item; t += blockDim.x) {
-      const int i_face = t/(nv*nfq), k = t%(nv*nfq);
-      FaceT* fine = m.face + (size_t)rf[1 + i_face]*S::slot_dof + offset*nv*nfq;
-      fine[k] = FaceT(s_face[t]);
-    }
-  } else {
-    for (int t = threadIdx.x; t < n_item; t += blockDim.x) {
-      const int i_face = t/(nv*nfq), k = t%(nv*nfq);
-      FaceT* fine = m.face + (size_t)rf[1 + i_face]*S::slot_dof + offset*nv*nfq;
-      fine[k] = FaceT(s_face[t]);
-    }
-    for (int k = threadIdx.x; k < nv*nfq; k += blockDim.x) {
+  for (int t = threadIdx.x; t < n_item; t += blockDim.x) {
+    const int i_face = t/(NVAR*nfq), k = t%(NVAR*nfq);
+    FaceT* fine = base + (size_t)rf[1 + i_face]*slot_stride + offset*ldg_offset;
+    fine[k] = FaceT(s_face[t]);
+  }
+  if (!PROLONG) {
+    for (int k = threadIdx.x; k < NVAR*nfq; k += blockDim.x) {
       double acc = 0.;
-      for (int i_face = 0; i_face < nf; ++i_face) acc += s_face[i_face*nv*nfq + k];
+      for (int i_face = 0; i_face < nf; ++i_face) acc += s_face[i_face*NVAR*nfq + k];
       coarse[k] = FaceT(acc);
     }
   }
+}
+
+// One CTA per refined face of the arena's face slots.
+template <int ND, int RS, bool PROLONG, typename FaceT>
+__global__ void k_refine(Dev<FaceT> m, Tab<RS> tab, int scale, int offset)
+{
+  using S = Shape<ND, RS>;
+  refine_face<ND, RS, PROLONG, S::nv, FaceT>(m.face, S::slot_dof, S::nv*S::nfq, m.ref_face + 7*blockIdx.x, tab,
+                                             scale, offset);
 }
 
 // ------------------------------------------------------------------- Write_face (standalone)

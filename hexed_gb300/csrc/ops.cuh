@@ -7,6 +7,7 @@
 #pragma once
 #include "kernels.cuh"
 #include "metrics.cuh"
+#include "sav.cuh"
 #include "ctx.h"
 
 namespace hx {
@@ -394,12 +395,133 @@ struct Runner
     k_segment_residual<ND, RS, FaceT><<<n_seg, 256, 0, c.stream>>>(dev(c), tab(c), d_begin, d_count, d_out);
   }
 
+  // ---------------------------------------------------------------- smoothness-based AV
+  static SavDev sav_dev(Ctx& c)
+  {
+    SavDev m;
+    m.n_car = c.n_car; m.n_elem = c.n_car + c.n_def; m.n_car_con = c.n_car_con; m.n_def_con = c.n_def_con;
+    m.n_bc_con = c.n_bc_con; m.n_ref = c.n_ref;
+    m.elem = c.elem; m.aux = c.sav_aux; m.face = c.sav_face;
+    m.nom_size = c.nom_size; m.vert_tss = c.vert_tss; m.jac = c.jac; m.face_nrml = c.face_nrml;
+    m.car_con = c.car_con; m.def_con = c.def_con; m.def_con_nrml = c.def_con_nrml;
+    m.bc_con = c.bc_con; m.bc_nrml = c.bc_nrml; m.ref_face = c.ref_face; m.bc_spec = c.bc_spec;
+    m.partials = c.sav_partials;
+    return m;
+  }
+
+  static int sav_slot_dof() { return SavShape<ND, RS>::slot_dof; }
+
+  template <int NVAR>
+  static void sav_refine(Ctx& c, const SavDev& m, const Tab<RS>& t, bool prolong, bool scale, bool offset)
+  {
+    if (!c.n_ref) return;
+    if (prolong) k_sav_refine<ND, RS, true, NVAR><<<c.n_ref, 256, 0, c.stream>>>(m, t, scale, offset);
+    else k_sav_refine<ND, RS, false, NVAR><<<c.n_ref, 256, 0, c.stream>>>(m, t, scale, offset);
+  }
+
+  // Solver::update_art_visc_smoothness (src/Solver.cpp:457-582) with Solver::diffuse_art_visc
+  // (src/Solver.cpp:428-455): the reference's kernel sequence, then the flow's Write_face and
+  // Prolong (src/Solver.cpp:577-578). d_residual receives art_visc_residual.
+  static void update_art_visc_smoothness(Ctx& c, const hexed_sav_params& p, double* d_residual)
+  {
+    using SS = SavShape<ND, RS>;
+    constexpr int nq = SS::nq;
+    const SavDev m = sav_dev(c);
+    const Tab<RS> t = tab(c);
+    const SavTab<RS> st = make_savtab<RS>(t);
+    const int n_elem = m.n_elem;
+    const long n_pts = (long)n_elem*nq;
+    const int g_pts = grid_for(n_pts, 256);
+    const long n_face_pts = (long)(m.n_car_con + m.n_def_con + m.n_bc_con)*SS::nfq;
+    const int g_con = grid_for(n_face_pts, 256);
+    const int g_bc = grid_for((long)m.n_bc_con*SS::nfq, 256);
+    const int blk = (nq + 31)/32*32 < 64 ? 64 : (nq + 31)/32*32;
+    constexpr size_t smem_adv = sizeof(double)*ND*SS::n_adv*nq;
+    constexpr size_t smem_diff = sizeof(double)*(SS::n_sav + ND*SS::n_sav)*nq;
+    static bool configured = false;
+    if (!configured) {
+      cudaFuncSetAttribute(k_sav_local_advection<ND, RS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_adv);
+      cudaFuncSetAttribute(k_sav_local_diffusion<ND, RS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_diff);
+      configured = true;
+    }
+    auto sav_faces = [&](int mode) {
+      const long n = (long)n_elem*ND*SS::nfq*(mode ? SS::n_sav : SS::n_adv_extrap);
+      k_sav_write_face<ND, RS><<<grid_for(n, 256), 256, 0, c.stream>>>(m, st, mode);
+    };
+    {
+      ProfScope ps(c, "sav_setup");
+      // advection velocity, then Max_dt of pde::Advection with local time stepping
+      k_sav_velocity<ND, RS><<<g_pts, 256, 0, c.stream>>>(m);
+      k_sav_max_dt<ND, RS><<<g_pts, 256, 0, c.stream>>>(m, st, 0, t.max_cfl*p.advect_safety);
+    }
+    for (int iter = 0; iter < p.advect_iters; ++iter) {
+      sav_faces(0);
+      sav_refine<SS::n_adv_extrap>(c, m, t, true, false, false);
+      for (int stage = 0; stage < 2; ++stage) {
+        if (m.n_bc_con) k_sav_bc_advection<ND, RS><<<g_bc, 256, 0, c.stream>>>(m);
+        if (n_face_pts) {
+          ProfScope ps(c, "sav_neighbor_advection");
+          k_sav_neighbor_advection<ND, RS><<<g_con, 256, 0, c.stream>>>(m, st);
+        }
+        sav_refine<SS::n_adv_extrap>(c, m, t, false, true, false);
+        {
+          ProfScope ps(c, "sav_local_advection");
+          k_sav_local_advection<ND, RS><<<n_elem, blk, smem_adv, c.stream>>>(m, st, stage, p.advect_length,
+                                                                            t.step_ratio);
+        }
+        sav_faces(0);
+        sav_refine<SS::n_adv_extrap>(c, m, t, true, false, false);
+      }
+    }
+    // projection onto the Legendre mode of degree av_rs - 1
+    AvTab<RS, double> wo;
+    for (int i = 0; i < RS; ++i) {
+      wo.w[i] = t.weight[i];
+      wo.ow[i] = c.tables.ortho[(p.av_row_size - 1)*RS + i];
+      wo.node[i] = t.node[i];
+    }
+    k_sav_project<ND, RS><<<g_pts, 256, 0, c.stream>>>(m, wo);
+    // diffuse_art_visc: n_forcing - 1 = 3 real steps of pde::Smooth_art_visc at once
+    const double diff_time = p.diff_ratio*p.advect_length*p.advect_length/(SS::n_forcing - 1);
+    k_sav_max_dt<ND, RS><<<g_pts, 256, 0, c.stream>>>(m, st, 1, -2/t.min_eig_diffusion*p.diff_safety);
+    sav_faces(1);
+    sav_refine<SS::nv>(c, m, t, true, false, false);   // compute_prolong: the flow's nv variables
+    for (int i_iter = 0; i_iter < p.diff_iters; ++i_iter) {
+      for (int i_cheby = 0; i_cheby < p.n_cheby; ++i_cheby) {
+        // math::chebyshev_step (src/math.cpp:104-107)
+        const double s = 1/(1 - std::cos((p.n_cheby - i_cheby - 0.5)*3.14159265358979323846/p.n_cheby));
+        if (m.n_bc_con) k_sav_bc_diffusion<ND, RS><<<g_bc, 256, 0, c.stream>>>(m, 0);
+        if (n_face_pts) k_sav_neighbor_ldg<ND, RS><<<g_con, 256, 0, c.stream>>>(m, 0);
+        sav_refine<SS::n_sav>(c, m, t, false, true, false);
+        sav_refine<SS::n_sav>(c, m, t, false, false, true);
+        {
+          ProfScope ps(c, "sav_local_diffusion");
+          k_sav_local_diffusion<ND, RS><<<n_elem, blk, smem_diff, c.stream>>>(m, st, s, diff_time);
+        }
+        sav_refine<SS::n_sav>(c, m, t, true, true, true);
+        if (m.n_bc_con) k_sav_bc_diffusion<ND, RS><<<g_bc, 256, 0, c.stream>>>(m, 1);
+        if (n_face_pts) k_sav_neighbor_ldg<ND, RS><<<g_con, 256, 0, c.stream>>>(m, 1);
+        sav_refine<SS::n_sav>(c, m, t, false, true, true);
+        k_sav_reconcile<ND, RS><<<g_pts, 256, 0, c.stream>>>(m, st, s, diff_time, s);
+        sav_faces(1);
+        sav_refine<SS::n_sav>(c, m, t, true, false, false);
+      }
+    }
+    // coefficient, residual, momentum put back; then the flow's traces
+    const double mult = p.visc_mult*p.advect_length;
+    const double us_max = p.advect_length*p.unscaled_max*std::sqrt(2*p.freestream_energy/p.freestream_mass);
+    k_sav_finish<ND, RS><<<grid_for(n_elem, 1), 128, 0, c.stream>>>(m, wo, mult, us_max);
+    k_sav_residual<<<1, 256, 0, c.stream>>>(m.partials, n_elem, d_residual);
+    write_face(c, 0, n_elem);
+    refine(c, true, false, false);
+  }
+
   static const OpsTable* table()
   {
     static const OpsTable t = {
       compute_euler, compute_navier_stokes, max_dt, refine, write_face, bc_state, bc_flux, residual_norm,
       set_art_visc_admis, segment_residual_norms, local_elems_per_cta, admissible, compute_jacobian,
-      fix_admis_coef, ref_terms,
+      fix_admis_coef, ref_terms, update_art_visc_smoothness, sav_slot_dof,
     };
     return &t;
   }

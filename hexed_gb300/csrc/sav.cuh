@@ -1,0 +1,731 @@
+// sav.cuh -- smoothness-based artificial viscosity on the device (FP64):
+// Solver::update_art_visc_smoothness (src/Solver.cpp:457-582) and Solver::diffuse_art_visc
+// (src/Solver.cpp:428-455), the Spatial kernels applied to pde::Advection and
+// pde::Smooth_art_visc (include/pde.hpp:265-431).
+//
+// Storage beside the arena (allocated on first use, kept between calls like the reference's
+// element storage):
+//  * aux  [n_elem][4 + 2 rs][nq]: the four art_visc_forcing rows (Storage_params::n_forcing),
+//    the advection state (rs rows, 1 at creation as Solver's constructor sets it,
+//    src/Solver.cpp:201-211) and its residual cache (rs rows);
+//  * face [n_slot][slot_dof], slot_dof = max(2 nv, nd + rs) nfq: one slot per arena slot, the
+//    size of a reference Face_connection face (include/connection.hpp:58-66), LDG half at
+//    nv nfq as in Element::face (src/Element.cpp:189). The reference keeps these traces in the
+//    flow's face storage; here they have their own, so the flow's traces are untouched.
+// The flow state is used in place as the reference does: momentum is divided by sqrt(2 rho E)
+// (the advection velocity) and multiplied back at the end; the time-step-scale row holds the
+// pseudo-time steps; the bulk AV row receives the coefficient.
+//
+// Every kernel is FP64 with one thread per quadrature point (volume) or face point (faces):
+// an advection stage moves nd + 3 rs rows per element and its traces, and is bound by HBM like
+// the flow's inviscid kernel; the diffusion stages move 3-row fields.
+#pragma once
+#include "kernels.cuh"
+
+namespace hx {
+
+// Double views of the arena and of the smoothness-AV storage (both precision forms keep the
+// double metrics and normals beside their float copies).
+struct SavDev {
+  int n_car, n_elem, n_car_con, n_def_con, n_bc_con, n_ref;
+  double* elem;
+  double* aux;
+  double* face;
+  const double* nom_size;
+  const double* vert_tss;
+  const double* jac;
+  const double* face_nrml;
+  const int* car_con;
+  const int* def_con;
+  const double* def_con_nrml;
+  const int* bc_con;
+  const double* bc_nrml;
+  const int* ref_face;
+  const hexed_bc_spec* bc_spec;
+  double* partials;
+};
+
+template <int ND, int RS>
+struct SavShape {
+  static constexpr int nq = ipow(RS, ND), nfq = nq/RS, nv = ND + 2, nvert = 1 << ND;
+  static constexpr int n_forcing = 4;
+  static constexpr int n_adv = RS;                       // Storage_params::n_advection
+  static constexpr int n_aux = n_forcing + 2*n_adv;
+  static constexpr int n_adv_extrap = ND + n_adv;        // pde::Advection::n_extrap
+  static constexpr int n_sav = 3;                        // pde::Smooth_art_visc::n_extrap
+  static constexpr int slot_dof = (2*nv > n_adv_extrap ? 2*nv : n_adv_extrap)*nfq;
+  static __device__ __forceinline__ double* forcing(const SavDev& m, int e) { return m.aux + (size_t)e*n_aux*nq; }
+  static __device__ __forceinline__ double* adv(const SavDev& m, int e) { return forcing(m, e) + n_forcing*nq; }
+  static __device__ __forceinline__ double* adv_cache(const SavDev& m, int e) { return adv(m, e) + n_adv*nq; }
+  static __device__ __forceinline__ double* slot(const SavDev& m, int s, bool ldg)
+  {
+    return m.face + (size_t)s*slot_dof + (ldg ? nv*nfq : 0);
+  }
+  // quadrature point of node i of row i_fq along dimension d (include/Row_index.hpp)
+  static __device__ __forceinline__ int row_qpoint(int d, int i_fq, int i)
+  {
+    const int stride = ipow(RS, ND - 1 - d);
+    return (i_fq/stride)*stride*RS + i_fq%stride + i*stride;
+  }
+};
+
+// Row-local operators of Derivative (include/Derivative.hpp:22-60) and the advection nodes.
+template <int RS>
+struct SavTab {
+  double diff[RS*RS], bound[2*RS], lift[RS*2], node[RS], adv_node[RS];
+};
+
+template <int RS>
+inline SavTab<RS> make_savtab(const Tab<RS>& t)
+{
+  SavTab<RS> s;
+  for (int i = 0; i < RS*RS; ++i) s.diff[i] = t.diff[i];
+  for (int i = 0; i < 2*RS; ++i) { s.bound[i] = t.bound[i]; s.lift[i] = t.lift[i]; }
+  for (int i = 0; i < RS; ++i) { s.node[i] = t.node[i]; s.adv_node[i] = 2*t.node[i] - 1.; }   // pde.hpp:281
+  return s;
+}
+
+// Derivative::operator() for output node i of a row x with face values fb (Derivative.hpp:50-55):
+// sum_j diff[i][j] x_j + (lift[i][0] (fb0 - B0.x) + lift[i][1] (fb1 - B1.x)).
+template <int RS>
+__device__ __forceinline__ double row_derivative(const SavTab<RS>& t, const double (&x)[RS], double fb0, double fb1,
+                                                 int i)
+{
+  double b0 = 0., b1 = 0.;
+  #pragma unroll
+  for (int j = 0; j < RS; ++j) { b0 += t.bound[j]*x[j]; b1 += t.bound[RS + j]*x[j]; }
+  const double bf0 = fb0 - b0, bf1 = fb1 - b1;
+  double d = 0.;
+  #pragma unroll
+  for (int j = 0; j < RS; ++j) d += t.diff[i*RS + j]*x[j];
+  double l = 0.;
+  l += t.lift[i*2]*bf0;
+  l += t.lift[i*2 + 1]*bf1;
+  return d + l;
+}
+
+// math::interp of the vertex time-step scales at a qpoint (include/math.hpp:207-218)
+template <int ND, int RS>
+__device__ __forceinline__ double sav_spacing(const SavDev& m, const SavTab<RS>& t, int e, int q)
+{
+  constexpr int nvert = 1 << ND;
+  double vals[nvert];
+  #pragma unroll
+  for (int i = 0; i < nvert; ++i) vals[i] = m.vert_tss[(size_t)e*nvert + i];
+  int stride = nvert;
+  #pragma unroll
+  for (int d = 0; d < ND; ++d) {
+    const double coord = t.node[(q/ipow(RS, ND - 1 - d))%RS];
+    stride /= 2;
+    for (int i = 0; i < stride; ++i) vals[i] += coord*(vals[i + stride] - vals[i]);
+  }
+  return vals[0];
+}
+
+// Momentum over sqrt(2 rho E): the advection velocity (Solver.cpp:468-478).
+template <int ND, int RS>
+__global__ void k_sav_velocity(SavDev m)
+{
+  using S = SavShape<ND, RS>;
+  const long total = (long)m.n_elem*S::nq;
+  for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
+    const int e = int(t/S::nq), q = int(t%S::nq);
+    double* st = m.elem + (size_t)e*(S::nv + 3)*S::nq;
+    const double scale = sqrt(2*st[ND*S::nq + q]*st[(ND + 1)*S::nq + q]);
+    #pragma unroll
+    for (int d = 0; d < ND; ++d) st[d*S::nq + q] /= scale;
+  }
+}
+
+// Local time step of pde::Advection (char speed max(1, |v|), pde.hpp:343-346) or of
+// pde::Smooth_art_visc (diffusivity 1): Spatial::Max_dt with local time stepping
+// (include/Spatial.hpp:784-828). max_cfl = max_cfl_c (advection) or max_cfl_d (diffusion).
+template <int ND, int RS>
+__global__ void k_sav_max_dt(SavDev m, SavTab<RS> tab, int diffusion, double max_cfl)
+{
+  using S = SavShape<ND, RS>;
+  const long total = (long)m.n_elem*S::nq;
+  for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
+    const int e = int(t/S::nq), q = int(t%S::nq);
+    double* st = m.elem + (size_t)e*(S::nv + 3)*S::nq;
+    const double sp = sav_spacing<ND, RS>(m, tab, e, q);
+    double scale = 0;
+    if (diffusion) {
+      scale += 1./max_cfl/sp/sp;
+    } else {
+      double sq = 0.;
+      #pragma unroll
+      for (int d = 0; d < ND; ++d) sq += st[d*S::nq + q]*st[d*S::nq + q];
+      const double cs = fmax(1., sqrt(sq));
+      scale += cs/max_cfl/sp;
+    }
+    st[S::nv*S::nq + q] = 1./scale;
+  }
+}
+
+// Spatial::Write_face (include/Spatial.hpp:41-57) into the smoothness-AV slots: mode 0 the
+// Advection traces (velocity rows, then the advection state; pde.hpp:284-290), mode 1 the
+// Smooth_art_visc traces (forcing rows 1-3; pde.hpp:372-377). One thread per (element,
+// dimension, face point, variable) writes both faces of its row.
+template <int ND, int RS>
+__global__ void k_sav_write_face(SavDev m, SavTab<RS> tab, int mode)
+{
+  using S = SavShape<ND, RS>;
+  const int n_var = mode ? S::n_sav : S::n_adv_extrap;
+  const long total = (long)m.n_elem*ND*S::nfq*n_var;
+  for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
+    const int v = int(t%n_var);
+    long r = t/n_var;
+    const int i_fq = int(r%S::nfq);
+    r /= S::nfq;
+    const int d = int(r%ND), e = int(r/ND);
+    const double* row;
+    if (mode) row = S::forcing(m, e) + (1 + v)*S::nq;
+    else if (v < ND) row = m.elem + ((size_t)e*(S::nv + 3) + v)*S::nq;
+    else row = S::adv(m, e) + (v - ND)*S::nq;
+    double x[RS];
+    #pragma unroll
+    for (int i = 0; i < RS; ++i) x[i] = row[S::row_qpoint(d, i_fq, i)];
+    #pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      double acc = 0.;
+      #pragma unroll
+      for (int i = 0; i < RS; ++i) acc += tab.bound[s*RS + i]*x[i];
+      S::slot(m, e*2*ND + 2*d + s, false)[v*S::nfq + i_fq] = acc;
+    }
+  }
+}
+
+// Prolong_refined / Restrict_refined of NVAR variables of the smoothness-AV slots.
+template <int ND, int RS, bool PROLONG, int NVAR>
+__global__ void k_sav_refine(SavDev m, Tab<RS> tab, int scale, int offset)
+{
+  using S = SavShape<ND, RS>;
+  refine_face<ND, RS, PROLONG, NVAR, double>(m.face, S::slot_dof, S::nv*S::nfq, m.ref_face + 7*blockIdx.x, tab,
+                                             scale, offset);
+}
+
+// Flow_bc::apply_advection and its overrides (src/Boundary_condition.cpp:24-41, 346-368,
+// 429-448, 460-463); one thread per boundary face point.
+template <int ND, int RS>
+__global__ void k_sav_bc_advection(SavDev m)
+{
+  using S = SavShape<ND, RS>;
+  constexpr int nfq = S::nfq;
+  const long total = (long)m.n_bc_con*nfq;
+  for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
+    const int i = int(t/nfq), q = int(t%nfq);
+    const int* c = m.bc_con + 4*i;
+    const hexed_bc_spec& b = m.bc_spec[c[3]];
+    const double* in = S::slot(m, c[0], false);
+    double* gh = S::slot(m, c[1], false);
+    switch (b.kind) {
+      case HEXED_BC_NONPENETRATION: {
+        const double* nrml = m.bc_nrml + (size_t)i*ND*nfq;
+        double dot = 0., nsq = 0.;
+        #pragma unroll
+        for (int d = 0; d < ND; ++d) {
+          const double n = nrml[d*nfq + q];
+          dot += in[d*nfq + q]*n;
+          nsq += n*n;
+        }
+        #pragma unroll
+        for (int d = 0; d < ND; ++d) gh[d*nfq + q] = in[d*nfq + q] - 2*dot*nrml[d*nfq + q]/nsq;
+        for (int a = 0; a < S::n_adv; ++a) gh[(ND + a)*nfq + q] = in[(ND + a)*nfq + q];
+        break;
+      }
+      case HEXED_BC_NO_SLIP:
+        #pragma unroll
+        for (int d = 0; d < ND; ++d) gh[d*nfq + q] = -in[d*nfq + q];
+        for (int a = 0; a < S::n_adv; ++a) gh[(ND + a)*nfq + q] = in[(ND + a)*nfq + q];
+        break;
+      case HEXED_BC_COPY:
+        // copy_state (src/Boundary_condition.cpp:12-22): both halves of the face, nv nfq each
+        for (int k = 0; k < 2*S::nv; ++k) gh[k*nfq + q] = in[k*nfq + q];
+        break;
+      default:
+        // velocity as inside; advected scalars mirrored about 1
+        #pragma unroll
+        for (int d = 0; d < ND; ++d) gh[d*nfq + q] = in[d*nfq + q];
+        for (int a = 0; a < S::n_adv; ++a) gh[(ND + a)*nfq + q] = 2. - in[(ND + a)*nfq + q];
+    }
+  }
+}
+
+// Connection i of the concatenated lists (Cartesian, deformed, boundary): its slots, packed
+// direction and normal (null for Cartesian), with the direction encoding of Neighbor.
+__device__ __forceinline__ const double* sav_connection(const SavDev& m, int nd, int nfq, int i, int& s0, int& s1,
+                                                        int& dir)
+{
+  if (i < m.n_car_con) {
+    const int* c = m.car_con + 3*i;
+    s0 = c[0]; s1 = c[1]; dir = c[2] | (c[2] << 2) | (1 << 4);
+    return nullptr;
+  }
+  i -= m.n_car_con;
+  if (i < m.n_def_con) {
+    const int* c = m.def_con + 3*i;
+    s0 = c[0]; s1 = c[1]; dir = c[2];
+    return m.def_con_nrml + (size_t)i*nd*nfq;
+  }
+  i -= m.n_def_con;
+  const int* c = m.bc_con + 4*i;
+  s0 = c[0]; s1 = c[1]; dir = bc_dir(c[2]);
+  return m.bc_nrml + (size_t)i*nd*nfq;
+}
+
+// Spatial<pde::Advection>::Neighbor (include/Spatial.hpp:613-705): local Lax-Friedrichs flux
+// of the advected scalars, written over the first rs face variables of both sides.
+template <int ND, int RS>
+__global__ void k_sav_neighbor_advection(SavDev m, SavTab<RS> tab)
+{
+  using S = SavShape<ND, RS>;
+  constexpr int nfq = S::nfq, n_adv = S::n_adv, n_ex = S::n_adv_extrap;
+  const long total = (long)(m.n_car_con + m.n_def_con + m.n_bc_con)*nfq;
+  for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
+    int s0, s1, dir;
+    const double* nrml = sav_connection(m, ND, nfq, int(t/nfq), s0, s1, dir);
+    const int q = int(t%nfq);
+    const bool deformed = nrml != nullptr;
+    int sign0 = 1, sign1 = 1;
+    if (deformed) {
+      sign0 = 1 - 2*(((dir >> 4) & 1) == 0);
+      sign1 = 1 - 2*(((dir >> 5) & 1) == 1);
+    }
+    const int q1 = deformed ? perm_index<ND, RS>(dir, q) : q;
+    double* f0 = S::slot(m, s0, false);
+    double* f1 = S::slot(m, s1, false);
+    double n[ND];
+    #pragma unroll
+    for (int d = 0; d < ND; ++d) n[d] = deformed ? sign0*nrml[d*nfq + q] : (d == (dir & 3) ? 1. : 0.);
+    double u0[n_ex], u1[n_ex];
+    #pragma unroll
+    for (int v = 0; v < n_ex; ++v) { u0[v] = f0[v*nfq + q]; u1[v] = f1[v*nfq + q1]; }
+    double nv0 = 0., nv1 = 0., sq0 = 0., sq1 = 0.;
+    #pragma unroll
+    for (int d = 0; d < ND; ++d) { nv0 += u0[d]*n[d]; nv1 += u1[d]*n[d]; }
+    #pragma unroll
+    for (int d = 0; d < ND; ++d) { sq0 += u0[d]*u0[d]; sq1 += u1[d]*u1[d]; }
+    const double cs0 = fmax(1., sqrt(sq0)), cs1 = fmax(1., sqrt(sq1));
+    double nn = 0.;
+    #pragma unroll
+    for (int d = 0; d < ND; ++d) nn += n[d]*n[d];
+    const double mult = fmax(cs0, cs1)*sqrt(nn);
+    #pragma unroll
+    for (int a = 0; a < n_adv; ++a) {
+      const double fl0 = tab.adv_node[a]*nv0*u0[ND + a];
+      const double fl1 = tab.adv_node[a]*nv1*u1[ND + a];
+      const double flux = .5*(fl0 + fl1 + mult*(u0[ND + a] - u1[ND + a]));
+      f0[a*nfq + q] = sign0*flux;
+      f1[a*nfq + q1] = sign1*flux;
+    }
+  }
+}
+
+// Spatial<pde::Advection>::Local (include/Spatial.hpp:326-509): flux node_a (v.n_i) a_a, the
+// source 2/advect_length in the first stage, and Advection::write_update (pde.hpp:292-300):
+// pseudo = 1 + 2 tss/advect_length; the first stage sets a = (a + update)/pseudo, the second
+// adds update/pseudo. One CTA per element, one thread per quadrature point; the fluxes of the
+// element sit in shared memory [nd][rs][nq].
+template <int ND, int RS>
+__global__ void __launch_bounds__(SavShape<ND, RS>::nq < 64 ? 64 : SavShape<ND, RS>::nq)
+k_sav_local_advection(SavDev m, SavTab<RS> tab, int stage, double advect_length, double step_ratio)
+{
+  using S = SavShape<ND, RS>;
+  constexpr int nq = S::nq, nfq = S::nfq, n_adv = S::n_adv;
+  extern __shared__ double s_flux[];   // [ND][n_adv][nq]
+  const int e = blockIdx.x;
+  const int q = threadIdx.x;
+  const bool deformed = e >= m.n_car;
+  double* st = m.elem + (size_t)e*(S::nv + 3)*nq;
+  double* a_st = S::adv(m, e);
+  double* rcache = S::adv_cache(m, e);
+  const double* nrml = deformed ? m.jac + (size_t)(e - m.n_car)*(ND*ND + 1)*nq : nullptr;
+  const double d_pos = m.nom_size[e];
+  if (q < nq) {
+    #pragma unroll
+    for (int i = 0; i < ND; ++i) {
+      double nrml_veloc = 0;
+      #pragma unroll
+      for (int j = 0; j < ND; ++j) nrml_veloc += st[j*nq + q]*(deformed ? nrml[(i*ND + j)*nq + q] : (i == j ? 1. : 0.));
+      for (int a = 0; a < n_adv; ++a) s_flux[(i*n_adv + a)*nq + q] = tab.adv_node[a]*nrml_veloc*a_st[a*nq + q];
+    }
+  }
+  __syncthreads();
+  if (q >= nq) return;
+  double rate[n_adv];
+  #pragma unroll
+  for (int a = 0; a < n_adv; ++a) rate[a] = 0.;
+  #pragma unroll
+  for (int d = 0; d < ND; ++d) {
+    const int stride = ipow(RS, ND - 1 - d);
+    const int i = (q/stride)%RS;
+    const int i_fq = (q/(stride*RS))*stride + q%stride;
+    const double* fa = S::slot(m, e*2*ND + 2*d, false);
+    const double* fb = S::slot(m, e*2*ND + 2*d + 1, false);
+    #pragma unroll
+    for (int a = 0; a < n_adv; ++a) {
+      double x[RS];
+      #pragma unroll
+      for (int k = 0; k < RS; ++k) x[k] = s_flux[(d*n_adv + a)*nq + q - i*stride + k*stride];
+      const double der = row_derivative<RS>(tab, x, fa[a*nfq + i_fq], fb[a*nfq + i_fq], i);
+      rate[a] = 1.*rate[a] + -der;
+    }
+  }
+  const double tss = st[S::nv*nq + q];
+  const double det = deformed ? nrml[ND*ND*nq + q] : 1.;
+  const double update_coef = stage ? 1.*step_ratio : 1.;
+  double mult = update_coef*tss/d_pos;
+  if (deformed) mult /= det;
+  const double pseudo = 1 + tss*2/advect_length;
+  double src_mult = d_pos;
+  if (deformed) src_mult *= det;
+  const double source = src_mult*(2/advect_length);
+  #pragma unroll
+  for (int a = 0; a < n_adv; ++a) {
+    double u = rate[a];
+    if (stage) {
+      u -= rcache[a*nq + q];
+    } else {
+      rcache[a*nq + q] = u;
+      u += source;
+    }
+    u *= mult;
+    const double x = a_st[a*nq + q];
+    a_st[a*nq + q] = stage ? x + u/pseudo : (x + u)/pseudo;
+  }
+}
+
+// Solver.cpp:527-542: projection of the advection state onto the Legendre mode of degree
+// av_rs - 1 (w[i] weight_i, ow[i] orthogonal(av_rs - 1)_i), into forcing row 0 as
+// proj^2 * 2 E / rho.
+template <int ND, int RS>
+__global__ void k_sav_project(SavDev m, AvTab<RS, double> wo)
+{
+  using S = SavShape<ND, RS>;
+  const long total = (long)m.n_elem*S::nq;
+  for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
+    const int e = int(t/S::nq), q = int(t%S::nq);
+    const double* a_st = S::adv(m, e);
+    const double* st = m.elem + (size_t)e*(S::nv + 3)*S::nq;
+    double proj = 0;
+    #pragma unroll
+    for (int i = 0; i < RS; ++i) proj += a_st[i*S::nq + q]*wo.w[i]*wo.ow[i];
+    S::forcing(m, e)[q] = proj*proj*2*st[(ND + 1)*S::nq + q]/st[ND*S::nq + q];
+  }
+}
+
+// Flow_bc::apply_diffusion (ghost state = inside, src/Boundary_condition.cpp:43-52) or
+// flux_diffusion (ghost LDG flux = -inside, :54-60) over nv face variables.
+template <int ND, int RS>
+__global__ void k_sav_bc_diffusion(SavDev m, int flux)
+{
+  using S = SavShape<ND, RS>;
+  constexpr int nfq = S::nfq;
+  const long total = (long)m.n_bc_con*nfq;
+  for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
+    const int i = int(t/nfq), q = int(t%nfq);
+    const int* c = m.bc_con + 4*i;
+    const double* in = S::slot(m, c[0], flux);
+    double* gh = S::slot(m, c[1], flux);
+    for (int v = 0; v < S::nv; ++v) gh[v*nfq + q] = flux ? -in[v*nfq + q] : in[v*nfq + q];
+  }
+}
+
+// Spatial<pde::Smooth_art_visc>::Neighbor (reconcile = 0: the LDG average of the three traces
+// on both sides) and Neighbor_reconcile (reconcile = 1, include/Spatial.hpp:716-759).
+template <int ND, int RS>
+__global__ void k_sav_neighbor_ldg(SavDev m, int reconcile)
+{
+  using S = SavShape<ND, RS>;
+  constexpr int nfq = S::nfq;
+  const long total = (long)(m.n_car_con + m.n_def_con + m.n_bc_con)*nfq;
+  for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
+    int s0, s1, dir;
+    const double* nrml = sav_connection(m, ND, nfq, int(t/nfq), s0, s1, dir);
+    const int q = int(t%nfq);
+    const bool deformed = nrml != nullptr;
+    const int q1 = deformed ? perm_index<ND, RS>(dir, q) : q;
+    double* l0 = S::slot(m, s0, true);
+    double* l1 = S::slot(m, s1, true);
+    if (!reconcile) {
+      const double* f0 = S::slot(m, s0, false);
+      const double* f1 = S::slot(m, s1, false);
+      #pragma unroll
+      for (int v = 0; v < S::n_sav; ++v) {
+        const double avg = .5*(f0[v*nfq + q] + f1[v*nfq + q1]);
+        l0[v*nfq + q] = avg;
+        l1[v*nfq + q1] = avg;
+      }
+    } else {
+      int sign0 = 1, sign1 = 1;
+      if (deformed) {
+        sign0 = 1 - 2*(((dir >> 4) & 1) == 0);
+        sign1 = 1 - 2*(((dir >> 5) & 1) == 1);
+      }
+      #pragma unroll
+      for (int v = 0; v < S::n_sav; ++v) {
+        const double a = l0[v*nfq + q], b = l1[v*nfq + q1];
+        double avg = 0;
+        avg += .5*sign0*a;
+        avg += .5*sign1*b;
+        l0[v*nfq + q] = sign0*avg - a;
+        l1[v*nfq + q1] = sign1*avg - b;
+      }
+    }
+  }
+}
+
+// Spatial<pde::Smooth_art_visc>::Local, first stage (include/Spatial.hpp:326-509): the
+// unknowns are forcing rows 1-3, their gradient (times the Jacobian determinant, product rule
+// with the metric on deformed elements, Spatial.hpp:371-402) gives the flux -gradient.normal
+// (diffusivity 1); the source of unknown v is f(forcing row v)/diff_time with f = |x| for rows
+// 0 and 2 and sqrt|x| for row 1 (pde.hpp:422-429); the flux's face values go to the LDG faces
+// and write_update adds (pde.hpp:379-387). One CTA per element, one thread per quadrature
+// point; shared memory holds the three rows and then the fluxes [nd][3][nq].
+template <int ND, int RS>
+__global__ void __launch_bounds__(SavShape<ND, RS>::nq < 64 ? 64 : SavShape<ND, RS>::nq)
+k_sav_local_diffusion(SavDev m, SavTab<RS> tab, double dt, double diff_time)
+{
+  using S = SavShape<ND, RS>;
+  constexpr int nq = S::nq, nfq = S::nfq, n_sav = S::n_sav;
+  extern __shared__ double s_mem[];
+  double* s_r = s_mem;                   // [3][nq]
+  double* s_f = s_mem + n_sav*nq;        // [ND][3][nq]
+  const int e = blockIdx.x;
+  const int q = threadIdx.x;
+  const bool deformed = e >= m.n_car;
+  const double* st = m.elem + (size_t)e*(S::nv + 3)*nq;
+  double* fc = S::forcing(m, e);
+  const double d_pos = m.nom_size[e];
+  const int ed = e - m.n_car;
+  const double* nrml = deformed ? m.jac + (size_t)ed*(ND*ND + 1)*nq : nullptr;
+  if (q < nq) {
+    #pragma unroll
+    for (int v = 0; v < n_sav; ++v) s_r[v*nq + q] = fc[(1 + v)*nq + q];
+  }
+  __syncthreads();
+  if (q < nq) {
+    double g[n_sav][ND];
+    #pragma unroll
+    for (int v = 0; v < n_sav; ++v)
+      #pragma unroll
+      for (int d = 0; d < ND; ++d) g[v][d] = 0.;
+    #pragma unroll
+    for (int d = 0; d < ND; ++d) {
+      const int stride = ipow(RS, ND - 1 - d);
+      const int i = (q/stride)%RS;
+      const int i_fq = (q/(stride*RS))*stride + q%stride;
+      const int r0 = q - i*stride;
+      const double* la = S::slot(m, e*2*ND + 2*d, true);
+      const double* lb = S::slot(m, e*2*ND + 2*d + 1, true);
+      if (deformed) {
+        const double* fna = m.face_nrml + ((size_t)ed*2*ND + 2*d)*ND*nfq;
+        const double* fnb = fna + ND*nfq;
+        #pragma unroll
+        for (int j = 0; j < ND; ++j) {
+          double row_n[RS];
+          #pragma unroll
+          for (int k = 0; k < RS; ++k) row_n[k] = nrml[(d*ND + j)*nq + r0 + k*stride];
+          #pragma unroll
+          for (int v = 0; v < n_sav; ++v) {
+            double x[RS];
+            #pragma unroll
+            for (int k = 0; k < RS; ++k) x[k] = row_n[k]*s_r[v*nq + r0 + k*stride];
+            const double der = row_derivative<RS>(tab, x, fna[j*nfq + i_fq]*la[v*nfq + i_fq],
+                                                  fnb[j*nfq + i_fq]*lb[v*nfq + i_fq], i);
+            g[v][j] = 1.*g[v][j] + der/d_pos;
+          }
+        }
+      } else {
+        #pragma unroll
+        for (int v = 0; v < n_sav; ++v) {
+          double x[RS];
+          #pragma unroll
+          for (int k = 0; k < RS; ++k) x[k] = s_r[v*nq + r0 + k*stride];
+          const double der = row_derivative<RS>(tab, x, la[v*nfq + i_fq], lb[v*nfq + i_fq], i);
+          g[v][d] = 0*g[v][d] + der/d_pos;
+        }
+      }
+    }
+    // flux -gradient.normal (Spatial.hpp:405-442)
+    const double det = deformed ? nrml[ND*ND*nq + q] : 1.;
+    #pragma unroll
+    for (int v = 0; v < n_sav; ++v) {
+      if (deformed) {
+        #pragma unroll
+        for (int d = 0; d < ND; ++d) g[v][d] /= det;
+      }
+      #pragma unroll
+      for (int i = 0; i < ND; ++i) {
+        double acc = 0.;
+        #pragma unroll
+        for (int j = 0; j < ND; ++j) acc += -g[v][j]*(deformed ? nrml[(i*ND + j)*nq + q] : (i == j ? 1. : 0.));
+        s_f[(i*n_sav + v)*nq + q] = acc;
+      }
+    }
+  }
+  __syncthreads();
+  // the flux's face values to the LDG faces: one thread per (dimension, face point, unknown)
+  for (int t = threadIdx.x; t < ND*nfq*n_sav; t += blockDim.x) {
+    const int v = t%n_sav, i_fq = (t/n_sav)%nfq, d = t/(n_sav*nfq);
+    double x[RS];
+    #pragma unroll
+    for (int k = 0; k < RS; ++k) x[k] = s_f[(d*n_sav + v)*nq + S::row_qpoint(d, i_fq, k)];
+    #pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      double acc = 0.;
+      #pragma unroll
+      for (int k = 0; k < RS; ++k) acc += tab.bound[s*RS + k]*x[k];
+      S::slot(m, e*2*ND + 2*d + s, true)[v*nfq + i_fq] = acc;
+    }
+  }
+  if (q >= nq) return;
+  // source, then the interior divergence of the flux (Spatial.hpp:445-470)
+  double mult_src = d_pos;
+  const double det = deformed ? nrml[ND*ND*nq + q] : 1.;
+  if (deformed) mult_src *= det;
+  double rate[n_sav];
+  #pragma unroll
+  for (int v = 0; v < n_sav; ++v) {
+    const double f = fabs(fc[v*nq + q]);
+    rate[v] = mult_src*(((v == 1) ? sqrt(f) : f)/diff_time);
+  }
+  #pragma unroll
+  for (int d = 0; d < ND; ++d) {
+    const int stride = ipow(RS, ND - 1 - d);
+    const int i = (q/stride)%RS;
+    const int r0 = q - i*stride;
+    #pragma unroll
+    for (int v = 0; v < n_sav; ++v) {
+      double der = 0.;
+      #pragma unroll
+      for (int k = 0; k < RS; ++k) der += tab.diff[i*RS + k]*s_f[(d*n_sav + v)*nq + r0 + k*stride];
+      rate[v] = 1.*rate[v] + -der;
+    }
+  }
+  double mult = dt*st[S::nv*nq + q]/d_pos;
+  if (deformed) mult /= det;
+  #pragma unroll
+  for (int v = 0; v < n_sav; ++v) {
+    double u = 0.;
+    u += rate[v];
+    u *= mult;
+    fc[(1 + v)*nq + q] += u;
+  }
+}
+
+// Spatial<pde::Smooth_art_visc>::Reconcile_ldg_flux (include/Spatial.hpp:543-594): lift of the
+// flux differences, then the critical write_update (pde.hpp:379-387): add, then divide by
+// pseudo = 1 + tss cheby/diff_time. One thread per quadrature point.
+template <int ND, int RS>
+__global__ void k_sav_reconcile(SavDev m, SavTab<RS> tab, double dt, double diff_time, double cheby)
+{
+  using S = SavShape<ND, RS>;
+  constexpr int nq = S::nq, nfq = S::nfq, n_sav = S::n_sav;
+  const long total = (long)m.n_elem*nq;
+  for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
+    const int e = int(t/nq), q = int(t%nq);
+    const bool deformed = e >= m.n_car;
+    double rate[n_sav];
+    #pragma unroll
+    for (int v = 0; v < n_sav; ++v) rate[v] = 0.;
+    #pragma unroll
+    for (int d = 0; d < ND; ++d) {
+      const int stride = ipow(RS, ND - 1 - d);
+      const int i = (q/stride)%RS;
+      const int i_fq = (q/(stride*RS))*stride + q%stride;
+      const double* la = S::slot(m, e*2*ND + 2*d, true);
+      const double* lb = S::slot(m, e*2*ND + 2*d + 1, true);
+      #pragma unroll
+      for (int v = 0; v < n_sav; ++v) {
+        double l = 0.;
+        l += tab.lift[i*2]*la[v*nfq + i_fq];
+        l += tab.lift[i*2 + 1]*lb[v*nfq + i_fq];
+        rate[v] = 1.*rate[v] + -l;
+      }
+    }
+    const double* st = m.elem + (size_t)e*(S::nv + 3)*nq;
+    const double tss = st[S::nv*nq + q];
+    double mult = dt*tss/m.nom_size[e];
+    if (deformed) mult /= m.jac[((size_t)(e - m.n_car)*(ND*ND + 1) + ND*ND)*nq + q];
+    const double pseudo = 1 + tss*cheby/diff_time;
+    double* fc = S::forcing(m, e);
+    #pragma unroll
+    for (int v = 0; v < n_sav; ++v) {
+      double x = fc[(1 + v)*nq + q];
+      x += rate[v]*mult;
+      x /= pseudo;
+      fc[(1 + v)*nq + q] = x;
+    }
+  }
+}
+
+// Solver.cpp:552-575: the bulk AV coefficient us_max f/(us_max + f) from forcing row 3, the
+// element's share of art_visc_residual (partials[e]) and the momentum put back.
+template <int ND, int RS>
+__global__ void k_sav_finish(SavDev m, AvTab<RS, double> wt, double mult, double us_max)
+{
+  using S = SavShape<ND, RS>;
+  constexpr int nq = S::nq;
+  __shared__ double s_sum[32];
+  for (int e = blockIdx.x; e < m.n_elem; e += gridDim.x) {
+    double* st = m.elem + (size_t)e*(S::nv + 3)*nq;
+    double* av = st + (S::nv + 1)*nq;
+    const double* fc = S::forcing(m, e);
+    double volume = 1.;
+    #pragma unroll
+    for (int d = 0; d < ND; ++d) volume *= m.nom_size[e];
+    double part = 0.;
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+      double qw = 1.;
+      #pragma unroll
+      for (int d = 0; d < ND; ++d) qw *= wt.w[(q/ipow(RS, ND - 1 - d))%RS];
+      const double f = mult*fc[(S::n_forcing - 1)*nq + q];
+      const double new_av = us_max*f/(us_max + f);
+      const double diff = av[q] - new_av;
+      part += diff*diff*qw*volume;
+      av[q] = new_av;
+      const double scale = sqrt(2*st[ND*nq + q]*st[(ND + 1)*nq + q]);
+      #pragma unroll
+      for (int d = 0; d < ND; ++d) st[d*nq + q] *= scale;
+    }
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);
+    if ((threadIdx.x & 31) == 0) s_sum[threadIdx.x/32] = part;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double sum = 0.;
+      for (int w = 0; w < (int)(blockDim.x + 31)/32; ++w) sum += s_sum[w];
+      m.partials[e] = sum;
+    }
+    __syncthreads();
+  }
+}
+
+// The advection state starts at 1 (Solver's constructor, src/Solver.cpp:201-211).
+static __global__ void k_sav_init(double* aux, long n_elem, int n_aux, int first_row, int n_rows, int nq)
+{
+  const long total = n_elem*n_rows*nq;
+  for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
+    const long e = t/((long)n_rows*nq), k = t%((long)n_rows*nq);
+    aux[(e*n_aux + first_row)*nq + k] = 1.;
+  }
+}
+
+// sum of the per-element partials, then sqrt
+static __global__ void k_sav_residual(const double* partials, int n, double* out)
+{
+  __shared__ double s_sum[256];
+  double acc = 0.;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) acc += partials[i];
+  s_sum[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = blockDim.x/2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) s_sum[threadIdx.x] += s_sum[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sqrt(s_sum[0]);
+}
+
+} // namespace hx

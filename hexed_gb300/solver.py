@@ -115,6 +115,21 @@ class Context:
     def set_art_visc_admis(self, char_speed):
         abi.check(self.lib.hexed_gpu_set_art_visc_admis(self.handle, char_speed))
 
+    def update_art_visc_smoothness(self, params):
+        """Solver::update_art_visc_smoothness: writes the bulk AV row; returns art_visc_residual."""
+        out = ctypes.c_double()
+        abi.check(self.lib.hexed_gpu_update_art_visc_smoothness(self.handle, ctypes.byref(params), ctypes.byref(out)))
+        return out.value
+
+    def sav_storage(self):
+        """The smoothness-AV storage: aux [n_elem][4 + 2 rs][nq] (forcing rows, advection state,
+        its residual cache) and the face slots [n_slot][max(2 nv, nd + rs) nfq]."""
+        a = self.arena
+        slot_dof = max(2 * a.nv, a.n_dim + a.row_size) * a.nfq
+        aux = self.read_range(abi.ARRAY_SAV_AUX, 0, a.n_elem * (4 + 2 * a.row_size) * a.nq)
+        face = self.read_range(abi.ARRAY_SAV_FACE, 0, a.n_slot * slot_dof)
+        return aux.reshape(a.n_elem, 4 + 2 * a.row_size, a.nq), face.reshape(a.n_slot, slot_dof)
+
     def apply_flux_bcs(self):
         abi.check(self.lib.hexed_gpu_apply_flux_bcs(self.handle))
 

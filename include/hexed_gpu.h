@@ -140,7 +140,13 @@ enum hexed_array {
                                  (write it before the element's state and traces) */
   HEXED_ARRAY_JAC = 8,        /* [n_def][nd*nd + 1][nq] (read / write) */
   HEXED_ARRAY_FACE_NRML = 9,  /* [n_def][2nd][nd][nfq] */
-  HEXED_ARRAY_DEF_CON_NRML = 10 /* [n_def_con][nd][nfq] */
+  HEXED_ARRAY_DEF_CON_NRML = 10, /* [n_def_con][nd][nfq] */
+  HEXED_ARRAY_SAV_AUX = 11,   /* smoothness-based AV storage [n_elem][4 + 2 rs][nq]: the four
+                                 forcing rows, the advection state (rs rows, 1 at creation) and
+                                 its residual cache (rs rows); allocated on first use */
+  HEXED_ARRAY_SAV_FACE = 12   /* smoothness-based AV face slots [n_slot][max(2 nv, nd + rs) nfq]
+                                 (the size of a reference Face_connection face), LDG half at
+                                 nv nfq; allocated on first use */
 };
 
 /* Arithmetic of the volume and face kernels. */
@@ -293,6 +299,37 @@ int hexed_gpu_write_face_range(hexed_gpu_ctx* ctx, int elem_begin, int elem_coun
  * char_speed, maximum over the elements sharing each vertex, multilinear interpolation to
  * the quadrature points into the Laplacian AV row. Needs the arena's vertex table. */
 int hexed_gpu_set_art_visc_admis(hexed_gpu_ctx* ctx, double char_speed);
+
+/* Settings of Solver::update_art_visc_smoothness (src/Solver.cpp:457-582) and
+ * Solver::diffuse_art_visc (src/Solver.cpp:428-455); the reference's defaults
+ * (src/Solver.cpp:154-163) in brackets. */
+typedef struct hexed_sav_params {
+  double advect_length;      /* the `advect_length` argument (Case: art_visc_width) */
+  int advect_iters;          /* av_advect_iters [1] */
+  int diff_iters;            /* av_diff_iters [1] */
+  int n_cheby;               /* n_cheby_av [1] */
+  int av_row_size;           /* av_rs, degree + 1 of the projected Legendre mode [row_size] */
+  double advect_safety;      /* av_advect_max_safety [0.7] */
+  double diff_safety;        /* av_diff_max_safety [0.7] */
+  double diff_ratio;         /* av_diff_ratio [0.3] */
+  double visc_mult;          /* av_visc_mult [100] */
+  double unscaled_max;       /* av_unscaled_max [5] */
+  double freestream_mass;    /* freestream{n_dim} */
+  double freestream_energy;  /* freestream{n_dim + 1} */
+} hexed_sav_params;
+
+/* Solver::update_art_visc_smoothness (src/Solver.cpp:457-582): the smoothness-based artificial
+ * viscosity of set_shock. advect_iters pseudo-time iterations of pde::Advection (two stages,
+ * local time step) estimate a high-order derivative of the flow; its projection onto the
+ * Legendre mode of degree av_row_size - 1 is smeared by n_forcing - 1 = 3 implicit diffusion
+ * steps of pde::Smooth_art_visc (diff_iters x n_cheby sub-steps, Solver::diffuse_art_visc);
+ * the bulk AV row receives us_max f/(us_max + f). The flow state is restored and its face
+ * traces re-extrapolated (Write_face, Prolong); the time-step-scale row holds the last
+ * pseudo-time step, as in the reference. *residual (may be NULL) receives art_visc_residual
+ * (reading it synchronizes). The storage of HEXED_ARRAY_SAV_AUX / HEXED_ARRAY_SAV_FACE is
+ * allocated on the first call and persists: the advection state carries over between calls
+ * as the reference's element storage does. FP64 arithmetic in both precision forms. */
+int hexed_gpu_update_art_visc_smoothness(hexed_gpu_ctx* ctx, const hexed_sav_params* params, double* residual);
 
 /* Solver::apply_state_bcs / apply_flux_bcs (src/Solver.cpp:56-81). */
 int hexed_gpu_apply_state_bcs(hexed_gpu_ctx* ctx);
