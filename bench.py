@@ -458,6 +458,58 @@ def timed_updates(ctx, p, args, stream, barrier, local_rank):
     return ms, prof, clk
 
 
+def sav_advection_bytes(ar):
+    """Compulsory bytes of one launch of the smoothness-AV advection volume kernel: per element
+    the nd velocity rows, the advection state read and written, its residual cache written
+    (first stage) or read (second), the time-step scale, the deformed metric rows (nd^2 + 1),
+    and the rs flux traces of each of the 2 nd faces; all double."""
+    nd, rs, nq, nfq = ar.n_dim, ar.row_size, ar.nq, ar.nfq
+    per_elem = 8 * (nd * nq + 3 * rs * nq + nq + 2 * nd * rs * nfq)
+    return per_elem * ar.n_elem + 8 * (nd * nd + 1) * nq * ar.n_def
+
+
+def smooth_av_sample(wl, args, hbm_peak):
+    """Solver::update_art_visc_smoothness on the workload's arena (FP64): `sav_iters` advection
+    iterations (two stages each) and `sav_iters` / 2 diffusion iterations; the whole call timed
+    with CUDA events, then the same call under the per-kernel profiler for the advection volume
+    kernel's HBM roofline."""
+    import torch
+    from hexed_gb300.solver import Context
+    ar = wl.arena()
+    fs_mass = float(np.mean(ar.elem[:, ar.n_dim]))
+    fs_energy = float(np.mean(ar.elem[:, ar.n_dim + 1]))
+    length = 2.0 * float(np.mean(ar.nom_size))
+    p = abi.sav_params(length, ar.row_size, fs_mass, fs_energy, advect_iters=args.sav_iters,
+                       diff_iters=max(1, args.sav_iters // 2))
+    with Context(ar, abi.FP64) as c:
+        initialize(c)
+        stream = torch.cuda.ExternalStream(c.stream_ptr)
+        c.update_art_visc_smoothness(p)   # warm-up (allocates the storage)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        c.update_art_visc_smoothness(p)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        c.profile_enable(True)
+        c.update_art_visc_smoothness(p)
+        prof = c.profile_read()
+        c.profile_enable(False)
+    launches, total = prof.get("sav_local_advection", (0, 0.))
+    per_launch = total / max(launches, 1)
+    nbytes = sav_advection_bytes(ar)
+    achieved = nbytes / (per_launch * 1e-3) / 1e9 if per_launch else None
+    return {"workload": wl.name, "advect_iters": p.advect_iters, "diff_iters": p.diff_iters,
+            "advect_length": length, "ms_per_call": ms,
+            "ms_per_advection_iteration": ms / (p.advect_iters + p.diff_iters),
+            "roofline": {"bound": "hbm", "kernel": "sav_local_advection", "achieved": achieved, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": achieved / hbm_peak if achieved else None,
+                         "algorithmic_bytes_per_launch": nbytes, "launch_ms": per_launch},
+            "kernels": {k: {"launches": v[0], "total_ms": round(v[1], 4)}
+                        for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])}}
+
+
 def serving_sample(args):
     """A bounded sample of the serving stream (steady 2D Euler solves, Cartesian meshes of
     sides uniform in [8, serving_max_side], row size 4 or 6, Mach U(0.2, 0.8), angle
@@ -517,6 +569,8 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving sample of the default line")
     ap.add_argument("--serving-solves", type=int, default=24, help="solves in the default line's serving sample")
     ap.add_argument("--serving-max-side", type=int, default=16)
+    ap.add_argument("--no-smooth-av", action="store_true", help="skip the smoothness-AV measurement")
+    ap.add_argument("--sav-iters", type=int, default=20, help="advection iterations of the smoothness-AV sample")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -652,6 +706,11 @@ def main():
                              for k, v in sorted(mprof.items(), key=lambda kv: -kv[1][1])},
                  "error_vs_fp64": mixed_vs_fp64(wl, args.err_steps) if args.err_steps > 0 else None}
 
+    sav_line = None
+    if rank == 0 and world == 1 and not args.no_smooth_av:
+        ctx.close()
+        sav_line = smooth_av_sample(wl, args, hbm_peak)
+
     serving_line = None
     if rank == 0 and world == 1 and not args.no_serving:
         ctx.close()
@@ -685,6 +744,8 @@ def main():
             line["mixed"] = mixed
         if serving_line is not None:
             line["serving"] = serving_line
+        if sav_line is not None:
+            line["smooth_av"] = sav_line
         print(json.dumps(line))
     if pg:
         pg.destroy_process_group()
