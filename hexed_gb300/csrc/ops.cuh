@@ -435,7 +435,7 @@ struct Runner
     const long n_face_pts = (long)(m.n_car_con + m.n_def_con + m.n_bc_con)*SS::nfq;
     const int g_con = grid_for(n_face_pts, 256);
     const int g_bc = grid_for((long)m.n_bc_con*SS::nfq, 256);
-    const int blk = (nq + 31)/32*32 < 64 ? 64 : (nq + 31)/32*32;
+    constexpr int blk = SS::block;   // the volume kernels' launch bound
     constexpr size_t smem_adv = sizeof(double)*ND*SS::n_adv*nq;
     constexpr size_t smem_diff = sizeof(double)*(SS::n_sav + ND*SS::n_sav)*nq;
     static bool configured = false;

@@ -54,6 +54,8 @@ struct SavShape {
   static constexpr int n_adv_extrap = ND + n_adv;        // pde::Advection::n_extrap
   static constexpr int n_sav = 3;                        // pde::Smooth_art_visc::n_extrap
   static constexpr int slot_dof = (2*nv > n_adv_extrap ? 2*nv : n_adv_extrap)*nfq;
+  // threads of the per-element volume kernels: one per quadrature point, whole warps, >= 64
+  static constexpr int block = (nq + 31)/32*32 < 64 ? 64 : (nq + 31)/32*32;
   static __device__ __forceinline__ double* forcing(const SavDev& m, int e) { return m.aux + (size_t)e*n_aux*nq; }
   static __device__ __forceinline__ double* adv(const SavDev& m, int e) { return forcing(m, e) + n_forcing*nq; }
   static __device__ __forceinline__ double* adv_cache(const SavDev& m, int e) { return adv(m, e) + n_adv*nq; }
@@ -328,7 +330,7 @@ __global__ void k_sav_neighbor_advection(SavDev m, SavTab<RS> tab)
 // adds update/pseudo. One CTA per element, one thread per quadrature point; the fluxes of the
 // element sit in shared memory [nd][rs][nq].
 template <int ND, int RS>
-__global__ void __launch_bounds__(SavShape<ND, RS>::nq < 64 ? 64 : SavShape<ND, RS>::nq)
+__global__ void __launch_bounds__(SavShape<ND, RS>::block)
 k_sav_local_advection(SavDev m, SavTab<RS> tab, int stage, double advect_length, double step_ratio)
 {
   using S = SavShape<ND, RS>;
@@ -484,7 +486,7 @@ __global__ void k_sav_neighbor_ldg(SavDev m, int reconcile)
 // and write_update adds (pde.hpp:379-387). One CTA per element, one thread per quadrature
 // point; shared memory holds the three rows and then the fluxes [nd][3][nq].
 template <int ND, int RS>
-__global__ void __launch_bounds__(SavShape<ND, RS>::nq < 64 ? 64 : SavShape<ND, RS>::nq)
+__global__ void __launch_bounds__(SavShape<ND, RS>::block)
 k_sav_local_diffusion(SavDev m, SavTab<RS> tab, double dt, double diff_time)
 {
   using S = SavShape<ND, RS>;

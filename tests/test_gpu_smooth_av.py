@@ -118,7 +118,7 @@ def test_strip_3d():
     check(ar, 0.1, name="sav_strip_3d", advect_iters=60, diff_iters=30)
 
 
-@pytest.mark.parametrize("nd,rs", [(2, 4), (2, 6), (3, 3), (3, 5)])
+@pytest.mark.parametrize("nd,rs", [(2, 4), (2, 6), (3, 3), (3, 5), (3, 6)])
 def test_curved_mesh(nd, rs):
     spec = bc_spec(abi.BC_FREESTREAM, freestream=[1.1] + [0.] * (nd - 1) + [1., 1.5])
     ar = structured_mesh(nd, rs, 3, 0., 1., deformed=True,
