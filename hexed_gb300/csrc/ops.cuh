@@ -436,8 +436,8 @@ struct Runner
     const int g_con = grid_for(n_face_pts, 256);
     const int g_bc = grid_for((long)m.n_bc_con*SS::nfq, 256);
     constexpr int blk = SS::block;   // the volume kernels' launch bound
-    constexpr size_t smem_adv = sizeof(double)*ND*SS::n_adv*nq;
-    constexpr size_t smem_diff = sizeof(double)*(SS::n_sav + ND*SS::n_sav)*nq;
+    constexpr size_t smem_adv = SavAdvSmem<ND, RS>::bytes;
+    constexpr size_t smem_diff = SavDiffSmem<ND, RS>::bytes;
     static bool configured = false;
     if (!configured) {
       cudaFuncSetAttribute(k_sav_local_advection<ND, RS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_adv);
@@ -455,8 +455,12 @@ struct Runner
       k_sav_max_dt<ND, RS><<<g_pts, 256, 0, c.stream>>>(m, st, 0, t.max_cfl*p.advect_safety);
     }
     for (int iter = 0; iter < p.advect_iters; ++iter) {
-      sav_faces(0);
-      sav_refine<SS::n_adv_extrap>(c, m, t, true, false, false);
+      // compute_write_face_advection + compute_prolong_advection; after the first iteration the
+      // previous stage's volume kernel and prolongation have written these same traces
+      if (iter == 0) {
+        sav_faces(0);
+        sav_refine<SS::n_adv_extrap>(c, m, t, true, false, false);
+      }
       for (int stage = 0; stage < 2; ++stage) {
         if (m.n_bc_con) k_sav_bc_advection<ND, RS><<<g_bc, 256, 0, c.stream>>>(m);
         if (n_face_pts) {
@@ -466,10 +470,10 @@ struct Runner
         sav_refine<SS::n_adv_extrap>(c, m, t, false, true, false);
         {
           ProfScope ps(c, "sav_local_advection");
+          // Local with its Write_face of the new advection traces
           k_sav_local_advection<ND, RS><<<n_elem, blk, smem_adv, c.stream>>>(m, st, stage, p.advect_length,
                                                                             t.step_ratio);
         }
-        sav_faces(0);
         sav_refine<SS::n_adv_extrap>(c, m, t, true, false, false);
       }
     }

@@ -87,25 +87,6 @@ inline SavTab<RS> make_savtab(const Tab<RS>& t)
   return s;
 }
 
-// Derivative::operator() for output node i of a row x with face values fb (Derivative.hpp:50-55):
-// sum_j diff[i][j] x_j + (lift[i][0] (fb0 - B0.x) + lift[i][1] (fb1 - B1.x)).
-template <int RS>
-__device__ __forceinline__ double row_derivative(const SavTab<RS>& t, const double (&x)[RS], double fb0, double fb1,
-                                                 int i)
-{
-  double b0 = 0., b1 = 0.;
-  #pragma unroll
-  for (int j = 0; j < RS; ++j) { b0 += t.bound[j]*x[j]; b1 += t.bound[RS + j]*x[j]; }
-  const double bf0 = fb0 - b0, bf1 = fb1 - b1;
-  double d = 0.;
-  #pragma unroll
-  for (int j = 0; j < RS; ++j) d += t.diff[i*RS + j]*x[j];
-  double l = 0.;
-  l += t.lift[i*2]*bf0;
-  l += t.lift[i*2 + 1]*bf1;
-  return d + l;
-}
-
 // math::interp of the vertex time-step scales at a qpoint (include/math.hpp:207-218)
 template <int ND, int RS>
 __device__ __forceinline__ double sav_spacing(const SavDev& m, const SavTab<RS>& t, int e, int q)
@@ -324,18 +305,53 @@ __global__ void k_sav_neighbor_advection(SavDev m, SavTab<RS> tab)
   }
 }
 
+// Derivative::operator() for output node i of a row x whose boundary corrections
+// bf_s = fb_s - B_s.x were formed once for the whole row (Derivative.hpp:50-55):
+// sum_j diff[i][j] x_j + (lift[i][0] bf0 + lift[i][1] bf1).
+template <int RS>
+__device__ __forceinline__ double row_derivative_bf(const SavTab<RS>& t, const double (&x)[RS], double bf0,
+                                                    double bf1, int i)
+{
+  double d = 0.;
+  #pragma unroll
+  for (int j = 0; j < RS; ++j) d += t.diff[i*RS + j]*x[j];
+  double l = 0.;
+  l += t.lift[i*2]*bf0;
+  l += t.lift[i*2 + 1]*bf1;
+  return d + l;
+}
+
+// Shared memory of k_sav_local_advection, in doubles: fluxes [nd][rs][nq], the per-row boundary
+// corrections [nd][rs][nfq][2], and the rows whose traces the kernel writes ([nd + rs][nq]:
+// velocity, then the new advection state).
+template <int ND, int RS>
+struct SavAdvSmem {
+  using S = SavShape<ND, RS>;
+  static constexpr int flux = 0;
+  static constexpr int bf = ND*S::n_adv*S::nq;
+  static constexpr int rows = bf + ND*S::n_adv*S::nfq*2;
+  static constexpr size_t bytes = sizeof(double)*(size_t)(rows + S::n_adv_extrap*S::nq);
+};
+
 // Spatial<pde::Advection>::Local (include/Spatial.hpp:326-509): flux node_a (v.n_i) a_a, the
 // source 2/advect_length in the first stage, and Advection::write_update (pde.hpp:292-300):
 // pseudo = 1 + 2 tss/advect_length; the first stage sets a = (a + update)/pseudo, the second
-// adds update/pseudo. One CTA per element, one thread per quadrature point; the fluxes of the
-// element sit in shared memory [nd][rs][nq].
+// adds update/pseudo; then Write_face of the velocity and the new advection state
+// (Spatial.hpp:507, pde::Advection::fetch_extrap). One CTA per element, one thread per
+// quadrature point. The boundary corrections fb - B.f of each row are formed once per row (a
+// task per row), not once per point: the kernel is bound by the FP64 pipe, and they were most
+// of its work.
 template <int ND, int RS>
 __global__ void __launch_bounds__(SavShape<ND, RS>::block)
 k_sav_local_advection(SavDev m, SavTab<RS> tab, int stage, double advect_length, double step_ratio)
 {
   using S = SavShape<ND, RS>;
-  constexpr int nq = S::nq, nfq = S::nfq, n_adv = S::n_adv;
-  extern __shared__ double s_flux[];   // [ND][n_adv][nq]
+  using L = SavAdvSmem<ND, RS>;
+  constexpr int nq = S::nq, nfq = S::nfq, n_adv = S::n_adv, n_ex = S::n_adv_extrap;
+  extern __shared__ double s_mem[];
+  double* s_flux = s_mem + L::flux;   // [ND][n_adv][nq]
+  double* s_bf = s_mem + L::bf;       // [ND][n_adv][nfq][2]
+  double* s_rows = s_mem + L::rows;   // [n_ex][nq]
   const int e = blockIdx.x;
   const int q = threadIdx.x;
   const bool deformed = e >= m.n_car;
@@ -344,57 +360,94 @@ k_sav_local_advection(SavDev m, SavTab<RS> tab, int stage, double advect_length,
   double* rcache = S::adv_cache(m, e);
   const double* nrml = deformed ? m.jac + (size_t)(e - m.n_car)*(ND*ND + 1)*nq : nullptr;
   const double d_pos = m.nom_size[e];
+  double a_old[n_adv];
   if (q < nq) {
+    double vel[ND];
+    #pragma unroll
+    for (int j = 0; j < ND; ++j) { vel[j] = st[j*nq + q]; s_rows[j*nq + q] = vel[j]; }
+    #pragma unroll
+    for (int a = 0; a < n_adv; ++a) a_old[a] = a_st[a*nq + q];
     #pragma unroll
     for (int i = 0; i < ND; ++i) {
       double nrml_veloc = 0;
       #pragma unroll
-      for (int j = 0; j < ND; ++j) nrml_veloc += st[j*nq + q]*(deformed ? nrml[(i*ND + j)*nq + q] : (i == j ? 1. : 0.));
-      for (int a = 0; a < n_adv; ++a) s_flux[(i*n_adv + a)*nq + q] = tab.adv_node[a]*nrml_veloc*a_st[a*nq + q];
+      for (int j = 0; j < ND; ++j) nrml_veloc += vel[j]*(deformed ? nrml[(i*ND + j)*nq + q] : (i == j ? 1. : 0.));
+      #pragma unroll
+      for (int a = 0; a < n_adv; ++a) s_flux[(i*n_adv + a)*nq + q] = tab.adv_node[a]*nrml_veloc*a_old[a];
     }
   }
   __syncthreads();
-  if (q >= nq) return;
-  double rate[n_adv];
-  #pragma unroll
-  for (int a = 0; a < n_adv; ++a) rate[a] = 0.;
-  #pragma unroll
-  for (int d = 0; d < ND; ++d) {
-    const int stride = ipow(RS, ND - 1 - d);
-    const int i = (q/stride)%RS;
-    const int i_fq = (q/(stride*RS))*stride + q%stride;
-    const double* fa = S::slot(m, e*2*ND + 2*d, false);
-    const double* fb = S::slot(m, e*2*ND + 2*d + 1, false);
+  // boundary corrections of every row: fb_s - B_s.f with the face fluxes of Neighbor
+  for (int t = threadIdx.x; t < ND*n_adv*nfq; t += blockDim.x) {
+    const int i_fq = t%nfq, a = (t/nfq)%n_adv, d = t/(nfq*n_adv);
+    double x[RS];
+    #pragma unroll
+    for (int k = 0; k < RS; ++k) x[k] = s_flux[(d*n_adv + a)*nq + S::row_qpoint(d, i_fq, k)];
+    double b0 = 0., b1 = 0.;
+    #pragma unroll
+    for (int j = 0; j < RS; ++j) { b0 += tab.bound[j]*x[j]; b1 += tab.bound[RS + j]*x[j]; }
+    s_bf[2*t] = S::slot(m, e*2*ND + 2*d, false)[a*nfq + i_fq] - b0;
+    s_bf[2*t + 1] = S::slot(m, e*2*ND + 2*d + 1, false)[a*nfq + i_fq] - b1;
+  }
+  __syncthreads();
+  if (q < nq) {
+    double rate[n_adv];
+    #pragma unroll
+    for (int a = 0; a < n_adv; ++a) rate[a] = 0.;
+    #pragma unroll
+    for (int d = 0; d < ND; ++d) {
+      const int stride = ipow(RS, ND - 1 - d);
+      const int i = (q/stride)%RS;
+      const int i_fq = (q/(stride*RS))*stride + q%stride;
+      #pragma unroll
+      for (int a = 0; a < n_adv; ++a) {
+        double x[RS];
+        #pragma unroll
+        for (int k = 0; k < RS; ++k) x[k] = s_flux[(d*n_adv + a)*nq + q - i*stride + k*stride];
+        const int r = (d*n_adv + a)*nfq + i_fq;
+        const double der = row_derivative_bf<RS>(tab, x, s_bf[2*r], s_bf[2*r + 1], i);
+        rate[a] = 1.*rate[a] + -der;
+      }
+    }
+    const double tss = st[S::nv*nq + q];
+    const double det = deformed ? nrml[ND*ND*nq + q] : 1.;
+    const double update_coef = stage ? 1.*step_ratio : 1.;
+    double mult = update_coef*tss/d_pos;
+    if (deformed) mult /= det;
+    const double pseudo = 1 + tss*2/advect_length;
+    double src_mult = d_pos;
+    if (deformed) src_mult *= det;
+    const double source = src_mult*(2/advect_length);
     #pragma unroll
     for (int a = 0; a < n_adv; ++a) {
-      double x[RS];
-      #pragma unroll
-      for (int k = 0; k < RS; ++k) x[k] = s_flux[(d*n_adv + a)*nq + q - i*stride + k*stride];
-      const double der = row_derivative<RS>(tab, x, fa[a*nfq + i_fq], fb[a*nfq + i_fq], i);
-      rate[a] = 1.*rate[a] + -der;
+      double u = rate[a];
+      if (stage) {
+        u -= rcache[a*nq + q];
+      } else {
+        rcache[a*nq + q] = u;
+        u += source;
+      }
+      u *= mult;
+      const double x = a_old[a];
+      const double nx = stage ? x + u/pseudo : (x + u)/pseudo;
+      a_st[a*nq + q] = nx;
+      s_rows[(ND + a)*nq + q] = nx;
     }
   }
-  const double tss = st[S::nv*nq + q];
-  const double det = deformed ? nrml[ND*ND*nq + q] : 1.;
-  const double update_coef = stage ? 1.*step_ratio : 1.;
-  double mult = update_coef*tss/d_pos;
-  if (deformed) mult /= det;
-  const double pseudo = 1 + tss*2/advect_length;
-  double src_mult = d_pos;
-  if (deformed) src_mult *= det;
-  const double source = src_mult*(2/advect_length);
-  #pragma unroll
-  for (int a = 0; a < n_adv; ++a) {
-    double u = rate[a];
-    if (stage) {
-      u -= rcache[a*nq + q];
-    } else {
-      rcache[a*nq + q] = u;
-      u += source;
+  __syncthreads();
+  // Write_face of the velocity and the new advection state (both faces of each row)
+  for (int t = threadIdx.x; t < ND*n_ex*nfq; t += blockDim.x) {
+    const int i_fq = t%nfq, v = (t/nfq)%n_ex, d = t/(nfq*n_ex);
+    double x[RS];
+    #pragma unroll
+    for (int k = 0; k < RS; ++k) x[k] = s_rows[v*nq + S::row_qpoint(d, i_fq, k)];
+    #pragma unroll
+    for (int s2 = 0; s2 < 2; ++s2) {
+      double acc = 0.;
+      #pragma unroll
+      for (int k = 0; k < RS; ++k) acc += tab.bound[s2*RS + k]*x[k];
+      S::slot(m, e*2*ND + 2*d + s2, false)[v*nfq + i_fq] = acc;
     }
-    u *= mult;
-    const double x = a_st[a*nq + q];
-    a_st[a*nq + q] = stage ? x + u/pseudo : (x + u)/pseudo;
   }
 }
 
@@ -478,22 +531,36 @@ __global__ void k_sav_neighbor_ldg(SavDev m, int reconcile)
   }
 }
 
+// Shared memory of k_sav_local_diffusion, in doubles: the three unknowns [3][nq], the fluxes
+// [nd][3][nq], and the gradient rows' boundary corrections [nd][nd][3][nfq][2].
+template <int ND, int RS>
+struct SavDiffSmem {
+  using S = SavShape<ND, RS>;
+  static constexpr int rows = 0;
+  static constexpr int flux = S::n_sav*S::nq;
+  static constexpr int bf = flux + ND*S::n_sav*S::nq;
+  static constexpr size_t bytes = sizeof(double)*(size_t)(bf + ND*ND*S::n_sav*S::nfq*2);
+};
+
 // Spatial<pde::Smooth_art_visc>::Local, first stage (include/Spatial.hpp:326-509): the
 // unknowns are forcing rows 1-3, their gradient (times the Jacobian determinant, product rule
 // with the metric on deformed elements, Spatial.hpp:371-402) gives the flux -gradient.normal
 // (diffusivity 1); the source of unknown v is f(forcing row v)/diff_time with f = |x| for rows
 // 0 and 2 and sqrt|x| for row 1 (pde.hpp:422-429); the flux's face values go to the LDG faces
 // and write_update adds (pde.hpp:379-387). One CTA per element, one thread per quadrature
-// point; shared memory holds the three rows and then the fluxes [nd][3][nq].
+// point. The gradient rows' boundary corrections are formed once per row (a task per row), as
+// in k_sav_local_advection.
 template <int ND, int RS>
 __global__ void __launch_bounds__(SavShape<ND, RS>::block)
 k_sav_local_diffusion(SavDev m, SavTab<RS> tab, double dt, double diff_time)
 {
   using S = SavShape<ND, RS>;
+  using L = SavDiffSmem<ND, RS>;
   constexpr int nq = S::nq, nfq = S::nfq, n_sav = S::n_sav;
   extern __shared__ double s_mem[];
-  double* s_r = s_mem;                   // [3][nq]
-  double* s_f = s_mem + n_sav*nq;        // [ND][3][nq]
+  double* s_r = s_mem + L::rows;   // [3][nq]
+  double* s_f = s_mem + L::flux;   // [ND][3][nq]
+  double* s_bf = s_mem + L::bf;    // [ND (d)][ND (j)][3][nfq][2]
   const int e = blockIdx.x;
   const int q = threadIdx.x;
   const bool deformed = e >= m.n_car;
@@ -505,6 +572,38 @@ k_sav_local_diffusion(SavDev m, SavTab<RS> tab, double dt, double diff_time)
   if (q < nq) {
     #pragma unroll
     for (int v = 0; v < n_sav; ++v) s_r[v*nq + q] = fc[(1 + v)*nq + q];
+  }
+  __syncthreads();
+  // boundary corrections of every gradient row, once per row: fb_s - B_s.x with x the row of
+  // the unknown (times the metric normal n_dj on deformed elements) and fb_s its LDG face
+  // value (times the face normal)
+  const int n_j = deformed ? ND : 1;
+  for (int t = threadIdx.x; t < ND*n_j*n_sav*nfq; t += blockDim.x) {
+    const int i_fq = t%nfq, v = (t/nfq)%n_sav, j = (t/(nfq*n_sav))%n_j, d = t/(nfq*n_sav*n_j);
+    const double* la = S::slot(m, e*2*ND + 2*d, true);
+    const double* lb = S::slot(m, e*2*ND + 2*d + 1, true);
+    double x[RS];
+    double fb0 = la[v*nfq + i_fq], fb1 = lb[v*nfq + i_fq];
+    if (deformed) {
+      const double* fna = m.face_nrml + ((size_t)ed*2*ND + 2*d)*ND*nfq;
+      const double* fnb = fna + ND*nfq;
+      #pragma unroll
+      for (int k = 0; k < RS; ++k) {
+        const int qk = S::row_qpoint(d, i_fq, k);
+        x[k] = nrml[(d*ND + j)*nq + qk]*s_r[v*nq + qk];
+      }
+      fb0 = fna[j*nfq + i_fq]*fb0;
+      fb1 = fnb[j*nfq + i_fq]*fb1;
+    } else {
+      #pragma unroll
+      for (int k = 0; k < RS; ++k) x[k] = s_r[v*nq + S::row_qpoint(d, i_fq, k)];
+    }
+    double b0 = 0., b1 = 0.;
+    #pragma unroll
+    for (int k = 0; k < RS; ++k) { b0 += tab.bound[k]*x[k]; b1 += tab.bound[RS + k]*x[k]; }
+    const int r = ((d*ND + j)*n_sav + v)*nfq + i_fq;
+    s_bf[2*r] = fb0 - b0;
+    s_bf[2*r + 1] = fb1 - b1;
   }
   __syncthreads();
   if (q < nq) {
@@ -519,11 +618,7 @@ k_sav_local_diffusion(SavDev m, SavTab<RS> tab, double dt, double diff_time)
       const int i = (q/stride)%RS;
       const int i_fq = (q/(stride*RS))*stride + q%stride;
       const int r0 = q - i*stride;
-      const double* la = S::slot(m, e*2*ND + 2*d, true);
-      const double* lb = S::slot(m, e*2*ND + 2*d + 1, true);
       if (deformed) {
-        const double* fna = m.face_nrml + ((size_t)ed*2*ND + 2*d)*ND*nfq;
-        const double* fnb = fna + ND*nfq;
         #pragma unroll
         for (int j = 0; j < ND; ++j) {
           double row_n[RS];
@@ -534,8 +629,8 @@ k_sav_local_diffusion(SavDev m, SavTab<RS> tab, double dt, double diff_time)
             double x[RS];
             #pragma unroll
             for (int k = 0; k < RS; ++k) x[k] = row_n[k]*s_r[v*nq + r0 + k*stride];
-            const double der = row_derivative<RS>(tab, x, fna[j*nfq + i_fq]*la[v*nfq + i_fq],
-                                                  fnb[j*nfq + i_fq]*lb[v*nfq + i_fq], i);
+            const int r = ((d*ND + j)*n_sav + v)*nfq + i_fq;
+            const double der = row_derivative_bf<RS>(tab, x, s_bf[2*r], s_bf[2*r + 1], i);
             g[v][j] = 1.*g[v][j] + der/d_pos;
           }
         }
@@ -545,7 +640,8 @@ k_sav_local_diffusion(SavDev m, SavTab<RS> tab, double dt, double diff_time)
           double x[RS];
           #pragma unroll
           for (int k = 0; k < RS; ++k) x[k] = s_r[v*nq + r0 + k*stride];
-          const double der = row_derivative<RS>(tab, x, la[v*nfq + i_fq], lb[v*nfq + i_fq], i);
+          const int r = (d*n_sav + v)*nfq + i_fq;
+          const double der = row_derivative_bf<RS>(tab, x, s_bf[2*r], s_bf[2*r + 1], i);
           g[v][d] = 0*g[v][d] + der/d_pos;
         }
       }
