@@ -640,7 +640,7 @@ k_sav_local_diffusion(SavDev m, SavTab<RS> tab, double dt, double diff_time)
           double x[RS];
           #pragma unroll
           for (int k = 0; k < RS; ++k) x[k] = s_r[v*nq + r0 + k*stride];
-          const int r = (d*n_sav + v)*nfq + i_fq;
+          const int r = ((d*ND)*n_sav + v)*nfq + i_fq;   // the task layout with j = 0
           const double der = row_derivative_bf<RS>(tab, x, s_bf[2*r], s_bf[2*r + 1], i);
           g[v][d] = 0*g[v][d] + der/d_pos;
         }
