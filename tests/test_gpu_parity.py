@@ -277,3 +277,30 @@ def test_write_and_read_state(precision):
         assert np.array_equal(full[:, :ar.nv], new)
         assert np.array_equal(full[:, ar.nv:], ar.elem[:, ar.nv:])   # time-step and AV rows untouched
         assert np.array_equal(c.read_state(), new)
+
+
+@pytest.mark.parametrize("case,rs", [("cartesian_3d", 8), ("deformed_2d", 8), ("cartesian_3d", 6), ("deformed_2d", 6)])
+def test_viscosity_known_answer(case, rs):
+    """The reference's "Solver viscosity" test (test/test_Solver.cpp:588-615) on the GPU: one
+    update and compute_residual of a divergence-free sinusoidal velocity with constant
+    viscosity 3 give the analytic momentum rate -n_dim 3 u (the reference's margin), and the
+    oracle's state and residual cache to 1e-12."""
+    from test_oracle_reference import marching_mesh, sinusoid_veloc0, viscous_rate_check
+    ar = marching_mesh(case, rs)
+    ar.set_state(sinusoid_veloc0)
+    visc = abi.transport_constant(3.)
+    p = abi.update_params(max_safety=1e-4, visc=visc, cond=abi.transport_inviscid())
+
+    def o_op(o):
+        o.write_face()
+        o.update(p)
+        o.compute_residual(p)
+
+    def g_op(c):
+        c.write_face()
+        c.update(p)
+        c.compute_residual(p)
+    a, b, _ = run_pair(ar, o_op, g_op)
+    viscous_rate_check(b, b.rcache, b.elem[:, b.nv], b.elem[:, :b.nv])
+    errs, bad = compare_arenas(a, b, FP64_TOL, what=("elem", "rcache"))
+    assert not bad, errs

@@ -360,6 +360,52 @@ def test_marching(case):  # test/test_Solver.cpp:555-586
     assert np.abs(ar.state - state0).max() > 0
 
 
+def sinusoid_veloc0(pos):  # test/test_Solver.cpp:57-75
+    """Constant density and pressure, divergence-free sinusoidal velocity."""
+    nd = pos.shape[0]
+    cos_part = np.cos(sum(pos[d] for d in range(nd)))
+    mom = [1.2 * cos_part for _ in range(nd)]
+    mom[0] = mom[0] * (1 - nd)
+    energy = 1e5 / 0.4 + .5 * 1.2 * (nd - 1 + (1 - nd) * (1 - nd)) * cos_part * cos_part
+    return np.stack(mom + [1.2 + 0 * cos_part, energy])
+
+
+def marching_mesh(case, rs=6):
+    """The meshes of the restated marching tests, with Copy boundaries."""
+    copy = bc_spec(abi.BC_COPY)
+    if case == "cartesian_3d":
+        return structured_mesh(3, rs, 2, 0., 2., bcs={(d, s): copy for d in range(3) for s in range(2)})
+    return structured_mesh(2, rs, 3, 0., 3., deformed=True, displacement=problems.sinusoid_displacement(1., .1, 3, 2),
+                           bcs={(d, s): copy for d in range(2) for s in range(2)})
+
+
+def viscous_rate_check(ar, rcache, tss, state):
+    """test/test_Solver.cpp:588-615: with constant viscosity 3 the momentum rate is
+    -n_dim 3 u (u = momentum / 1.2), to an absolute margin of 1.2 x 1e-3 when the row size is
+    above 6 and 1.2 otherwise (the reference runs the test at its build's maximum row size and
+    takes the margin from that)."""
+    nd = ar.n_dim
+    rate = rcache[:, :nd] / tss[:, None, :]
+    want = -nd * 3. * state[:, :nd] / 1.2
+    err = np.abs(rate - want).max()
+    assert err <= 1.2 * (1e-3 if ar.row_size > 6 else 1.), err
+    return err
+
+
+@pytest.mark.parametrize("case,rs", [("cartesian_3d", 8), ("deformed_2d", 8), ("cartesian_3d", 6), ("deformed_2d", 6)])
+def test_viscosity(case, rs):  # test/test_Solver.cpp:588-615
+    ar = marching_mesh(case, rs)
+    ar.set_state(sinusoid_veloc0)
+    o = oracle.Oracle(ar)
+    o.write_face()
+    visc = abi.transport_constant(3.)
+    p = abi.update_params(max_safety=1e-4, visc=visc, cond=abi.transport_inviscid())
+    dt = o.update(p)
+    assert dt > 0
+    o.compute_residual(p)
+    viscous_rate_check(ar, ar.rcache, ar.tss, ar.state)
+
+
 @pytest.mark.parametrize("nd,deformed", [(2, False), (3, False), (2, True), (3, True)])
 def test_conservation(nd, deformed):  # test/test_Solver.cpp:617-639
     rng = np.random.default_rng(406)
