@@ -279,7 +279,8 @@ def test_write_and_read_state(precision):
         assert np.array_equal(c.read_state(), new)
 
 
-@pytest.mark.parametrize("case,rs", [("cartesian_3d", 8), ("deformed_2d", 8), ("cartesian_3d", 6), ("deformed_2d", 6)])
+@pytest.mark.parametrize("case,rs", [("cartesian_3d", 8), ("deformed_2d", 8), ("tree_2d", 8), ("tree_3d", 8),
+                                     ("cartesian_3d", 6), ("deformed_2d", 6)])
 def test_viscosity_known_answer(case, rs):
     """The reference's "Solver viscosity" test (test/test_Solver.cpp:588-615) on the GPU: one
     update and compute_residual of a divergence-free sinusoidal velocity with constant
@@ -293,11 +294,13 @@ def test_viscosity_known_answer(case, rs):
 
     def o_op(o):
         o.write_face()
+        o.prolong()
         o.update(p)
         o.compute_residual(p)
 
     def g_op(c):
         c.write_face()
+        c.prolong()
         c.update(p)
         c.compute_residual(p)
     a, b, _ = run_pair(ar, o_op, g_op)

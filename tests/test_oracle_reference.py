@@ -338,17 +338,13 @@ def nonuniform_residual(pos):  # test/test_Solver.cpp:149-168
     return np.stack([d_mass * VELOCS[d] for d in range(nd)] + [d_mass, d_mass * 0.5 * vsq])
 
 
-@pytest.mark.parametrize("case", ["cartesian_3d", "deformed_2d"])
+@pytest.mark.parametrize("case", ["cartesian_3d", "deformed_2d", "tree_2d", "tree_3d"])
 def test_marching(case):  # test/test_Solver.cpp:555-586
-    copy = bc_spec(abi.BC_COPY)
-    if case == "cartesian_3d":
-        ar = structured_mesh(3, 6, 2, 0., 2., bcs={(d, s): copy for d in range(3) for s in range(2)})
-    else:
-        ar = structured_mesh(2, 6, 3, 0., 3., deformed=True, displacement=problems.sinusoid_displacement(1., .1, 3, 2),
-                             bcs={(d, s): copy for d in range(2) for s in range(2)})
+    ar = marching_mesh(case)
     ar.set_state(nonuniform_mass)
     o = oracle.Oracle(ar)
     o.write_face()
+    o.prolong()
     state0 = ar.state.copy()
     p = abi.update_params(max_safety=1e-3)
     dt = o.update(p)
@@ -371,8 +367,16 @@ def sinusoid_veloc0(pos):  # test/test_Solver.cpp:57-75
 
 
 def marching_mesh(case, rs=6):
-    """The meshes of the restated marching tests, with Copy boundaries."""
+    """The meshes of the restated marching tests, with Copy boundaries: Cartesian 3D, deformed
+    2D, and tree meshes with hanging faces (2D, 3D) standing in for the reference's extruded
+    hanging-node meshes."""
     copy = bc_spec(abi.BC_COPY)
+    if case.startswith("tree"):
+        from hexed_gb300.tree import tree_mesh
+        nd = int(case[-2])
+        ar = tree_mesh(nd, rs, 2, 2, problems.sphere_refinement(2, 0.3), {(d, s): copy for d in range(nd) for s in range(2)})
+        assert len(ar.ref_face) > 0
+        return ar
     if case == "cartesian_3d":
         return structured_mesh(3, rs, 2, 0., 2., bcs={(d, s): copy for d in range(3) for s in range(2)})
     return structured_mesh(2, rs, 3, 0., 3., deformed=True, displacement=problems.sinusoid_displacement(1., .1, 3, 2),
@@ -392,12 +396,17 @@ def viscous_rate_check(ar, rcache, tss, state):
     return err
 
 
-@pytest.mark.parametrize("case,rs", [("cartesian_3d", 8), ("deformed_2d", 8), ("cartesian_3d", 6), ("deformed_2d", 6)])
+VISCOSITY_CASES = [("cartesian_3d", 8), ("deformed_2d", 8), ("tree_2d", 8), ("tree_3d", 8), ("cartesian_3d", 6),
+                   ("deformed_2d", 6)]
+
+
+@pytest.mark.parametrize("case,rs", VISCOSITY_CASES)
 def test_viscosity(case, rs):  # test/test_Solver.cpp:588-615
     ar = marching_mesh(case, rs)
     ar.set_state(sinusoid_veloc0)
     o = oracle.Oracle(ar)
     o.write_face()
+    o.prolong()
     visc = abi.transport_constant(3.)
     p = abi.update_params(max_safety=1e-4, visc=visc, cond=abi.transport_inviscid())
     dt = o.update(p)
