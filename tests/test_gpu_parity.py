@@ -6,7 +6,7 @@ import pytest
 from hexed_gb300 import abi, problems
 from hexed_gb300.solver import Context
 import oracle
-from helpers import FP64_TOL, air_transport, cartesian_case, compare_arenas, deformed_case
+from helpers import FP64_TOL, air_transport, cartesian_case, compare_arenas, deformed_case, per_variable_rel
 
 pytestmark = pytest.mark.gpu
 
@@ -285,7 +285,18 @@ def test_viscosity_known_answer(case, rs):
     """The reference's "Solver viscosity" test (test/test_Solver.cpp:588-615) on the GPU: one
     update and compute_residual of a divergence-free sinusoidal velocity with constant
     viscosity 3 give the analytic momentum rate -n_dim 3 u (the reference's margin), and the
-    oracle's state and residual cache to 1e-12."""
+    oracle's state to 1e-12 and its residual cache to within the residual's own conditioning.
+
+    The residual here is the small remainder of large fluxes: the test's pressure is 1e5 and
+    its energy 2.5e5, against a momentum rate of 18 and an energy rate of 54, and the density
+    rate -div(rho u) is zero up to the interpolation error of the sinusoid (2.7e-7 at row
+    size 8). Rounding in the flux terms therefore moves the residual by far more than 1e-12 of
+    its own size: re-running the oracle on its input with every conserved value moved by
+    about one ulp moves the momentum rate by ~3e-10 and the energy rate by ~8e-8 of their
+    magnitudes. That response is measured in the test, and the GPU's residual cache must lie
+    within four times it (and within 1e-12 where the response is smaller). Momentum
+    components and the density rate are measured against the momentum rate's scale, energy
+    against its own; the message also gives each variable against its own magnitude."""
     from test_oracle_reference import marching_mesh, sinusoid_veloc0, viscous_rate_check
     ar = marching_mesh(case, rs)
     ar.set_state(sinusoid_veloc0)
@@ -305,5 +316,23 @@ def test_viscosity_known_answer(case, rs):
         c.compute_residual(p)
     a, b, _ = run_pair(ar, o_op, g_op)
     viscous_rate_check(b, b.rcache, b.elem[:, b.nv], b.elem[:, :b.nv])
-    errs, bad = compare_arenas(a, b, FP64_TOL, what=("elem", "rcache"))
+    errs, bad = compare_arenas(a, b, FP64_TOL, what=("elem",))
+    nv = ar.nv
+
+    def rcache_rel(x, y):
+        out = per_variable_rel(x, y, nv=nv)
+        out[nv - 2] = float(np.abs(x[:, nv - 2] - y[:, nv - 2]).max()) / float(np.abs(y[:, :nv - 2]).max())
+        return out
+    # the oracle's own response to a one-ulp change of its input
+    c = ar.copy()
+    rng = np.random.default_rng(0)
+    c.elem[:, :nv] *= 1 + np.finfo(float).eps * rng.choice([-1., 1.], size=c.elem[:, :nv].shape)
+    o_op(oracle.Oracle(c))
+    response = rcache_rel(c.rcache, a.rcache)
+    rc = rcache_rel(b.rcache, a.rcache)
+    bars = [max(FP64_TOL, 4 * r) for r in response]
+    errs.update(rcache_per_variable=rc, oracle_ulp_response=response,
+                rcache_per_variable_own=per_variable_rel(b.rcache, a.rcache))
+    if any(e > bar for e, bar in zip(rc, bars)):
+        bad["rcache"] = rc
     assert not bad, errs
