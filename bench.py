@@ -126,7 +126,7 @@ def kernel_bytes(name, ar, precision="fp64"):
         "local_def_ns": d * (2 * nv + 3) * nq + w * nv * nq + w * 3 * F * nv * nfq + metric + w * F * nd * nfq,
         "reconcile_ldg_car": d * (2 * nv + 1) * nq + w * 2 * F * nv * nfq,
         "reconcile_ldg_def": d * (2 * nv + 2) * nq + w * 2 * F * nv * nfq,
-        "max_dt": d * (nv + 3) * nq + d * 2 ** nd,
+        "max_dt": d * (nv + 3) * nq + w * 2 ** nd,   # the mixed form reads float vertex scales
     }
     if name in per_elem:
         n = ar.n_def if "def" in name else ar.n_car if "car" in name else ar.n_elem

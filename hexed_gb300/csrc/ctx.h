@@ -98,6 +98,7 @@ struct Ctx {
   // state of each element [n_elem][nv] the traces and fluxes are offsets from (by default the
   // mean conserved state of the initial state)
   float* face_f; float* rcache_f; float* nrm_f; float* face_nrml_f; float* def_con_nrml_f; float* bc_nrml_f;
+  float* vert_tss_f;     // FP32 vertex time-step scales [n_elem][2^nd] (Max_dt)
   double* ref_state;
   // its terms in float for the offset fluxes (RefState: state and its rounding error, velocity,
   // |v|^2, enthalpy, 1/density), [n_elem][3 nd + 7], refreshed whenever ref_state changes

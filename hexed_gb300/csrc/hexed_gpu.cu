@@ -237,6 +237,7 @@ int refresh_metric_copies(Ctx* c, int which, long offset, long count)
   };
   if (which == HEXED_ARRAY_BC_NRML) narrow(c->bc_nrml, c->bc_nrml_f);
   if (which == HEXED_ARRAY_FACE_NRML) narrow(c->face_nrml, c->face_nrml_f);
+  if (which == HEXED_ARRAY_VERT_TSS) narrow(c->vert_tss, c->vert_tss_f);
   if (which == HEXED_ARRAY_DEF_CON_NRML) narrow(c->def_con_nrml, c->def_con_nrml_f);
   if (which == HEXED_ARRAY_REF_STATE) c->ops->ref_terms(*c);
   if (which == HEXED_ARRAY_JAC) {
@@ -445,6 +446,7 @@ int hexed_gpu_create(const hexed_mesh_desc* d, int precision, hexed_gpu_ctx** ou
     if (!st) st = narrow_copy(c, c->face_nrml, &c->face_nrml_f, (long)c->n_def*2*nd*nd*c->nfq);
     if (!st) st = narrow_copy(c, c->def_con_nrml, &c->def_con_nrml_f, (long)c->n_def_con*nd*c->nfq);
     if (!st) st = narrow_copy(c, c->bc_nrml, &c->bc_nrml_f, (long)c->n_bc_con*nd*c->nfq);
+    if (!st) st = narrow_copy(c, c->vert_tss, &c->vert_tss_f, (long)n_elem*nvert);
     // reference state of every element: the mean of its own initial state over its quadrature
     // points (zero without one; hexed_gpu_set_reference_state or HEXED_ARRAY_REF_STATE set it
     // then), so that the FP32 offsets carry only the variation inside the element
@@ -514,7 +516,7 @@ int hexed_gpu_destroy(hexed_gpu_ctx* c)
                   c->def_con, c->def_con_nrml, c->bc_con, c->bc_nrml, c->bc_cache, c->ref_face, c->bc_spec,
                   c->scalars, c->partials, c->status, c->dt_ticket, c->d_norm, c->vert_id, c->uncert, c->vmax,
                   c->seg_table, c->seg_out, c->inv_det, c->face_f, c->rcache_f, c->nrm_f, c->face_nrml_f,
-                  c->def_con_nrml_f, c->bc_nrml_f, c->ref_state, c->ref_terms, c->record, c->slot_elem,
+                  c->def_con_nrml_f, c->bc_nrml_f, c->vert_tss_f, c->ref_state, c->ref_terms, c->record, c->slot_elem,
                   c->sav_aux, c->sav_face, c->sav_partials};
   for (void* p : ptrs) if (p) cudaFree(p);
   if (c->graph) {
@@ -637,6 +639,7 @@ int hexed_gpu_compute_jacobian(hexed_gpu_ctx* c, const double* vert_pos)
   if (!st) st = refresh_metric_copies(c, HEXED_ARRAY_FACE_NRML, 0, n_fnr);
   if (!st) st = refresh_metric_copies(c, HEXED_ARRAY_DEF_CON_NRML, 0, n_con);
   if (!st) st = refresh_metric_copies(c, HEXED_ARRAY_BC_NRML, 0, n_bc);
+  if (!st) st = refresh_metric_copies(c, HEXED_ARRAY_VERT_TSS, 0, (long)array_count(c, HEXED_ARRAY_VERT_TSS));
   err = cudaStreamSynchronize(c->stream);
   if (scratch) cudaFree(scratch);
   if (!st && err != cudaSuccess) st = fail(HEXED_ERR_CUDA, "metric set-up: %s", cudaGetErrorString(err));

@@ -54,6 +54,7 @@ struct Dev {
   FaceT* face;
   const double* nom_size;
   const double* vert_tss;
+  const float* vert_tss_f;    // mixed form: the same in float (Max_dt's point scales); null in FP64
   const double* jac;          // FP64 [n_def][nd*nd + 1][nq]
   const double* inv_det;      // FP64 [n_def][nq], 1/det
   const FaceT* nrm;           // [n_def][nd*nd + 1][nq], reference-level normals in FaceT
@@ -115,27 +116,31 @@ template <typename T> __device__ __forceinline__ T load(const T* p) { return __l
 __device__ __forceinline__ float f32_of(double x)
 {
   const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
-  const unsigned sign = hi & 0x80000000u;
-  const unsigned ex = (hi >> 20) & 0x7ffu;
-  const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);   // leading 23 mantissa bits
-  const unsigned rest = lo & 0x1fffffffu;                    // the 29 bits rounded away
-  const int e = int(ex) - (1023 - 127);                      // biased float exponent
-  unsigned bits = (unsigned(e) << 23) + m;
-  bits += (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ? 1u : 0u;  // a carry may
-  bits = e >= 255 ? 0x7f800000u : bits;                      // reach the exponent (inf)
-  bits = (ex == 0x7ffu && (m | rest)) ? 0x7fc00000u : bits;
-  bits = e <= 0 ? 0u : bits;
-  return __uint_as_float(sign | bits);
+  const unsigned a = hi & 0x7fffffffu;   // high word of |x|
+  // |x| as float bits with the mantissa cut to 23 bits: the exponent rebiased from 1023 to 127
+  // (minus 896 << 20) and the 64-bit pattern shifted left by 3, keeping its high word
+  unsigned t = __funnelshift_l(lo, a - 0x38000000u, 3);
+  // round to nearest even on the 29 bits cut away: carry out of rest + (half - 1) + lsb; a
+  // carry may reach the exponent (up to inf, as rounding should)
+  t += ((lo & 0x1fffffffu) + 0x0fffffffu + (t & 1u)) >> 29;
+  // outside the float normal range, 2^-126 <= |x| < 2^128 (one unsigned compare; rare)
+  if (a - 0x38100000u >= 0x47f00000u - 0x38100000u)
+    t = a < 0x38100000u ? 0u : (a > 0x7ff00000u || (a == 0x7ff00000u && lo)) ? 0x7fc00000u : 0x7f800000u;
+  return __uint_as_float((hi & 0x80000000u) | t);
 }
 
 __device__ __forceinline__ double f64_of(float f)
 {
   const unsigned b = __float_as_uint(f);
-  const unsigned sign = b & 0x80000000u, ex = (b >> 23) & 0xffu, m = b & 0x7fffffu;
-  unsigned hi = sign | ((ex + (1023u - 127u)) << 20) | (m >> 3);
-  unsigned lo = m << 29;
-  if (ex == 0u) { hi = sign; lo = 0u; }
-  if (ex == 0xffu) hi = sign | 0x7ff00000u | (m >> 3) | (m ? 0x80000u : 0u);
+  const unsigned sign = b & 0x80000000u, a = b & 0x7fffffffu;
+  // a normal float: exponent and mantissa move together (right by 3), the exponent rebiased
+  unsigned hi = sign | ((a >> 3) + 0x38000000u);
+  unsigned lo = b << 29;
+  if (a - 0x00800000u >= 0x7f800000u - 0x00800000u) {   // zero, subnormal, inf or NaN (rare)
+    const unsigned m = b & 0x7fffffu;
+    hi = a < 0x00800000u ? sign : sign | 0x7ff00000u | (m >> 3) | (m ? 0x80000u : 0u);
+    lo = a < 0x00800000u ? 0u : lo;
+  }
   return __hiloint2double((int)hi, (int)lo);
 }
 
@@ -699,7 +704,10 @@ __device__ __forceinline__ R point_step(const Dev<FaceT>& m, int e, int q, const
   const double* state = m.elem + (size_t)e*(nv + 3)*nq;
   R vals[nvert];
   #pragma unroll
-  for (int i = 0; i < nvert; ++i) vals[i] = to_R<R>(m.vert_tss[(size_t)e*nvert + i]);
+  for (int i = 0; i < nvert; ++i) {
+    if constexpr (std::is_same<R, double>::value) vals[i] = m.vert_tss[(size_t)e*nvert + i];
+    else vals[i] = m.vert_tss_f[(size_t)e*nvert + i];   // converted once per vertex, not per point
+  }
   int stride = nvert;
   #pragma unroll
   for (int d = 0; d < ND; ++d) {

@@ -32,7 +32,8 @@ struct Runner
     m.n_car = c.n_car; m.n_def = c.n_def; m.n_elem = c.n_car + c.n_def; m.n_slot = c.n_slot;
     m.n_car_con = c.n_car_con; m.n_def_con = c.n_def_con; m.n_bc_con = c.n_bc_con; m.n_ref = c.n_ref;
     m.elem = c.elem;
-    m.nom_size = c.nom_size; m.vert_tss = c.vert_tss; m.jac = c.jac; m.inv_det = c.inv_det;
+    m.nom_size = c.nom_size; m.vert_tss = c.vert_tss; m.vert_tss_f = c.vert_tss_f; m.jac = c.jac;
+    m.inv_det = c.inv_det;
     m.car_con = c.car_con; m.def_con = c.def_con;
     m.bc_con = c.bc_con; m.bc_nrml = c.bc_nrml; m.bc_cache = c.bc_cache; m.ref_face = c.ref_face;
     m.bc_spec = c.bc_spec; m.scalars = c.scalars; m.partials = c.partials; m.status = c.status;
@@ -109,9 +110,11 @@ struct Runner
     const int blocks = (e_end - e_begin + EPB - 1)/EPB;
     constexpr size_t smem = LocalSmem<ND, RS, R, DEF, VISC, EPB>::bytes;
     // 3D kernels of row size >= 6 are register-capped for more resident CTAs: 72 registers
-    // per thread in float (4 CTAs per SM at row size 6), 128 for the FP64 viscous kernel (2)
+    // per thread for the float viscous kernel and 56 for the float inviscid one (4 and 5 CTAs
+    // per SM at row size 6, where shared memory allows as many), 128 for the FP64 viscous
+    // kernel (2)
     constexpr int threads = Tile<ND, RS, EPB>::threads;
-    constexpr int cap = std::is_same<R, float>::value ? 72 : VISC ? 128 : 0;
+    constexpr int cap = std::is_same<R, float>::value ? (VISC ? 72 : 56) : VISC ? 128 : 0;
     constexpr int minb = (cap && ND == 3 && S::nq > 128 && 65536/(threads*cap) > 1) ? 65536/(threads*cap) : 1;
     auto kern = k_local<ND, RS, R, DEF, VISC, FaceT, EPB, minb>;
     static bool configured = false;
@@ -310,8 +313,12 @@ struct Runner
   static void max_dt(Ctx& c, double msc, double msd, int local_time, int viscous, const hexed_transport& visc,
                      const hexed_transport& cond, double max_time_step, double cheby)
   {
+    // At most 16 CTAs per SM, each looping over its points: on the 32^3 row-size-6 mesh
+    // (7.1 M points) this took the float kernel from 0.205 to 0.168 ms and the double one from
+    // 1.49 to 1.42 ms against one CTA per 256 points (19,456 CTAs taking the ticket, and the
+    // last one reading as many partials). Caps of 4 to 32 CTAs per SM measured within 4%.
     const long total = (long)(c.n_car + c.n_def)*S::nq;
-    const int grid = grid_for(total, 256, c.max_partials);
+    const int grid = grid_for(total, 256, std::min(152*16, c.max_partials));
     {
       ProfScope ps(c, "max_dt");
       const R icc = R(inv_cfl_conv(c, msc)), icd = R(inv_cfl_diff(c, msd));

@@ -532,7 +532,9 @@ __global__ void k_sav_neighbor_ldg(SavDev m, int reconcile)
 }
 
 // Shared memory of k_sav_local_diffusion, in doubles: the three unknowns [3][nq], the fluxes
-// [nd][3][nq], and the gradient rows' boundary corrections [nd][nd][3][nfq][2].
+// [nd][3][nq] (which first hold, one dimension d at a time, the metric products n_dj u_v
+// [nd (j)][3][nq] of the deformed gradient), and the gradient rows' boundary corrections
+// [nd][nd][3][nfq][2].
 template <int ND, int RS>
 struct SavDiffSmem {
   using S = SavShape<ND, RS>;
@@ -542,14 +544,49 @@ struct SavDiffSmem {
   static constexpr size_t bytes = sizeof(double)*(size_t)(bf + ND*ND*S::n_sav*S::nfq*2);
 };
 
+// Boundary corrections of the gradient rows of dimension d, one task per (j, unknown, row):
+// fb_s - B_s.x with x the row of the unknown (times the metric normal n_dj on deformed
+// elements: rows of s_x, [j][3][nq]) and fb_s its LDG face value (times the face normal).
+template <int ND, int RS>
+__device__ __forceinline__ void sav_diff_row_corrections(const SavDev& m, const SavTab<RS>& tab, int e, int d,
+                                                         bool deformed, const double* s_x, double* s_bf)
+{
+  using S = SavShape<ND, RS>;
+  constexpr int nfq = S::nfq, n_sav = S::n_sav, nq = S::nq;
+  const int n_j = deformed ? ND : 1;
+  const double* la = S::slot(m, e*2*ND + 2*d, true);
+  const double* lb = S::slot(m, e*2*ND + 2*d + 1, true);
+  for (int t = threadIdx.x; t < n_j*n_sav*nfq; t += blockDim.x) {
+    const int i_fq = t%nfq, v = (t/nfq)%n_sav, j = t/(nfq*n_sav);
+    double x[RS];
+    #pragma unroll
+    for (int k = 0; k < RS; ++k) x[k] = s_x[(j*n_sav + v)*nq + S::row_qpoint(d, i_fq, k)];
+    double fb0 = la[v*nfq + i_fq], fb1 = lb[v*nfq + i_fq];
+    if (deformed) {
+      const double* fna = m.face_nrml + ((size_t)(e - m.n_car)*2*ND + 2*d)*ND*nfq;
+      fb0 = fna[j*nfq + i_fq]*fb0;
+      fb1 = fna[ND*nfq + j*nfq + i_fq]*fb1;
+    }
+    double b0 = 0., b1 = 0.;
+    #pragma unroll
+    for (int k = 0; k < RS; ++k) { b0 += tab.bound[k]*x[k]; b1 += tab.bound[RS + k]*x[k]; }
+    const int r = ((d*ND + j)*n_sav + v)*nfq + i_fq;
+    s_bf[2*r] = fb0 - b0;
+    s_bf[2*r + 1] = fb1 - b1;
+  }
+}
+
 // Spatial<pde::Smooth_art_visc>::Local, first stage (include/Spatial.hpp:326-509): the
 // unknowns are forcing rows 1-3, their gradient (times the Jacobian determinant, product rule
 // with the metric on deformed elements, Spatial.hpp:371-402) gives the flux -gradient.normal
 // (diffusivity 1); the source of unknown v is f(forcing row v)/diff_time with f = |x| for rows
 // 0 and 2 and sqrt|x| for row 1 (pde.hpp:422-429); the flux's face values go to the LDG faces
 // and write_update adds (pde.hpp:379-387). One CTA per element, one thread per quadrature
-// point. The gradient rows' boundary corrections are formed once per row (a task per row), as
-// in k_sav_local_advection.
+// point. On deformed elements each point forms its metric products n_dj u_v once per
+// dimension into shared memory, where the row tasks (boundary corrections) and the points'
+// derivatives read them. Divisions by the element size and the Jacobian determinant are
+// multiplications by reciprocals formed once: an ulp per operation from the reference's
+// divisions, of which there were 36 per point, each costing about ten FP64 operations.
 template <int ND, int RS>
 __global__ void __launch_bounds__(SavShape<ND, RS>::block)
 k_sav_local_diffusion(SavDev m, SavTab<RS> tab, double dt, double diff_time)
@@ -559,7 +596,7 @@ k_sav_local_diffusion(SavDev m, SavTab<RS> tab, double dt, double diff_time)
   constexpr int nq = S::nq, nfq = S::nfq, n_sav = S::n_sav;
   extern __shared__ double s_mem[];
   double* s_r = s_mem + L::rows;   // [3][nq]
-  double* s_f = s_mem + L::flux;   // [ND][3][nq]
+  double* s_f = s_mem + L::flux;   // [ND][3][nq]; during the gradient: products [ND (j)][3][nq]
   double* s_bf = s_mem + L::bf;    // [ND (d)][ND (j)][3][nfq][2]
   const int e = blockIdx.x;
   const int q = threadIdx.x;
@@ -567,74 +604,65 @@ k_sav_local_diffusion(SavDev m, SavTab<RS> tab, double dt, double diff_time)
   const double* st = m.elem + (size_t)e*(S::nv + 3)*nq;
   double* fc = S::forcing(m, e);
   const double d_pos = m.nom_size[e];
+  const double inv_dpos = 1./d_pos;
   const int ed = e - m.n_car;
   const double* nrml = deformed ? m.jac + (size_t)ed*(ND*ND + 1)*nq : nullptr;
   if (q < nq) {
     #pragma unroll
     for (int v = 0; v < n_sav; ++v) s_r[v*nq + q] = fc[(1 + v)*nq + q];
   }
-  __syncthreads();
-  // boundary corrections of every gradient row, once per row: fb_s - B_s.x with x the row of
-  // the unknown (times the metric normal n_dj on deformed elements) and fb_s its LDG face
-  // value (times the face normal)
-  const int n_j = deformed ? ND : 1;
-  for (int t = threadIdx.x; t < ND*n_j*n_sav*nfq; t += blockDim.x) {
-    const int i_fq = t%nfq, v = (t/nfq)%n_sav, j = (t/(nfq*n_sav))%n_j, d = t/(nfq*n_sav*n_j);
-    const double* la = S::slot(m, e*2*ND + 2*d, true);
-    const double* lb = S::slot(m, e*2*ND + 2*d + 1, true);
-    double x[RS];
-    double fb0 = la[v*nfq + i_fq], fb1 = lb[v*nfq + i_fq];
-    if (deformed) {
-      const double* fna = m.face_nrml + ((size_t)ed*2*ND + 2*d)*ND*nfq;
-      const double* fnb = fna + ND*nfq;
-      #pragma unroll
-      for (int k = 0; k < RS; ++k) {
-        const int qk = S::row_qpoint(d, i_fq, k);
-        x[k] = nrml[(d*ND + j)*nq + qk]*s_r[v*nq + qk];
-      }
-      fb0 = fna[j*nfq + i_fq]*fb0;
-      fb1 = fnb[j*nfq + i_fq]*fb1;
-    } else {
-      #pragma unroll
-      for (int k = 0; k < RS; ++k) x[k] = s_r[v*nq + S::row_qpoint(d, i_fq, k)];
-    }
-    double b0 = 0., b1 = 0.;
+  double g[n_sav][ND];
+  #pragma unroll
+  for (int v = 0; v < n_sav; ++v)
     #pragma unroll
-    for (int k = 0; k < RS; ++k) { b0 += tab.bound[k]*x[k]; b1 += tab.bound[RS + k]*x[k]; }
-    const int r = ((d*ND + j)*n_sav + v)*nfq + i_fq;
-    s_bf[2*r] = fb0 - b0;
-    s_bf[2*r + 1] = fb1 - b1;
-  }
-  __syncthreads();
-  if (q < nq) {
-    double g[n_sav][ND];
-    #pragma unroll
-    for (int v = 0; v < n_sav; ++v)
-      #pragma unroll
-      for (int d = 0; d < ND; ++d) g[v][d] = 0.;
+    for (int d = 0; d < ND; ++d) g[v][d] = 0.;
+  if (deformed) {
+    // grad_j u_v = sum_d [D_d (n_dj u_v) + lift_d (n^f_dj u^f_v - B_d (n_dj u_v))] / size
     #pragma unroll
     for (int d = 0; d < ND; ++d) {
-      const int stride = ipow(RS, ND - 1 - d);
-      const int i = (q/stride)%RS;
-      const int i_fq = (q/(stride*RS))*stride + q%stride;
-      const int r0 = q - i*stride;
-      if (deformed) {
+      __syncthreads();   // s_r staged (d = 0); the previous dimension's products read
+      if (q < nq) {
         #pragma unroll
         for (int j = 0; j < ND; ++j) {
-          double row_n[RS];
+          const double n_dj = nrml[(d*ND + j)*nq + q];
           #pragma unroll
-          for (int k = 0; k < RS; ++k) row_n[k] = nrml[(d*ND + j)*nq + r0 + k*stride];
+          for (int v = 0; v < n_sav; ++v) s_f[(j*n_sav + v)*nq + q] = n_dj*s_r[v*nq + q];
+        }
+      }
+      __syncthreads();
+      sav_diff_row_corrections<ND, RS>(m, tab, e, d, true, s_f, s_bf);
+      __syncthreads();
+      if (q < nq) {
+        const int stride = ipow(RS, ND - 1 - d);
+        const int i = (q/stride)%RS;
+        const int i_fq = (q/(stride*RS))*stride + q%stride;
+        const int r0 = q - i*stride;
+        #pragma unroll
+        for (int j = 0; j < ND; ++j)
           #pragma unroll
           for (int v = 0; v < n_sav; ++v) {
             double x[RS];
             #pragma unroll
-            for (int k = 0; k < RS; ++k) x[k] = row_n[k]*s_r[v*nq + r0 + k*stride];
+            for (int k = 0; k < RS; ++k) x[k] = s_f[(j*n_sav + v)*nq + r0 + k*stride];
             const int r = ((d*ND + j)*n_sav + v)*nfq + i_fq;
             const double der = row_derivative_bf<RS>(tab, x, s_bf[2*r], s_bf[2*r + 1], i);
-            g[v][j] = 1.*g[v][j] + der/d_pos;
+            g[v][j] = 1.*g[v][j] + der*inv_dpos;
           }
-        }
-      } else {
+      }
+    }
+    __syncthreads();   // every product read before the fluxes overwrite them
+  } else {
+    __syncthreads();
+    #pragma unroll
+    for (int d = 0; d < ND; ++d) sav_diff_row_corrections<ND, RS>(m, tab, e, d, false, s_r, s_bf);
+    __syncthreads();
+    if (q < nq) {
+      #pragma unroll
+      for (int d = 0; d < ND; ++d) {
+        const int stride = ipow(RS, ND - 1 - d);
+        const int i = (q/stride)%RS;
+        const int i_fq = (q/(stride*RS))*stride + q%stride;
+        const int r0 = q - i*stride;
         #pragma unroll
         for (int v = 0; v < n_sav; ++v) {
           double x[RS];
@@ -642,17 +670,19 @@ k_sav_local_diffusion(SavDev m, SavTab<RS> tab, double dt, double diff_time)
           for (int k = 0; k < RS; ++k) x[k] = s_r[v*nq + r0 + k*stride];
           const int r = ((d*ND)*n_sav + v)*nfq + i_fq;   // the task layout with j = 0
           const double der = row_derivative_bf<RS>(tab, x, s_bf[2*r], s_bf[2*r + 1], i);
-          g[v][d] = 0*g[v][d] + der/d_pos;
+          g[v][d] = 0*g[v][d] + der*inv_dpos;
         }
       }
     }
-    // flux -gradient.normal (Spatial.hpp:405-442)
-    const double det = deformed ? nrml[ND*ND*nq + q] : 1.;
+  }
+  // flux -gradient.normal (Spatial.hpp:405-442)
+  if (q < nq) {
+    const double inv_det = deformed ? 1./nrml[ND*ND*nq + q] : 1.;
     #pragma unroll
     for (int v = 0; v < n_sav; ++v) {
       if (deformed) {
         #pragma unroll
-        for (int d = 0; d < ND; ++d) g[v][d] /= det;
+        for (int d = 0; d < ND; ++d) g[v][d] *= inv_det;
       }
       #pragma unroll
       for (int i = 0; i < ND; ++i) {

@@ -139,3 +139,28 @@ def test_integer_conversions_match_hardware():
     bad = ctypes.c_long()
     abi.check(lib.hexed_gpu_check_conversions(x.ctypes.data_as(abi.P_double), x.size, ctypes.byref(bad)))
     assert bad.value == 0
+
+
+@pytest.mark.parametrize("viscous", [False, True])
+def test_mixed_max_dt_follows_vertex_scales(viscous):
+    """The mixed form's Max_dt reads a float copy of the vertex time-step scales. Uploading new
+    scales (whole array, then a range) refreshes it: after each, the mixed step matches the FP64
+    step to float precision, and the steps really changed. (Recomputing the metrics on the
+    device refreshes it too: test_gpu_metrics' mixed case updates after hexed_gpu_compute_jacobian
+    has rewritten the scales from zero.)"""
+    from helpers import air_transport
+    ar = deformed_case(3, 4, 3, abi.BC_RIEMANN)
+    visc, cond = air_transport()
+    n = ar.vert_tss.size
+    dts = {}
+    for prec in (abi.FP64, abi.MIXED):
+        with Context(ar.copy(), prec) as c:
+            out = [c.max_dt(0.7, 0.5, False, viscous, visc, cond)]
+            c.upload(abi.ARRAY_VERT_TSS, 0.5 * ar.vert_tss)
+            out.append(c.max_dt(0.7, 0.5, False, viscous, visc, cond))
+            c.write_range(abi.ARRAY_VERT_TSS, n // 2, 0.25 * ar.vert_tss.reshape(-1)[n // 2:])
+            out.append(c.max_dt(0.7, 0.5, False, viscous, visc, cond))
+            dts[prec] = out
+    d64, d32 = np.array(dts[abi.FP64]), np.array(dts[abi.MIXED])
+    assert np.all(np.abs(np.diff(d64)) > 1e-3 * d64[0])
+    assert np.max(np.abs(d32 - d64) / d64) < 1e-6, (d32, d64)
