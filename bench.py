@@ -166,7 +166,7 @@ NCU_FP64_FLOPS_PER_ELEM = {
     ("local_def_ns", 6): 455624.,
     ("local_def_euler", 6): 106920.,
     # the smoothness-AV advection volume kernel (3D deformed, row size 6; ncu on the 16^3 mesh)
-    ("sav_local_advection", 6): 159192.,
+    ("sav_local_advection", 6): 136728.,
 }
 
 
@@ -471,6 +471,33 @@ def fp64_peak_tflops_cached():
     return _FP64_PEAK[0]
 
 
+_DGEMM_PEAK = []
+
+
+def fp64_dgemm_tflops_cached(n=4096, reps=3):
+    """A library cross-check of the FP64 rate: cuBLAS DGEMM (torch.matmul in float64) of
+    n x n operands, best of `reps` after one warm-up, 2 n^3 flops each, CUDA events on the
+    current stream. Measured once per run."""
+    if not _DGEMM_PEAK:
+        import torch
+        a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+        b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+        torch.matmul(a, b)
+        best = None
+        for _ in range(reps):
+            t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            t0.record()
+            torch.matmul(a, b)
+            t1.record()
+            torch.cuda.synchronize()
+            ms = t0.elapsed_time(t1)
+            best = ms if best is None else min(best, ms)
+        _DGEMM_PEAK.append(2 * n ** 3 / (best * 1e-3) / 1e12)
+        del a, b
+        torch.cuda.empty_cache()
+    return _DGEMM_PEAK[0]
+
+
 def sav_advection_bytes(ar):
     """Compulsory bytes of one launch of the smoothness-AV advection volume kernel: per element
     the nd velocity rows, the advection state read and written, its residual cache written
@@ -696,6 +723,10 @@ def main():
                             "flops_source": "ncu 2*dfma + dadd + dmul thread instructions per element of one "
                                             "launch on the 16^3 Taylor-Green mesh, scaled by elements",
                             "peak_source": "hexed_gpu_fp64_peak, measured in this run"}
+        dgemm = fp64_dgemm_tflops_cached()
+        roofline["fp64"]["dgemm_tflops"] = dgemm
+        roofline["fp64"]["frac_of_dgemm"] = achieved_tf / dgemm
+        roofline["fp64"]["dgemm_source"] = "cuBLAS DGEMM 4096^3 (torch.matmul, float64), best of 3, this run"
     kernels = {k: {"launches": v[0], "total_ms": round(v[1], 4), "share": round(v[1] / sum(x[1] for x in prof.values()), 4)}
                for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])}
 

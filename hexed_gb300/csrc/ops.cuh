@@ -426,6 +426,37 @@ struct Runner
     else k_sav_refine<ND, RS, false, NVAR><<<c.n_ref, 256, 0, c.stream>>>(m, t, scale, offset);
   }
 
+  // Runs body(0), ..., body(n - 1), where body(i) enqueues the same launches for every i >= 1.
+  // From the second iteration on, the launches of one iteration are captured once as a CUDA
+  // graph and the graph is launched for the rest: a pseudo-time loop of thousands of
+  // iterations on a small mesh is otherwise bound by launch latency. Eager throughout when
+  // the per-kernel profiler is on (so that it sees every kernel), inside another capture, for
+  // fewer than three iterations, or if a graph call fails (from that iteration on).
+  template <typename F>
+  static void repeat_iterations(Ctx& c, int n, F&& body)
+  {
+    const bool eager = n < 3 || c.capturing || (c.prof && c.prof->enabled);
+    int i = 0;
+    if (!eager) {
+      body(i++);
+      cudaGraph_t graph = nullptr;
+      cudaGraphExec_t exec = nullptr;
+      bool failed = cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess;
+      if (!failed) {
+        c.capturing = true;
+        body(1);   // recorded, not run
+        c.capturing = false;
+        failed = cudaStreamEndCapture(c.stream, &graph) != cudaSuccess || !graph ||
+                 cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess;
+        for (; !failed && i < n; ++i) failed = cudaGraphLaunch(exec, c.stream) != cudaSuccess;
+        if (graph) cudaGraphDestroy(graph);
+        if (exec) cudaGraphExecDestroy(exec);   // freed once its launches complete
+      }
+      if (failed) cudaGetLastError();   // the graph call's error; the eager loop runs the rest
+    }
+    for (; i < n; ++i) body(i);
+  }
+
   // Solver::update_art_visc_smoothness (src/Solver.cpp:457-582) with Solver::diffuse_art_visc
   // (src/Solver.cpp:428-455): the reference's kernel sequence, then the flow's Write_face and
   // Prolong (src/Solver.cpp:577-578). d_residual receives art_visc_residual.
@@ -453,6 +484,7 @@ struct Runner
     }
     auto sav_faces = [&](int mode) {
       const long n = (long)n_elem*ND*SS::nfq*(mode ? SS::n_sav : SS::n_adv_extrap);
+      ProfScope ps(c, "sav_write_face");
       k_sav_write_face<ND, RS><<<grid_for(n, 256), 256, 0, c.stream>>>(m, st, mode);
     };
     {
@@ -461,7 +493,7 @@ struct Runner
       k_sav_velocity<ND, RS><<<g_pts, 256, 0, c.stream>>>(m);
       k_sav_max_dt<ND, RS><<<g_pts, 256, 0, c.stream>>>(m, st, 0, t.max_cfl*p.advect_safety);
     }
-    for (int iter = 0; iter < p.advect_iters; ++iter) {
+    repeat_iterations(c, p.advect_iters, [&](int iter) {
       // compute_write_face_advection + compute_prolong_advection; after the first iteration the
       // previous stage's volume kernel and prolongation have written these same traces
       if (iter == 0) {
@@ -483,7 +515,7 @@ struct Runner
         }
         sav_refine<SS::n_adv_extrap>(c, m, t, true, false, false);
       }
-    }
+    });
     // projection onto the Legendre mode of degree av_rs - 1
     AvTab<RS, double> wo;
     for (int i = 0; i < RS; ++i) {
@@ -491,18 +523,24 @@ struct Runner
       wo.ow[i] = c.tables.ortho[(p.av_row_size - 1)*RS + i];
       wo.node[i] = t.node[i];
     }
-    k_sav_project<ND, RS><<<g_pts, 256, 0, c.stream>>>(m, wo);
     // diffuse_art_visc: n_forcing - 1 = 3 real steps of pde::Smooth_art_visc at once
     const double diff_time = p.diff_ratio*p.advect_length*p.advect_length/(SS::n_forcing - 1);
-    k_sav_max_dt<ND, RS><<<g_pts, 256, 0, c.stream>>>(m, st, 1, -2/t.min_eig_diffusion*p.diff_safety);
+    {
+      ProfScope ps(c, "sav_setup");
+      k_sav_project<ND, RS><<<g_pts, 256, 0, c.stream>>>(m, wo);
+      k_sav_max_dt<ND, RS><<<g_pts, 256, 0, c.stream>>>(m, st, 1, -2/t.min_eig_diffusion*p.diff_safety);
+    }
     sav_faces(1);
     sav_refine<SS::nv>(c, m, t, true, false, false);   // compute_prolong: the flow's nv variables
-    for (int i_iter = 0; i_iter < p.diff_iters; ++i_iter) {
+    repeat_iterations(c, p.diff_iters, [&](int) {
       for (int i_cheby = 0; i_cheby < p.n_cheby; ++i_cheby) {
         // math::chebyshev_step (src/math.cpp:104-107)
         const double s = 1/(1 - std::cos((p.n_cheby - i_cheby - 0.5)*3.14159265358979323846/p.n_cheby));
         if (m.n_bc_con) k_sav_bc_diffusion<ND, RS><<<g_bc, 256, 0, c.stream>>>(m, 0);
-        if (n_face_pts) k_sav_neighbor_ldg<ND, RS><<<g_con, 256, 0, c.stream>>>(m, 0);
+        if (n_face_pts) {
+          ProfScope ps(c, "sav_neighbor_ldg");
+          k_sav_neighbor_ldg<ND, RS><<<g_con, 256, 0, c.stream>>>(m, 0);
+        }
         sav_refine<SS::n_sav>(c, m, t, false, true, false);
         sav_refine<SS::n_sav>(c, m, t, false, false, true);
         {
@@ -511,18 +549,27 @@ struct Runner
         }
         sav_refine<SS::n_sav>(c, m, t, true, true, true);
         if (m.n_bc_con) k_sav_bc_diffusion<ND, RS><<<g_bc, 256, 0, c.stream>>>(m, 1);
-        if (n_face_pts) k_sav_neighbor_ldg<ND, RS><<<g_con, 256, 0, c.stream>>>(m, 1);
+        if (n_face_pts) {
+          ProfScope ps(c, "sav_neighbor_ldg");
+          k_sav_neighbor_ldg<ND, RS><<<g_con, 256, 0, c.stream>>>(m, 1);
+        }
         sav_refine<SS::n_sav>(c, m, t, false, true, true);
-        k_sav_reconcile<ND, RS><<<g_pts, 256, 0, c.stream>>>(m, st, s, diff_time, s);
+        {
+          ProfScope ps(c, "sav_reconcile");
+          k_sav_reconcile<ND, RS><<<g_pts, 256, 0, c.stream>>>(m, st, s, diff_time, s);
+        }
         sav_faces(1);
         sav_refine<SS::n_sav>(c, m, t, true, false, false);
       }
-    }
+    });
     // coefficient, residual, momentum put back; then the flow's traces
     const double mult = p.visc_mult*p.advect_length;
     const double us_max = p.advect_length*p.unscaled_max*std::sqrt(2*p.freestream_energy/p.freestream_mass);
-    k_sav_finish<ND, RS><<<grid_for(n_elem, 1), 128, 0, c.stream>>>(m, wo, mult, us_max);
-    k_sav_residual<<<1, 256, 0, c.stream>>>(m.partials, n_elem, d_residual);
+    {
+      ProfScope ps(c, "sav_setup");
+      k_sav_finish<ND, RS><<<grid_for(n_elem, 1), 128, 0, c.stream>>>(m, wo, mult, us_max);
+      k_sav_residual<<<1, 256, 0, c.stream>>>(m.partials, n_elem, d_residual);
+    }
     write_face(c, 0, n_elem);
     refine(c, true, false, false);
   }

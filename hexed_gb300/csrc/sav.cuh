@@ -289,11 +289,13 @@ __global__ void k_sav_neighbor_advection(SavDev m, SavTab<RS> tab)
     for (int d = 0; d < ND; ++d) { nv0 += u0[d]*n[d]; nv1 += u1[d]*n[d]; }
     #pragma unroll
     for (int d = 0; d < ND; ++d) { sq0 += u0[d]*u0[d]; sq1 += u1[d]*u1[d]; }
-    const double cs0 = fmax(1., sqrt(sq0)), cs1 = fmax(1., sqrt(sq1));
+    // max(max(1, |v0|), max(1, |v1|)) with one square root: sqrt is correctly rounded and
+    // monotonic, and sqrt(1) = 1, so this is the same number
+    const double cs = sqrt(fmax(1., fmax(sq0, sq1)));
     double nn = 0.;
     #pragma unroll
     for (int d = 0; d < ND; ++d) nn += n[d]*n[d];
-    const double mult = fmax(cs0, cs1)*sqrt(nn);
+    const double mult = cs*(deformed ? sqrt(nn) : 1.);   // Cartesian normals are unit vectors
     #pragma unroll
     for (int a = 0; a < n_adv; ++a) {
       const double fl0 = tab.adv_node[a]*nv0*u0[ND + a];
@@ -409,15 +411,18 @@ k_sav_local_advection(SavDev m, SavTab<RS> tab, int stage, double advect_length,
         rate[a] = 1.*rate[a] + -der;
       }
     }
+    // three divisions per point (the element's size times the determinant, the pseudo-time
+    // factor, 2/advect_length) and reciprocal multiplies after them: each FP64 division costs
+    // about ten FP64 operations, and this kernel is bound by the FP64 pipe
     const double tss = st[S::nv*nq + q];
     const double det = deformed ? nrml[ND*ND*nq + q] : 1.;
     const double update_coef = stage ? 1.*step_ratio : 1.;
-    double mult = update_coef*tss/d_pos;
-    if (deformed) mult /= det;
-    const double pseudo = 1 + tss*2/advect_length;
+    const double mult = update_coef*tss/(deformed ? d_pos*det : d_pos);
+    const double two_l = 2/advect_length;
+    const double inv_pseudo = 1/(1 + tss*two_l);
     double src_mult = d_pos;
     if (deformed) src_mult *= det;
-    const double source = src_mult*(2/advect_length);
+    const double source = src_mult*two_l;
     #pragma unroll
     for (int a = 0; a < n_adv; ++a) {
       double u = rate[a];
@@ -429,7 +434,7 @@ k_sav_local_advection(SavDev m, SavTab<RS> tab, int stage, double advect_length,
       }
       u *= mult;
       const double x = a_old[a];
-      const double nx = stage ? x + u/pseudo : (x + u)/pseudo;
+      const double nx = stage ? x + u*inv_pseudo : (x + u)*inv_pseudo;
       a_st[a*nq + q] = nx;
       s_rows[(ND + a)*nq + q] = nx;
     }
@@ -775,15 +780,16 @@ __global__ void k_sav_reconcile(SavDev m, SavTab<RS> tab, double dt, double diff
     }
     const double* st = m.elem + (size_t)e*(S::nv + 3)*nq;
     const double tss = st[S::nv*nq + q];
-    double mult = dt*tss/m.nom_size[e];
-    if (deformed) mult /= m.jac[((size_t)(e - m.n_car)*(ND*ND + 1) + ND*ND)*nq + q];
-    const double pseudo = 1 + tss*cheby/diff_time;
+    const double size = deformed ? m.nom_size[e]*m.jac[((size_t)(e - m.n_car)*(ND*ND + 1) + ND*ND)*nq + q]
+                                 : m.nom_size[e];
+    const double mult = dt*tss/size;
+    const double inv_pseudo = 1/(1 + tss*cheby/diff_time);   // one division for the three unknowns
     double* fc = S::forcing(m, e);
     #pragma unroll
     for (int v = 0; v < n_sav; ++v) {
       double x = fc[(1 + v)*nq + q];
       x += rate[v]*mult;
-      x /= pseudo;
+      x *= inv_pseudo;
       fc[(1 + v)*nq + q] = x;
     }
   }

@@ -166,3 +166,53 @@ def test_invalid_parameters():
                     abi.sav_params(0., 4, 1., 1.5), abi.sav_params(0.1, 4, 1., 1.5, n_cheby=0)):
             with pytest.raises(abi.HexedError):
                 c.update_art_visc_smoothness(bad)
+
+
+def test_graph_replay_matches_eager_launches():
+    """From the second pseudo-time iteration on, each iteration replays a captured CUDA graph;
+    with the per-kernel profiler on, every launch is eager. Both give the same bits."""
+    ar = strip(4, (10, 2))
+    tanh_state(ar, 0.1)
+    pg = abi.sav_params(0.1, ar.row_size, 1., 1.5, advect_iters=30, diff_iters=12, n_cheby=2)
+    out = []
+    for profile in (False, True):
+        b = ar.copy()
+        with Context(b) as c:
+            c.write_face()
+            c.prolong()
+            if profile:
+                c.profile_enable(True)
+            res = [c.update_art_visc_smoothness(pg) for _ in range(2)]
+            if profile:
+                assert c.profile_read()["sav_local_advection"][0] == 2 * 2 * 30
+            out.append((res, c.download(abi.ARRAY_ELEM), c.sav_storage()[0]))
+    assert out[0][0] == out[1][0]
+    assert np.array_equal(out[0][1], out[1][1]) and np.array_equal(out[0][2], out[1][2])
+
+
+def test_reference_convergence():
+    """The reference's "artificial viscosity convergence" test (test/test_Solver.cpp:829-877)
+    on the GPU with its settings: row size 8, 100 x 2 elements, 6000 advection and 3000
+    diffusion iterations, diffusion ratio 1e-6, unscaled maximum 1000, one solver throughout
+    (the advection state carries over between calls). Doubling the advection length
+    multiplies the coefficient by more than 2^(row_size - 1); halving the flow's length scale,
+    by more than 2^(row_size - 2)."""
+    import math
+    rs = 8
+    ar = strip(rs, (100, 2))
+    tanh_state(ar, 0.04)
+    kw = dict(advect_iters=6000, diff_iters=3000, diff_ratio=1e-6, unscaled_max=1000.)
+    with Context(ar.copy()) as c:
+        c.write_face()
+        c.prolong()
+
+        def coef(length):
+            resid = c.update_art_visc_smoothness(abi.sav_params(length, rs, 1., 1.5, **kw))
+            assert resid > 0 and np.isfinite(resid)
+            return c.download(abi.ARRAY_ELEM)[:, ar.nv + 1].max()
+        init_max = coef(0.01)
+        assert init_max > 0
+        assert math.log2(coef(0.02) / init_max) > rs - 1.
+        tanh_state(ar, 0.02)
+        c.write_state(ar.elem[:, :ar.nv])
+        assert math.log2(coef(0.01) / init_max) > rs - 2.
