@@ -697,7 +697,9 @@ def main():
     achieved = nbytes / (per_launch_ms * 1e-3) / 1e9 if nbytes else None
     fp64_peak = fp64_peak_tflops_cached()
     traffic = None
-    per_elem = NCU_DRAM_BYTES_PER_ELEM.get((top_name, args.precision, wl.rs)) if wl.kind == "tgv" else None
+    # the Mach-2 case runs the same deformed kernels on the same mesh kind (same arrays per
+    # element), so the Taylor-Green captures' per-element figures apply to it too
+    per_elem = NCU_DRAM_BYTES_PER_ELEM.get((top_name, args.precision, wl.rs)) if wl.kind in ("tgv", "mach2") else None
     if per_elem is not None:
         traffic = per_elem * (ar.n_def if "def" in top_name else ar.n_car if "car" in top_name else ar.n_elem)
     roofline = {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
@@ -708,7 +710,7 @@ def main():
                 "algorithmic_bytes_per_launch": nbytes, "launch_ms": per_launch_ms,
                 "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
                 "fp64_peak_tflops_measured": fp64_peak}
-    pipe = NCU_PIPE_FRAC.get((top_name, args.precision, wl.rs)) if wl.kind == "tgv" else None
+    pipe = NCU_PIPE_FRAC.get((top_name, args.precision, wl.rs)) if wl.kind in ("tgv", "mach2") else None
     if pipe is not None:
         # what bounds this kernel instead of HBM: the busiest pipe in the same ncu capture
         roofline["compute_bound"] = {"pipe": pipe[0], "frac_of_peak_ncu": pipe[1]}
@@ -750,7 +752,7 @@ def main():
         mlaunch_ms = mtop_ms / max(mlaunches, 1)
         mbytes = kernel_bytes(mtop, ar, "mixed")
         machieved = mbytes / (mlaunch_ms * 1e-3) / 1e9 if mbytes else None
-        mper_elem = NCU_DRAM_BYTES_PER_ELEM.get((mtop, "mixed", wl.rs)) if wl.kind == "tgv" else None
+        mper_elem = NCU_DRAM_BYTES_PER_ELEM.get((mtop, "mixed", wl.rs)) if wl.kind in ("tgv", "mach2") else None
         mroof = {"bound": "hbm", "kernel": mtop, "achieved": machieved, "peak": hbm_peak, "unit": "GB/s",
                  "frac": machieved / hbm_peak if machieved else None, "algorithmic_bytes_per_launch": mbytes,
                  "launch_ms": mlaunch_ms,
