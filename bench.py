@@ -146,8 +146,8 @@ def kernel_bytes(name, ar, precision="fp64"):
 # dram__bytes_write.sum, one launch) on smaller Taylor-Green meshes of the same kernels: FP64
 # on the 16^3 mesh, mixed on the 24^3 mesh, row size 6.
 NCU_DRAM_BYTES_PER_ELEM = {
-    ("local_def_ns", "fp64", 6): 73281.,
-    ("local_def_euler", "fp64", 6): 69966.,
+    ("local_def_ns", "fp64", 6): 73092.,
+    ("local_def_euler", "fp64", 6): 69626.,
     ("local_def_ns", "mixed", 6): (490.465792e6 + 201.874944e6) / 13824,
     ("local_def_euler", "mixed", 6): (514.078720e6 + 149.316096e6) / 13824,
 }
@@ -155,18 +155,18 @@ NCU_DRAM_BYTES_PER_ELEM = {
 
 # Busiest pipe of the same kernels in those captures (fraction of peak sustained over active cycles).
 NCU_PIPE_FRAC = {
-    ("local_def_ns", "fp64", 6): ("fp64", 0.919),
-    ("local_def_euler", "fp64", 6): ("fp64", 0.879),
+    ("local_def_ns", "fp64", 6): ("fp64", 0.940),
+    ("local_def_euler", "fp64", 6): ("fp64", 0.930),
 }
 
 # FP64 flops per element of the FP64 kernels (2 x DFMA + DADD + DMUL thread instructions
 # counted by ncu on the 16^3 Taylor-Green mesh, row size 6): the compute roofline of the FP64
 # form, against the FP64 FMA rate hexed_gpu_fp64_peak measures in the same run.
 NCU_FP64_FLOPS_PER_ELEM = {
-    ("local_def_ns", 6): 455624.,
-    ("local_def_euler", 6): 106920.,
+    ("local_def_ns", 6): 419984.,
+    ("local_def_euler", 6): 100440.,
     # the smoothness-AV advection volume kernel (3D deformed, row size 6; ncu on the 16^3 mesh)
-    ("sav_local_advection", 6): 136728.,
+    ("sav_local_advection", 6): 128952.,
 }
 
 

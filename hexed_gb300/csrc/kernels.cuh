@@ -487,8 +487,9 @@ __device__ __forceinline__ void bound_dot(const RowTab<RS, R>& t, const R (&x)[R
 }
 
 // (D.x)_i + lift_i.(b0, b1): Derivative::operator() at node i, with b_s the face value minus
-// the extrapolated row (include/Derivative.hpp:56-60). One FMA chain, lift terms first: the
-// row-task body is the float form's, whose sums need not follow the reference's order.
+// the extrapolated row (include/Derivative.hpp:56-60). One FMA chain, lift terms first, as in
+// the FP64 body: the sums need not follow the reference's order (they agree with it to
+// roundoff, far inside the parity bars), and a chain saves the separate additions.
 template <int RS, typename R>
 __device__ __forceinline__ R row_deriv(const RowTab<RS, R>& t, const R (&x)[RS], int i, R b0, R b1)
 {
@@ -719,17 +720,17 @@ __device__ __forceinline__ R point_step(const Dev<FaceT>& m, int e, int q, const
   R s[nv];
   #pragma unroll
   for (int v = 0; v < nv; ++v) s[v] = to_R<R>(state[v*nq + q]);
-  const R inv_spacing = R(1)/spacing;
-  if (m.fta) return R(1)/(inv_cfl_d*inv_spacing*inv_spacing);   // Fix_therm_admis: diffusivity 1
+  // 1/(c icc/h + nu icd/h^2) = h^2/(c icc h + nu icd): one division instead of two (each
+  // costs several FP64 operations on this GPU's FP64 pipe)
+  if (m.fta) return spacing*spacing/inv_cfl_d;   // Fix_therm_admis: diffusivity 1
   Conv<ND, R> c(s);
-  R scale = 0;
-  scale += char_speed<ND, R>(s, c.inv_mass)*inv_cfl_c*inv_spacing;
+  R denom = char_speed<ND, R>(s, c.inv_mass)*inv_cfl_c*spacing;
   if constexpr (VISC) {
     DiffScalars<ND, R> df(s, c, to_R<R>(state[(nv + 1)*nq + q]), to_R<R>(state[(nv + 2)*nq + q]), visc, cond);
     R diffusivity = fabs(df.laplacian_av) + fmax(fabs(df.bulk_av) + df.mu*c.inv_mass, df.energy_cond*c.inv_mass);
-    scale += diffusivity*inv_cfl_d*inv_spacing*inv_spacing;
+    denom += diffusivity*inv_cfl_d;
   }
-  return R(1)/scale;
+  return spacing*spacing/denom;
 }
 
 // Reference coordinates of point q from a node table (RS entries in R)
@@ -899,14 +900,13 @@ __device__ __forceinline__ void local_body_points(Dev<FaceT> m, const Tab<RS>& t
           const R* bf = my_bf + d*2*nv*nfq;
           #pragma unroll
           for (int v = 0; v < nv; ++v) {
+            // one FMA chain per output, lift terms first (as in row_deriv)
             const R* row = my_u + v*nq + base_of[d];
-            R acc = 0;
+            R acc = st.lift[i*2]*bf[v*nfq + row_of[d]];
+            acc += st.lift[i*2 + 1]*bf[(nv + v)*nfq + row_of[d]];
             #pragma unroll
             for (int j = 0; j < RS; ++j) acc += st.diff[i*RS + j]*row[j*stride];
-            R l = 0;
-            l += st.lift[i*2]*bf[v*nfq + row_of[d]];
-            l += st.lift[i*2 + 1]*bf[(nv + v)*nfq + row_of[d]];
-            grad[v][d] = (acc + l)*inv_dpos_r;
+            grad[v][d] = acc*inv_dpos_r;
           }
         }
       }
@@ -953,18 +953,23 @@ __device__ __forceinline__ void local_body_points(Dev<FaceT> m, const Tab<RS>& t
             const R* bf = my_bf + j*2*nv*nfq;
             #pragma unroll
             for (int v = 0; v < nv; ++v) {
+              // the sum over d accumulates unscaled in one FMA chain per output, lift terms
+              // first; the 1/size factor is applied once after the last dimension
               const R* row = my_f + (j*nv + v)*nq + base_of[d];
-              R acc = 0;
+              R acc = grad[v][j];
+              acc += st.lift[i*2]*bf[v*nfq + row_of[d]];
+              acc += st.lift[i*2 + 1]*bf[(nv + v)*nfq + row_of[d]];
               #pragma unroll
               for (int jj = 0; jj < RS; ++jj) acc += st.diff[i*RS + jj]*row[jj*stride];
-              R l = 0;
-              l += st.lift[i*2]*bf[v*nfq + row_of[d]];
-              l += st.lift[i*2 + 1]*bf[(nv + v)*nfq + row_of[d]];
-              grad[v][j] = grad[v][j] + (acc + l)*inv_dpos_r;
+              grad[v][j] = acc;
             }
           }
         }
       }
+      #pragma unroll
+      for (int v = 0; v < nv; ++v)
+        #pragma unroll
+        for (int j = 0; j < ND; ++j) grad[v][j] *= inv_dpos_r;
     }
     __syncthreads(); // s_f / s_bf are reused below
   }
@@ -1054,20 +1059,20 @@ __device__ __forceinline__ void local_body_points(Dev<FaceT> m, const Tab<RS>& t
       const R* bf = my_bf + d*2*nv*nfq;
       #pragma unroll
       for (int v = 0; v < nv; ++v) {
+        // rate -= D.f + lift.(f* - B.f) as one FMA chain per output over all dimensions
         const R* row = my_f + (d*nv + v)*nq + base_of[d];
-        R acc = 0;
+        R acc = rate[v];
+        acc -= st.lift[i*2]*bf[v*nfq + row_of[d]];
+        acc -= st.lift[i*2 + 1]*bf[(nv + v)*nfq + row_of[d]];
         #pragma unroll
-        for (int j = 0; j < RS; ++j) acc += st.diff[i*RS + j]*row[j*stride];
-        R l = 0;
-        l += st.lift[i*2]*bf[v*nfq + row_of[d]];
-        l += st.lift[i*2 + 1]*bf[(nv + v)*nfq + row_of[d]];
-        rate[v] = rate[v] + -(acc + l);
+        for (int j = 0; j < RS; ++j) acc -= st.diff[i*RS + j]*row[j*stride];
+        rate[v] = acc;
         if constexpr (VISC) {
           const R* rg = my_g + (d*nv + v)*nq + base_of[d];
-          R ag = 0;
+          R ag = vrate[v];
           #pragma unroll
-          for (int j = 0; j < RS; ++j) ag += st.diff[i*RS + j]*rg[j*stride];
-          vrate[v] = vrate[v] + -ag;
+          for (int j = 0; j < RS; ++j) ag -= st.diff[i*RS + j]*rg[j*stride];
+          vrate[v] = ag;
         }
       }
     }
@@ -1641,10 +1646,10 @@ k_reconcile_ldg(Dev<FaceT> m, Tab<RS> tab, RowTab<RS, R> rt, int e_begin, int e_
       #pragma unroll
       for (int v = 0; v < nv; ++v) {
         R b0 = R(fl[v*nfq]), b1 = R(fl[S::slot_dof + v*nfq]);
-        R l = 0;
-        l += st.lift[i*2]*b0;
-        l += st.lift[i*2 + 1]*b1;
-        tr[v] = tr[v] + -l;
+        R acc = tr[v];   // tr -= lift.(b0, b1), one FMA chain
+        acc -= st.lift[i*2]*b0;
+        acc -= st.lift[i*2 + 1]*b1;
+        tr[v] = acc;
       }
     }
   }

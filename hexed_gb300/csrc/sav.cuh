@@ -307,20 +307,19 @@ __global__ void k_sav_neighbor_advection(SavDev m, SavTab<RS> tab)
   }
 }
 
-// Derivative::operator() for output node i of a row x whose boundary corrections
-// bf_s = fb_s - B_s.x were formed once for the whole row (Derivative.hpp:50-55):
-// sum_j diff[i][j] x_j + (lift[i][0] bf0 + lift[i][1] bf1).
-template <int RS>
-__device__ __forceinline__ double row_derivative_bf(const SavTab<RS>& t, const double (&x)[RS], double bf0,
-                                                    double bf1, int i)
+// acc + sign*(Derivative::operator() for output node i) of a row x whose boundary
+// corrections bf_s = fb_s - B_s.x were formed once for the whole row (Derivative.hpp:50-55),
+// sum_j diff[i][j] x_j + (lift[i][0] bf0 + lift[i][1] bf1), as one FMA chain into acc, lift
+// terms first (each FP64 operation saved counts: these kernels are bound by the FP64 pipe).
+template <int RS, int SIGN>
+__device__ __forceinline__ double accumulate_derivative_bf(double acc, const SavTab<RS>& t, const double (&x)[RS],
+                                                           double bf0, double bf1, int i)
 {
-  double d = 0.;
+  acc += SIGN*t.lift[i*2]*bf0;
+  acc += SIGN*t.lift[i*2 + 1]*bf1;
   #pragma unroll
-  for (int j = 0; j < RS; ++j) d += t.diff[i*RS + j]*x[j];
-  double l = 0.;
-  l += t.lift[i*2]*bf0;
-  l += t.lift[i*2 + 1]*bf1;
-  return d + l;
+  for (int j = 0; j < RS; ++j) acc += SIGN*t.diff[i*RS + j]*x[j];
+  return acc;
 }
 
 // Shared memory of k_sav_local_advection, in doubles: fluxes [nd][rs][nq], the per-row boundary
@@ -407,8 +406,7 @@ k_sav_local_advection(SavDev m, SavTab<RS> tab, int stage, double advect_length,
         #pragma unroll
         for (int k = 0; k < RS; ++k) x[k] = s_flux[(d*n_adv + a)*nq + q - i*stride + k*stride];
         const int r = (d*n_adv + a)*nfq + i_fq;
-        const double der = row_derivative_bf<RS>(tab, x, s_bf[2*r], s_bf[2*r + 1], i);
-        rate[a] = 1.*rate[a] + -der;
+        rate[a] = accumulate_derivative_bf<RS, -1>(rate[a], tab, x, s_bf[2*r], s_bf[2*r + 1], i);
       }
     }
     // three divisions per point (the element's size times the determinant, the pseudo-time
@@ -650,11 +648,14 @@ k_sav_local_diffusion(SavDev m, SavTab<RS> tab, double dt, double diff_time)
             #pragma unroll
             for (int k = 0; k < RS; ++k) x[k] = s_f[(j*n_sav + v)*nq + r0 + k*stride];
             const int r = ((d*ND + j)*n_sav + v)*nfq + i_fq;
-            const double der = row_derivative_bf<RS>(tab, x, s_bf[2*r], s_bf[2*r + 1], i);
-            g[v][j] = 1.*g[v][j] + der*inv_dpos;
+            g[v][j] = accumulate_derivative_bf<RS, 1>(g[v][j], tab, x, s_bf[2*r], s_bf[2*r + 1], i);
           }
       }
     }
+    #pragma unroll
+    for (int v = 0; v < n_sav; ++v)
+      #pragma unroll
+      for (int j = 0; j < ND; ++j) g[v][j] *= inv_dpos;   // the sum over d, scaled once
     __syncthreads();   // every product read before the fluxes overwrite them
   } else {
     __syncthreads();
@@ -674,8 +675,7 @@ k_sav_local_diffusion(SavDev m, SavTab<RS> tab, double dt, double diff_time)
           #pragma unroll
           for (int k = 0; k < RS; ++k) x[k] = s_r[v*nq + r0 + k*stride];
           const int r = ((d*ND)*n_sav + v)*nfq + i_fq;   // the task layout with j = 0
-          const double der = row_derivative_bf<RS>(tab, x, s_bf[2*r], s_bf[2*r + 1], i);
-          g[v][d] = 0*g[v][d] + der*inv_dpos;
+          g[v][d] = accumulate_derivative_bf<RS, 1>(0., tab, x, s_bf[2*r], s_bf[2*r + 1], i)*inv_dpos;
         }
       }
     }
@@ -731,10 +731,10 @@ k_sav_local_diffusion(SavDev m, SavTab<RS> tab, double dt, double diff_time)
     const int r0 = q - i*stride;
     #pragma unroll
     for (int v = 0; v < n_sav; ++v) {
-      double der = 0.;
+      double acc = rate[v];   // rate -= D.flux, one FMA chain
       #pragma unroll
-      for (int k = 0; k < RS; ++k) der += tab.diff[i*RS + k]*s_f[(d*n_sav + v)*nq + r0 + k*stride];
-      rate[v] = 1.*rate[v] + -der;
+      for (int k = 0; k < RS; ++k) acc -= tab.diff[i*RS + k]*s_f[(d*n_sav + v)*nq + r0 + k*stride];
+      rate[v] = acc;
     }
   }
   double mult = dt*st[S::nv*nq + q]/d_pos;
