@@ -552,7 +552,7 @@ def smooth_av_sample(wl, args, hbm_peak):
                         "flops_per_launch": flops * ar.n_elem,
                         "flops_source": "ncu 2*dfma + dadd + dmul thread instructions per element of one launch "
                                         "on the 16^3 Taylor-Green mesh, scaled by elements"}
-        roof["compute_bound"] = {"pipe": "fp64", "frac_of_peak_ncu": 0.874}
+        roof["compute_bound"] = {"pipe": "fp64", "frac_of_peak_ncu": 0.877}
     return {"workload": wl.name, "advect_iters": p.advect_iters, "diff_iters": p.diff_iters,
             "advect_length": length, "ms_per_call": ms,
             "ms_per_advection_iteration": ms / (p.advect_iters + p.diff_iters),
