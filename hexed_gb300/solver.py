@@ -294,6 +294,57 @@ class Solver:
     def state(self):
         return self.ctx.download(abi.ARRAY_ELEM)[:, :self.arena.nv]
 
+    def n_var_numeric(self):
+        """Storage_params::n_var_numeric (src/Storage_params.cpp:32-35) for two stages: the
+        numeric rows of an element's storage."""
+        a = self.arena
+        return a.nv + 3 + 4 + a.row_size + max(a.nv, a.row_size)
+
+    def numeric_storage(self):
+        """Every element's numeric storage [n_elem][n_var_numeric][nq], rows in the order of
+        Element's storage (src/Element.cpp:114-188): the state, time-step scale, bulk and
+        Laplacian AV coefficients, the four art_visc_forcing rows, the row_size advection
+        rows, then the residual cache (the flow's nv rows; rows beyond them zero). The
+        reference lets the flow's residual cache and the advection's share those last rows,
+        and each is written before it is read, so their content between calls does not
+        matter; here they are separate arrays and the flow's is the one stored."""
+        a = self.arena
+        nv, rs = a.nv, a.row_size
+        out = np.zeros((a.n_elem, self.n_var_numeric(), a.nq))
+        out[:, :nv + 3] = self.ctx.download(abi.ARRAY_ELEM)
+        aux, _ = self.ctx.sav_storage()
+        out[:, nv + 3:nv + 7 + rs] = aux[:, :4 + rs]
+        out[:, nv + 7 + rs:nv + 7 + rs + nv] = self.ctx.download(abi.ARRAY_RCACHE)
+        return out
+
+    def set_numeric_storage(self, storage):
+        """Inverse of numeric_storage: the device arena and smoothness-AV storage from it."""
+        a = self.arena
+        nv, rs = a.nv, a.row_size
+        storage = np.asarray(storage, dtype=np.float64)
+        want = (a.n_elem, self.n_var_numeric(), a.nq)
+        if storage.shape != want:
+            raise ValueError(f"numeric storage of shape {storage.shape}, this mesh needs {want}")
+        self.ctx.upload(abi.ARRAY_ELEM, storage[:, :nv + 3])
+        aux, _ = self.ctx.sav_storage()
+        aux[:, :4 + rs] = storage[:, nv + 3:nv + 7 + rs]
+        self.ctx.write_range(abi.ARRAY_SAV_AUX, 0, aux.reshape(-1))
+        self.ctx.upload(abi.ARRAY_RCACHE, storage[:, nv + 7 + rs:nv + 7 + rs + nv])
+
+    def write_state(self, file_name):
+        """Solver::write_state (src/Solver.cpp:253-271): one dataset `state`, [n_elem]
+        [n_var_numeric][n_qpoint] doubles (numeric_storage), in `file_name + ".state.npz"`.
+        The reference writes the same dataset to `.state.h5`; HDF5 is not available to this
+        package, so the container is NumPy's (h5py can copy the array into HDF5 as is)."""
+        np.savez(file_name + ".state.npz", state=self.numeric_storage())
+
+    def read_state(self, file_name):
+        """Solver::read_state (src/Solver.cpp:232-251) from write_state's file. Like the
+        reference, it restores the element storage only; call initialize() (Write_face and
+        prolongation of the restored state) before the next update."""
+        with np.load(file_name + ".state.npz") as f:
+            self.set_numeric_storage(f["state"])
+
     def close(self):
         self.ctx.close()
 
