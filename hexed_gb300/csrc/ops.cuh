@@ -112,10 +112,13 @@ struct Runner
     // 3D kernels of row size >= 6 are register-capped for more resident CTAs: 72 registers
     // per thread for the float viscous kernel and 56 for the float inviscid one (4 and 5 CTAs
     // per SM at row size 6, where shared memory allows as many), 128 for the FP64 viscous
-    // kernel (2)
+    // kernel (2). Below row size 6 the float inviscid kernel is held at 64 (4 CTAs of 256
+    // threads): at 66 registers the row-size-4 kernel lost a CTA per SM and ran 19% slower.
+    constexpr bool f32 = std::is_same<R, float>::value;
     constexpr int threads = Tile<ND, RS, EPB>::threads;
-    constexpr int cap = std::is_same<R, float>::value ? (VISC ? 72 : 56) : VISC ? 128 : 0;
-    constexpr int minb = (cap && ND == 3 && S::nq > 128 && 65536/(threads*cap) > 1) ? 65536/(threads*cap) : 1;
+    constexpr int cap = f32 ? (VISC ? 72 : S::nq > 128 ? 56 : 64) : VISC ? 128 : 0;
+    constexpr bool capped = ND == 3 && (S::nq > 128 || (f32 && !VISC));
+    constexpr int minb = (cap && capped && 65536/(threads*cap) > 1) ? 65536/(threads*cap) : 1;
     auto kern = k_local<ND, RS, R, DEF, VISC, FaceT, EPB, minb>;
     static bool configured = false;
     if (!configured) {
