@@ -459,7 +459,7 @@ int hexed_gpu_create(const hexed_mesh_desc* d, int precision, hexed_gpu_ctx** ou
         refs[e*nv_ + v] = sum/double(nq_);
       }
     if (!st) st = upload_array(&c->ref_state, refs.data(), refs.size(), "reference state");
-    if (!st && cudaMalloc((void**)&c->ref_terms, n_elem*(3*nd + 7)*sizeof(float)) != cudaSuccess)
+    if (!st && cudaMalloc((void**)&c->ref_terms, n_elem*((3*nd + 7 + 3)/4*4)*sizeof(float)) != cudaSuccess)
       st = fail(HEXED_ERR_ALLOC, "reference-term allocation failed");
     if (!st) c->ops->ref_terms(*c);
     // owners of the slots beyond the element slots: boundary ghosts take the inside element,

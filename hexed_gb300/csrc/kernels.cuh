@@ -222,7 +222,7 @@ __device__ __forceinline__ R char_speed(const R* s, R inv_mass) // pde.hpp:161-1
 // references, (s1 - s0) + (lo1 - lo0), has the relative accuracy of float whatever the
 // references' size (the face kernels convert traces between neighbouring elements with it).
 template <int ND, typename R>
-struct RefState {
+struct alignas(16) RefState {   // 16-byte aligned: read with vector loads (float: 3 nd + 7 values, padded)
   R s[ND + 2];   // conserved reference state
   R lo[ND + 2];  // ref - s (zero in double)
   R v[ND];       // its velocity

@@ -393,7 +393,8 @@ struct Runner
   // RefState terms of every element, after the reference state changed (mixed form)
   static void ref_terms(Ctx& c)
   {
-    static_assert(sizeof(RefState<ND, float>) == (3*ND + 7)*sizeof(float), "ref_terms rows are 3 nd + 7 floats");
+    static_assert(sizeof(RefState<ND, float>) == (3*ND + 7 + 3)/4*4*sizeof(float),
+                  "ref_terms rows are 3 nd + 7 floats, padded to 16 bytes");
     const int n = c.cap_car + c.n_def;
     if (c.ref_state && c.ref_terms && n > 0)
       k_ref_terms<ND><<<grid_for(n, 256), 256, 0, c.stream>>>(c.ref_state, n, reinterpret_cast<RefState<ND, float>*>(c.ref_terms));
