@@ -94,6 +94,8 @@ struct Ctx {
   bool capturing;
   // Jacobian determinant reciprocal [n_def][nq] (both forms)
   double* inv_det;
+  // contiguous staging of hexed_gpu_write_state [n_elem][nv][nq] (allocated on first use)
+  double* state_stage;
   // mixed form: FP32 face traces, residual cache and metric-normal copies, and the reference
   // state of each element [n_elem][nv] the traces and fluxes are offsets from (by default the
   // mean conserved state of the initial state)

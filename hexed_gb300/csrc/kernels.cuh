@@ -2579,6 +2579,17 @@ static __global__ void k_widen(const float* src, double* dst, long n)
 {
   for (long i = blockIdx.x*(long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x*blockDim.x) dst[i] = double(src[i]);
 }
+// Conserved rows [n][row] of a contiguous staging buffer into the element array, whose
+// elements are `pitch` doubles apart (hexed_gpu_write_state: the host copy goes to the
+// staging buffer as one contiguous transfer).
+static __global__ void k_scatter_rows(const double* stage, double* elem, long n, int row, int pitch)
+{
+  const long total = n*row;
+  for (long i = blockIdx.x*(long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x*blockDim.x) {
+    const long e = i/row, r = i%row;
+    elem[e*pitch + r] = stage[i];
+  }
+}
 static __global__ void k_inv_det(const double* jac, double* inv_det, long n_def, int nq, int n_metric)
 {
   const long n = n_def*nq;

@@ -284,8 +284,10 @@ int hexed_gpu_set_reference_state(hexed_gpu_ctx* ctx, const double* state);
 /* The conserved state of the active elements as host arrays [n_elem][nv][nq] (the first nv
  * rows of each element of the arena, without the time-step and AV rows): the copy a caller
  * whose state lives in host memory makes around each update, as the reference's elements hold
- * it (Element::state(), src/Element.cpp:119-142). One strided copy; returns when it is
- * complete. Pinned host memory gives the full transfer rate. */
+ * it (Element::state(), src/Element.cpp:119-142). Returns when the copy is complete. Pinned
+ * host memory gives the full transfer rate. write_state stages the host array in device
+ * memory (n_elem nv nq doubles, allocated on the first call) and scatters it into the
+ * arena; read_state is one strided copy. */
 int hexed_gpu_write_state(hexed_gpu_ctx* ctx, const double* state);
 int hexed_gpu_read_state(hexed_gpu_ctx* ctx, double* state);
 
