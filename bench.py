@@ -663,6 +663,14 @@ def main():
     host_out = torch.empty_like(host_in).pin_memory()
     lib = ctx.lib
     n_bytes = host_in.numel() * 8
+
+    def e2e_step():
+        # a new state from the host, its face traces (Solver::initialize), one update, read back
+        abi.check(lib.hexed_gpu_write_state(ctx.handle, abi.ctypes.cast(host_in.data_ptr(), abi.P_double)))
+        initialize(ctx)
+        ctx.update(p, read_dt=False)
+        abi.check(lib.hexed_gpu_read_state(ctx.handle, abi.ctypes.cast(host_out.data_ptr(), abi.P_double)))
+    e2e_step()   # untimed: the first write_state allocates its device staging buffer
     ctx.synchronize()
     barrier()
     torch.cuda.synchronize()
@@ -670,11 +678,7 @@ def main():
     f0.record(stream)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        # a new state from the host, its face traces (Solver::initialize), one update, read back
-        abi.check(lib.hexed_gpu_write_state(ctx.handle, abi.ctypes.cast(host_in.data_ptr(), abi.P_double)))
-        initialize(ctx)
-        ctx.update(p, read_dt=False)
-        abi.check(lib.hexed_gpu_read_state(ctx.handle, abi.ctypes.cast(host_out.data_ptr(), abi.P_double)))
+        e2e_step()
     f1.record(stream)
     torch.cuda.synchronize()
     wall_e2e = time.perf_counter() - t0

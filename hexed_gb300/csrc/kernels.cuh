@@ -312,8 +312,19 @@ struct DiffScalars { // compute_scalars_diff (pde.hpp:130-138)
     bulk_av = fabs(bulk);
     laplacian_av = fabs(lap);
     R sqrt_temp = sqrt(fmax((s[ND + 1] - c.kin_ener)*c.inv_mass, R(0))*R(heat_rat - 1)*R(1./specific_gas_air));
-    mu = transport_coef(visc, sqrt_temp);
-    R k = transport_coef(cond, sqrt_temp);
+    R k;
+    if (visc.inv_sqrt_ref_temp == cond.inv_sqrt_ref_temp && visc.ref_temp_plus_offset == cond.ref_temp_plus_offset &&
+        visc.temp_offset == cond.temp_offset) {
+      // the two models share their temperature law (Sutherland with one offset, as for air):
+      // its factor (T/T_ref)^1.5 (T_ref + S)/(T + S) once, with one division
+      const R r = sqrt_temp*R(visc.inv_sqrt_ref_temp);
+      const R law = r*r*r*R(visc.ref_temp_plus_offset)/(sqrt_temp*sqrt_temp + R(visc.temp_offset));
+      mu = R(visc.const_val) + R(visc.ref_val)*law;
+      k = R(cond.const_val) + R(cond.ref_val)*law;
+    } else {
+      mu = transport_coef(visc, sqrt_temp);
+      k = transport_coef(cond, sqrt_temp);
+    }
     energy_cond = k*R(heat_rat - 1)*R(1./specific_gas_air);
   }
 };
