@@ -118,7 +118,9 @@ def kernel_bytes(name, ar, precision="fp64"):
     nd, nq, nfq, nv = ar.n_dim, ar.nq, ar.nfq, ar.nv
     F = 2 * nd
     d, w = 8, (4 if precision == "mixed" else 8)
-    metric = w * nd * nd * nq + d * nq
+    # deformed metrics: the normals and 1/J (FP64 form); the float normals with their
+    # determinant row, from which the mixed volume kernel forms 1/J (mixed form)
+    metric = w * (nd * nd + 1) * nq if precision == "mixed" else w * nd * nd * nq + d * nq
     per_elem = {
         "local_car_euler": d * (2 * nv + 1) * nq + w * nv * nq + w * 2 * F * nv * nfq,
         "local_def_euler": d * (2 * nv + 1) * nq + w * nv * nq + w * 2 * F * nv * nfq + metric,

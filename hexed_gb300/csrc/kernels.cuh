@@ -44,8 +44,9 @@ struct Tab {
 // Device view of the arena (include/hexed_gpu.h). `face` is stored as FaceT.
 // Device view of the arena. FaceT is the storage type of the face traces, the residual cache
 // and the metric normals the flux kernels read: double in the FP64 form; float in the mixed
-// form, where those arrays are FP32 copies (the FP64 metrics stay in `jac`, and the Jacobian
-// determinant enters the stage update through the FP64 `inv_det`).
+// form, where those arrays are FP32 copies (the FP64 metrics stay in `jac`). The FP64 form's
+// stage update multiplies by the FP64 `inv_det`; the mixed form's volume kernel forms 1/det
+// in float from the determinant row of its staged normals.
 template <typename FaceT>
 struct Dev {
   int n_car, n_def, n_elem, n_slot, n_car_con, n_def_con, n_bc_con, n_ref;
@@ -653,7 +654,8 @@ __device__ __forceinline__ void prefetch_element_arrays(const Dev<FaceT>& m, int
   if constexpr (DEF) {
     const size_t ed0 = (size_t)(e0 - m.n_car);
     prefetch_l2(m.nrm + ed0*(ND*ND + 1)*nq, sizeof(FaceT)*(size_t)n_here*(ND*ND + 1)*nq);
-    prefetch_l2(m.inv_det + ed0*nq, sizeof(double)*(size_t)n_here*nq);
+    // the float form takes the determinant from the staged normals' last row instead
+    if constexpr (std::is_same<FaceT, double>::value) prefetch_l2(m.inv_det + ed0*nq, sizeof(double)*(size_t)n_here*nq);
     if constexpr (VISC) prefetch_l2(m.face_nrml + ed0*2*ND*ND*nfq, sizeof(FaceT)*(size_t)n_here*2*ND*ND*nfq);
   }
 }
@@ -1267,7 +1269,7 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
     if (!(bulk_n && staged) && active) {
       const FaceT* nr = m.nrm + (size_t)ed*(ND*ND + 1)*nq;
       #pragma unroll
-      for (int k = 0; k < ND*ND; ++k) s_n[(le*(ND*ND + 1) + k)*nq + q] = R(nr[k*nq + q]);
+      for (int k = 0; k <= ND*ND; ++k) s_n[(le*(ND*ND + 1) + k)*nq + q] = R(nr[k*nq + q]);   // normals, determinant
     }
   }
   // comp.normal(j, i) of this thread's point, in shared memory (deformed elements)
@@ -1405,7 +1407,8 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
     }
     if constexpr (VISC) {
       R g[nv][ND];
-      const R inv_det = DEF ? to_R<R>(m.inv_det[(size_t)ed*nq + q]) : R(1);
+      // 1/det from the staged normals' determinant row (float; no double array read)
+      const R inv_det = DEF ? R(1)/s_n[(le*(ND*ND + 1) + ND*ND)*nq + q] : R(1);
       #pragma unroll
       for (int v = 0; v < nv; ++v)
         #pragma unroll
@@ -1562,7 +1565,7 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
       // is a double add. The offset-form trace of the new state is the old one plus the
       // increment.
       R mult = to_R<R>(update_coef)*to_R<R>(tss)*inv_dpos_r;
-      if constexpr (DEF) mult *= to_R<R>(m.inv_det[(size_t)ed*nq + q]);
+      if constexpr (DEF) mult *= R(1)/s_n[(le*(ND*ND + 1) + ND*ND)*nq + q];
       #pragma unroll
       for (int v = 0; v < nv; ++v) {
         R ur = rate[v];
