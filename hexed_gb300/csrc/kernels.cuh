@@ -1203,6 +1203,9 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
 {
   using S = Shape<ND, RS>;
   constexpr int nq = S::nq, nfq = S::nfq, nv = S::nv;
+  // the CTA size k_local is launched with (its launch bound): task loops stride by a constant,
+  // so one whose tasks fit in a CTA compiles to a single guarded pass
+  constexpr int kThreads = Tile<ND, RS, EPB>::threads;
   // Mixed form: traces and convective fluxes are offsets from the element's reference state
   // (flux_delta). The reference flux's parts of interior and face fluxes cancel by the discrete
   // metric identity sum_d [D.n_d + lift.(n_face - B.n_d)] = 0 (free-stream preservation), so
@@ -1305,7 +1308,7 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
       __syncthreads();
       // grad[v][d] along each row: D.u + lift.(face LDG state - B.u), over 1/size
       constexpr int per_d = EPB*nv*nfq;
-      for (int t = threadIdx.x; t < ND*per_d; t += blockDim.x) {
+      for (int t = threadIdx.x; t < ND*per_d; t += kThreads) {
         const int d = t/per_d, rem = t - d*per_d;
         const int r = rem%nfq, rest = rem/nfq;
         const int v = rest%nv, l = rest/nv;
@@ -1340,7 +1343,7 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
         __syncthreads();   // d = 0: s_u and s_n complete; d > 0: the previous dimension's tasks are done
         constexpr int stride = S::stride(d);
         constexpr int n_task = EPB*nv*nfq;
-        for (int t = threadIdx.x; t < n_task; t += blockDim.x) {
+        for (int t = threadIdx.x; t < n_task; t += kThreads) {
           const int r = t%nfq, rest = t/nfq;
           const int v = rest%nv, l = rest/nv;
           const int ee = e0 + l;
@@ -1434,7 +1437,7 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
     __syncthreads();
     constexpr int stride = S::stride(d);
     constexpr int n_task = EPB*nv*nfq;
-    for (int t = threadIdx.x; t < n_task; t += blockDim.x) {
+    for (int t = threadIdx.x; t < n_task; t += kThreads) {
       const int r = t%nfq, rest = t/nfq;
       const int v = rest%nv, l = rest/nv;
       const int ee = e0 + l;
@@ -1497,7 +1500,7 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
       }
       __syncthreads();
       constexpr int stride = S::stride(d);
-      for (int t = threadIdx.x; t < EPB*nf*nfq; t += blockDim.x) {
+      for (int t = threadIdx.x; t < EPB*nf*nfq; t += kThreads) {
         const int r = t%nfq, rest = t/nfq;
         const int v = rest%nf, l = rest/nf;
         R* row = s_x + (l*nf + v)*nq + row_base<ND, RS, d>(r);
