@@ -103,6 +103,9 @@ struct Shape {
   static __host__ __device__ constexpr int stride(int d) { return ipow(RS, ND - 1 - d); }
 };
 
+// Threads of a volume-kernel CTA holding EPB elements (whole warps).
+template <int ND, int RS, int EPB>
+struct Tile { static constexpr int threads = (EPB*ipow(RS, ND) + 31)/32*32; };
 template <typename T> __device__ __forceinline__ T load(const T* p) { return __ldg(p); }
 
 // ------------------------------------------------------------------- conversions (mixed form)
@@ -544,19 +547,23 @@ __device__ __forceinline__ void write_faces_from_smem(const Dev<FaceT>& m, const
   using S = Shape<ND, RS>;
   constexpr int nq = S::nq, nfq = S::nfq, nv = S::nv;
   constexpr int per_d = EPB*nv*nfq;
-  for (int t = threadIdx.x; t < ND*per_d; t += blockDim.x) {
+  // callers launch Tile<ND, RS, EPB>::threads threads (k_local, k_reconcile_ldg): a constant
+  // stride, and 32-bit offsets from the CTA's first element's face slots
+  constexpr int kThreads = Tile<ND, RS, EPB>::threads;
+  FaceT* const face_cta = m.face + (size_t)e0*2*ND*S::slot_dof;
+  for (int t = threadIdx.x; t < ND*per_d; t += kThreads) {
     const int d = t/per_d, rem = t - d*per_d;
     const int r = rem%nfq, rest = rem/nfq;
     const int v = rest%nv, le = rest/nv;
     const int e = e0 + le;
-    if (e >= e_end) continue;
+    if (EPB > 1 && e >= e_end) continue;
     dim_switch<ND>(d, [&](auto dc) {
       constexpr int D = decltype(dc)::value;
       R x[RS];
       load_row<RS, S::stride(D)>(s_u + (le*nv + v)*nq + row_base<ND, RS, D>(r), x);
       R a0, a1;
       bound_dot(rt, x, a0, a1);
-      FaceT* f0 = m.face + (size_t)(e*2*ND + 2*D)*S::slot_dof + v*nfq + r;
+      FaceT* f0 = face_cta + (le*2*ND + 2*D)*S::slot_dof + v*nfq + r;
       f0[0] = FaceT(a0);
       f0[S::slot_dof] = FaceT(a1);   // slot of face 2d + 1
     });
@@ -765,9 +772,6 @@ struct LocalDt {
   double dt;
 };
 
-// Threads of a volume-kernel CTA holding EPB elements (whole warps).
-template <int ND, int RS, int EPB>
-struct Tile { static constexpr int threads = (EPB*ipow(RS, ND) + 31)/32*32; };
 
 // Offset form of the state used for face traces and derivatives: the mixed form subtracts the
 // element's reference state (in double, before narrowing), so the FP32 values carry the
@@ -1226,6 +1230,10 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
   const int le = threadIdx.x/nq;
   const int q = threadIdx.x%nq;
   const int e0 = e_begin + blockIdx.x*EPB;
+  // the CTA's first element's face slots and (deformed) face normals: row tasks address their
+  // element's rows from these with 32-bit offsets
+  FaceT* const face_cta = m.face + (size_t)e0*2*ND*S::slot_dof;
+  const FaceT* const fnrml_cta = DEF ? m.face_nrml + (size_t)(e0 - m.n_car)*2*ND*ND*nfq : nullptr;
   const int e = e0 + le;
   const bool active = threadIdx.x < EPB*nq && e < e_end;
   const int n_here = min(EPB, e_end - e0);
@@ -1313,7 +1321,7 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
         const int r = rem%nfq, rest = rem/nfq;
         const int v = rest%nv, l = rest/nv;
         const int ee = e0 + l;
-        if (ee >= e_end) continue;
+        if (EPB > 1 && ee >= e_end) continue;   // one element per CTA: always in range
         dim_switch<ND>(d, [&](auto dc) {
           constexpr int D = decltype(dc)::value;
           constexpr int stride = S::stride(D);
@@ -1322,7 +1330,7 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
           load_row<RS, stride>(s_u + (l*nv + v)*nq + base, x);
           R a0, a1;
           bound_dot(rt, x, a0, a1);
-          const FaceT* fl = m.face + (size_t)(ee*2*ND + 2*D)*S::slot_dof + nv*nfq + v*nfq + r;
+          const FaceT* fl = face_cta + (l*2*ND + 2*D)*S::slot_dof + nv*nfq + v*nfq + r;
           const R b0 = R(fl[0]) - a0, b1 = R(fl[S::slot_dof]) - a1;
           const R idp = s_idp[l];
           R* g = s_g + ((l*ND + D)*nv + v)*nq + base;
@@ -1347,13 +1355,13 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
           const int r = t%nfq, rest = t/nfq;
           const int v = rest%nv, l = rest/nv;
           const int ee = e0 + l;
-          if (ee >= e_end) continue;
+          if (EPB > 1 && ee >= e_end) continue;   // one element per CTA: always in range
           const int base = row_base<ND, RS, d>(r);
           R xu[RS];
           load_row<RS, stride>(s_u + (l*nv + v)*nq + base, xu);
-          const FaceT* fl = m.face + (size_t)(ee*2*ND + 2*d)*S::slot_dof + nv*nfq + v*nfq + r;
+          const FaceT* fl = face_cta + (l*2*ND + 2*d)*S::slot_dof + nv*nfq + v*nfq + r;
           const R fl0 = R(fl[0]), fl1 = R(fl[S::slot_dof]);
-          const FaceT* fnr = m.face_nrml + ((size_t)(ee - m.n_car)*2*ND + 2*d)*ND*nfq + r;
+          const FaceT* fnr = fnrml_cta + (l*2*ND + 2*d)*ND*nfq + r;
           const R idp = s_idp[l];
           #pragma unroll
           for (int j = 0; j < ND; ++j) {
@@ -1441,13 +1449,13 @@ __device__ __forceinline__ void local_body_rows(Dev<FaceT> m, const Tab<RS>& tab
       const int r = t%nfq, rest = t/nfq;
       const int v = rest%nv, l = rest/nv;
       const int ee = e0 + l;
-      if (ee >= e_end) continue;
+      if (EPB > 1 && ee >= e_end) continue;   // one element per CTA: always in range
       const int base = row_base<ND, RS, d>(r);
       R x[RS];
       load_row<RS, stride>(s_x + ((l*ND + d)*nv + v)*nq + base, x);
       R a0, a1;
       bound_dot(rt, x, a0, a1);
-      FaceT* fl = m.face + (size_t)(ee*2*ND + 2*d)*S::slot_dof + v*nfq + r;
+      FaceT* fl = face_cta + (l*2*ND + 2*d)*S::slot_dof + v*nfq + r;
       // Fix_therm_admis: no convective flux, in the faces as in the volume
       const bool conv = !(VISC && m.fta);
       const R b0 = (conv ? R(fl[0]) : R(0)) - a0, b1 = (conv ? R(fl[S::slot_dof]) : R(0)) - a1;
