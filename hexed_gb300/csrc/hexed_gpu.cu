@@ -112,6 +112,14 @@ int validate(const hexed_mesh_desc* d)
     return fail(HEXED_ERR_INVALID, "negative count in mesh descriptor");
   const long n_elem = (long)d->n_car_elem + d->n_def_elem;
   if (n_elem == 0) return fail(HEXED_ERR_INVALID, "mesh has no elements");
+  // the face kernels and Max_dt index face points and points with 32-bit unsigned integers
+  long nfq = 1;
+  for (int i = 1; i < d->n_dim; ++i) nfq *= d->row_size;
+  const long n_con = (long)d->n_car_con + d->n_def_con + d->n_bc_con;
+  if (n_con*nfq >= (1L << 31))
+    return fail(HEXED_ERR_INVALID, "%ld connections of %ld face points each: over 2^31 face points", n_con, nfq);
+  if (n_elem*nfq*d->row_size >= (1L << 31))   // Max_dt indexes quadrature points the same way
+    return fail(HEXED_ERR_INVALID, "%ld elements of %ld points each: over 2^31 points", n_elem, nfq*d->row_size);
   if (d->n_slot < n_elem*2*d->n_dim) return fail(HEXED_ERR_INVALID, "n_slot %d < 2*n_dim*n_elem", d->n_slot);
   auto slot_ok = [&](int s) { return s >= 0 && s < d->n_slot; };
   for (int i = 0; i < d->n_car_con; ++i) {
