@@ -127,7 +127,8 @@ def kernel_bytes(name, ar, precision="fp64"):
         "local_car_ns": d * (2 * nv + 3) * nq + w * nv * nq + w * 3 * F * nv * nfq,
         "local_def_ns": d * (2 * nv + 3) * nq + w * nv * nq + w * 3 * F * nv * nfq + metric + w * F * nd * nfq,
         "reconcile_ldg_car": d * (2 * nv + 1) * nq + w * 2 * F * nv * nfq,
-        "reconcile_ldg_def": d * (2 * nv + 2) * nq + w * 2 * F * nv * nfq,
+        # 1/J: the FP64 array (FP64 form), the float normals' determinant row (mixed form)
+        "reconcile_ldg_def": d * (2 * nv + 1) * nq + w * nq + w * 2 * F * nv * nfq,
         "max_dt": d * (nv + 3) * nq + w * 2 ** nd,   # the mixed form reads float vertex scales
     }
     if name in per_elem:

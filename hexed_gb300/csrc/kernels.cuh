@@ -1723,7 +1723,8 @@ k_reconcile_ldg(Dev<FaceT> m, Tab<RS> tab, RowTab<RS, R> rt, int e_begin, int e_
     } else {
       // mixed form: increment in float, accumulated into the double state (see k_local)
       R mult = to_R<R>(dt)*to_R<R>(st_w[nv*nq + q])*(R(1)/to_R<R>(m.nom_size[e]));
-      if constexpr (DEF) mult *= to_R<R>(m.inv_det[(size_t)(e - m.n_car)*nq + q]);
+      // 1/det from the float normals' determinant row (4 bytes per point, no conversion)
+      if constexpr (DEF) mult *= R(1)/R(m.nrm[((size_t)(e - m.n_car)*(ND*ND + 1) + ND*ND)*nq + q]);
       if (compute_residual) {
         FaceT* rc = m.rcache + (size_t)e*nv*nq;
         #pragma unroll
