@@ -476,7 +476,6 @@ struct Runner
     const int g_pts = grid_for(n_pts, 256);
     const long n_face_pts = (long)(m.n_car_con + m.n_def_con + m.n_bc_con)*SS::nfq;
     const int g_con = grid_for(n_face_pts, 256);
-    const int g_bc = grid_for((long)m.n_bc_con*SS::nfq, 256);
     constexpr int blk = SS::block;   // the volume kernels' launch bound
     constexpr size_t smem_adv = SavAdvSmem<ND, RS>::bytes;
     constexpr size_t smem_diff = SavDiffSmem<ND, RS>::bytes;
@@ -505,8 +504,7 @@ struct Runner
         sav_refine<SS::n_adv_extrap>(c, m, t, true, false, false);
       }
       for (int stage = 0; stage < 2; ++stage) {
-        if (m.n_bc_con) k_sav_bc_advection<ND, RS><<<g_bc, 256, 0, c.stream>>>(m);
-        if (n_face_pts) {
+        if (n_face_pts) {   // boundary ghosts included (sav_bc_advection_point)
           ProfScope ps(c, "sav_neighbor_advection");
           k_sav_neighbor_advection<ND, RS><<<g_con, 256, 0, c.stream>>>(m, st);
         }
@@ -540,8 +538,7 @@ struct Runner
       for (int i_cheby = 0; i_cheby < p.n_cheby; ++i_cheby) {
         // math::chebyshev_step (src/math.cpp:104-107)
         const double s = 1/(1 - std::cos((p.n_cheby - i_cheby - 0.5)*3.14159265358979323846/p.n_cheby));
-        if (m.n_bc_con) k_sav_bc_diffusion<ND, RS><<<g_bc, 256, 0, c.stream>>>(m, 0);
-        if (n_face_pts) {
+        if (n_face_pts) {   // boundary ghosts included (sav_bc_diffusion_point)
           ProfScope ps(c, "sav_neighbor_ldg");
           k_sav_neighbor_ldg<ND, RS><<<g_con, 256, 0, c.stream>>>(m, 0);
         }
@@ -552,7 +549,6 @@ struct Runner
           k_sav_local_diffusion<ND, RS><<<n_elem, blk, smem_diff, c.stream>>>(m, st, s, diff_time);
         }
         sav_refine<SS::n_sav>(c, m, t, true, true, true);
-        if (m.n_bc_con) k_sav_bc_diffusion<ND, RS><<<g_bc, 256, 0, c.stream>>>(m, 1);
         if (n_face_pts) {
           ProfScope ps(c, "sav_neighbor_ldg");
           k_sav_neighbor_ldg<ND, RS><<<g_con, 256, 0, c.stream>>>(m, 1);

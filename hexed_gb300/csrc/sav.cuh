@@ -189,15 +189,15 @@ __global__ void k_sav_refine(SavDev m, Tab<RS> tab, int scale, int offset)
 }
 
 // Flow_bc::apply_advection and its overrides (src/Boundary_condition.cpp:24-41, 346-368,
-// 429-448, 460-463); one thread per boundary face point.
+// 429-448, 460-463) at face point q of boundary connection i: the ghost from the inside at the
+// same point. Run by k_sav_neighbor_advection's thread for that point just before its flux
+// (a boundary connection's faces are not permuted), so it needs no launch of its own.
 template <int ND, int RS>
-__global__ void k_sav_bc_advection(SavDev m)
+__device__ __forceinline__ void sav_bc_advection_point(const SavDev& m, int i, int q)
 {
   using S = SavShape<ND, RS>;
   constexpr int nfq = S::nfq;
-  const long total = (long)m.n_bc_con*nfq;
-  for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
-    const int i = int(t/nfq), q = int(t%nfq);
+  {
     const int* c = m.bc_con + 4*i;
     const hexed_bc_spec& b = m.bc_spec[c[3]];
     const double* in = S::slot(m, c[0], false);
@@ -269,6 +269,8 @@ __global__ void k_sav_neighbor_advection(SavDev m, SavTab<RS> tab)
     int s0, s1, dir;
     const double* nrml = sav_connection(m, ND, nfq, int(t/nfq), s0, s1, dir);
     const int q = int(t%nfq);
+    const int i_bc = int(t/nfq) - m.n_car_con - m.n_def_con;
+    if (i_bc >= 0) sav_bc_advection_point<ND, RS>(m, i_bc, q);   // the ghost first
     const bool deformed = nrml != nullptr;
     int sign0 = 1, sign1 = 1;
     if (deformed) {
@@ -474,20 +476,17 @@ __global__ void k_sav_project(SavDev m, AvTab<RS, double> wo)
 }
 
 // Flow_bc::apply_diffusion (ghost state = inside, src/Boundary_condition.cpp:43-52) or
-// flux_diffusion (ghost LDG flux = -inside, :54-60) over nv face variables.
+// flux_diffusion (ghost LDG flux = -inside, :54-60) over nv face variables, at face point q of
+// boundary connection i; run by k_sav_neighbor_ldg's thread for that point first.
 template <int ND, int RS>
-__global__ void k_sav_bc_diffusion(SavDev m, int flux)
+__device__ __forceinline__ void sav_bc_diffusion_point(const SavDev& m, int i, int q, int flux)
 {
   using S = SavShape<ND, RS>;
   constexpr int nfq = S::nfq;
-  const long total = (long)m.n_bc_con*nfq;
-  for (long t = blockIdx.x*(long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x*blockDim.x) {
-    const int i = int(t/nfq), q = int(t%nfq);
-    const int* c = m.bc_con + 4*i;
-    const double* in = S::slot(m, c[0], flux);
-    double* gh = S::slot(m, c[1], flux);
-    for (int v = 0; v < S::nv; ++v) gh[v*nfq + q] = flux ? -in[v*nfq + q] : in[v*nfq + q];
-  }
+  const int* c = m.bc_con + 4*i;
+  const double* in = S::slot(m, c[0], flux);
+  double* gh = S::slot(m, c[1], flux);
+  for (int v = 0; v < S::nv; ++v) gh[v*nfq + q] = flux ? -in[v*nfq + q] : in[v*nfq + q];
 }
 
 // Spatial<pde::Smooth_art_visc>::Neighbor (reconcile = 0: the LDG average of the three traces
@@ -502,6 +501,8 @@ __global__ void k_sav_neighbor_ldg(SavDev m, int reconcile)
     int s0, s1, dir;
     const double* nrml = sav_connection(m, ND, nfq, int(t/nfq), s0, s1, dir);
     const int q = int(t%nfq);
+    const int i_bc = int(t/nfq) - m.n_car_con - m.n_def_con;
+    if (i_bc >= 0) sav_bc_diffusion_point<ND, RS>(m, i_bc, q, reconcile);   // the ghost first
     const bool deformed = nrml != nullptr;
     const int q1 = deformed ? perm_index<ND, RS>(dir, q) : q;
     double* l0 = S::slot(m, s0, true);
