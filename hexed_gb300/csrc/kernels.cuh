@@ -1879,7 +1879,7 @@ __device__ __forceinline__ void for_face_points(int n_con, F&& f)
 // connection's record of 3 ints (slot, slot, orientation) from `con`. Each iteration loads
 // the next iteration's record before it works its own face point, so that the gathers of
 // the next iteration do not first wait for their record's load (float face kernels: 0.093
-// -> 0.090 ms per Neighbor launch on the 32^3 Taylor-Green mesh, at 63 registers instead of
+// -> 0.090 ms per Neighbor launch on the 32^3 Taylor-Green mesh, at 64 registers instead of
 // 56, still 4 CTAs of 256 per SM).
 template <int NFQ, typename F>
 __device__ __forceinline__ void for_face_records(int n_con, const int* con, F&& f)
